@@ -1,0 +1,436 @@
+#!/usr/bin/env python
+"""Throughput/latency benchmark of the Shack-Hartmann WFS step.
+
+Workload (one GPU): the 74x74-subaperture ELT NGS sensor -- 39 m pupil with
+0.28 central obstruction (3972 lit subapertures), phasesize 10, fftsize 20,
+clipsize 20, nimg 10, 2-D Gaussian spot PSF of FWHM 1.5 FFT pixels, 500
+photons/subaperture, Poisson shot noise, 3 e- read noise, sky 10 e-/px,
+threshold 6 (2 sigma) -- on seeded synthetic von Karman phase screens
+(r0 0.157 m at 500 nm, L0 25 m, lambda 589 nm, 740x740 px).
+
+A step is one batch of F independent frames through the fused kernel with
+the phase already in HBM (``value``).  ``e2e`` is the same metric through the
+reference-facing call (``centcmod.run`` -> ``shwfs_run``) with host phase and
+host outputs, one synchronous frame at a time, which also gives the per-frame
+latency percentiles.  ``--impl reference`` times the CPU implementation of
+the path on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(name="elt74x74_ngs_psf_noisy", nsubx=74, p=10, N=20, C=20, m=10, ncen=10, obs=0.28, Dtel=39.0,
+                r0=0.157, L0=25.0, wavelength=589.0, psf_fwhm=1.5, sig=500.0, addPoisson=1, readnoise=3.0,
+                readbg=0.0, sky=10.0, floor=6.0, threshType=0)
+METRIC = "SH WFS subap-frames/s (74x74 NGS, fftsize 20, Gaussian spot PSF, Poisson+read noise)"
+UNIT = "subap-frames/s"
+FPSTEP = 64  # frames per step
+
+
+# ---------------------------------------------------------------- inputs
+
+def make_pupil():
+    from dasp_gb300.tel import Pupil
+    w = WORKLOAD
+    npup = w["nsubx"] * w["p"]
+    return Pupil(npup, npup / 2.0, npup / 2.0 * w["obs"])
+
+
+def make_screens(n, seed0=1000):
+    from dasp_gb300.screens import von_karman_screen
+    w = WORKLOAD
+    npup = w["nsubx"] * w["p"]
+    return [von_karman_screen(npup, w["Dtel"], w["r0"], w["L0"], seed0 + s, w["wavelength"]) for s in range(n)]
+
+
+def make_frames(screens, nframes, seed):
+    """nframes distinct frames from a few screens: flips, transposes, rolls."""
+    rng = np.random.default_rng(seed)
+    out = np.empty((nframes,) + screens[0].shape, np.float32)
+    for f in range(nframes):
+        s = screens[f % len(screens)]
+        if rng.random() < 0.5:
+            s = s[::-1]
+        if rng.random() < 0.5:
+            s = s.T
+        out[f] = np.roll(s, (int(rng.integers(0, 740)), int(rng.integers(0, 740))), axis=(0, 1))
+    return out
+
+
+def make_engine(pup, phs, cents, bimg, noiseless=False):
+    from dasp_gb300.centcmod import centcmod
+    from dasp_gb300.screens import gaussian_psf
+    w = WORKLOAD
+    psf = gaussian_psf(w["C"], w["psf_fwhm"])
+    return centcmod(8, w["nsubx"], w["ncen"], w["N"], w["C"], w["m"], w["p"],
+                    0.0 if noiseless else w["readnoise"], w["readbg"], 0 if noiseless else w["addPoisson"],
+                    w["floor"], w["sig"], w["sky"], 0, 1.0, 1, 0, 1234, phs, pup, psf, cents, bimg, 0.5, 0, None,
+                    0, 0.0, None, None, w["threshType"], 0, 0, 1, 0, None)
+
+
+# ---------------------------------------------------------------- algorithmic work
+
+def algorithmic_per_subap():
+    """Per lit subap-frame: flops (F_alg) and bytes (B_alg).
+
+    F_alg = 6p^2 + 10 N^2 log2 N + 3c^2 + [10 P^2 log2 P + 6 P (P/2+1)] + C^2 + 3 m^2
+    B_alg = 4p^2 (phase in) + 4m^2 (image out) + 8 (centroids out)
+    """
+    w = WORKLOAD
+    p, N, C, m, P = w["p"], w["N"], w["C"], w["m"], w["C"]
+    c = min(N, P)
+    F = 6 * p * p + 10 * N * N * np.log2(N) + 3 * c * c + 10 * P * P * np.log2(P) + 6 * P * (P // 2 + 1) \
+        + C * C + 3 * m * m
+    B = 4 * p * p + 4 * m * m + 8
+    return float(F), float(B)
+
+
+# ---------------------------------------------------------------- clocks
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- distributed
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def reduce_max(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ---------------------------------------------------------------- CPU baseline
+
+def cpu_sample(frames, nthreads=1, seed=0):
+    """Time the CPU restatement of the path (the oracle) on ``frames`` frames."""
+    from oracle.shwfs_oracle import CentOracle
+    from dasp_gb300.screens import gaussian_psf
+    w = WORKLOAD
+    pup = make_pupil()
+    nsx, p = w["nsubx"], w["p"]
+    orc = CentOracle(nsubx=nsx, phasesize=p, fftsize=w["N"], clipsize=w["C"], nimg=w["m"], ncen=w["ncen"],
+                     pupfn=pup.perSubap(nsx, 0), subflag=pup.getSubapFlag(nsx, 0.5),
+                     fracSubArea=(pup.getSubarea(nsx) / (p * p)).astype(np.float32), sig=w["sig"],
+                     readnoise=w["readnoise"], readbg=w["readbg"], addPoisson=w["addPoisson"],
+                     noiseFloor=w["floor"], skybrightness=w["sky"], seed=1234 + seed, nthreads=nthreads,
+                     spotpsf=gaussian_psf(w["C"], w["psf_fwhm"]), threshType=w["threshType"])
+    screens = make_screens(2, 5000 + seed)
+    cents = np.zeros(nsx * nsx * 2, np.float32)
+    bimg = np.zeros((nsx * nsx, w["m"], w["m"]), np.float32)
+    t0 = time.perf_counter()
+    for f in range(frames):
+        orc.run(screens[f % 2], cents, bimg)
+    return time.perf_counter() - t0, int(orc.subflag.sum())
+
+
+def _cpu_worker(args):
+    frames, seed = args
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    dt, nlit = cpu_sample(frames, 1, seed)
+    return dt, nlit, frames
+
+
+def cpu_parallel(frames_per_worker, workers):
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(workers) as pool:
+        t0 = time.perf_counter()
+        res = pool.map(_cpu_worker, [(frames_per_worker, i) for i in range(workers)])
+        wall = time.perf_counter() - t0
+    nlit = res[0][1]
+    total = sum(r[2] for r in res)
+    return wall, nlit, total
+
+
+def accuracy_vs_fp64(eng_cents, phs):
+    """Noiseless centroid error of the engine vs the float64 oracle (px)."""
+    from oracle.shwfs_oracle import CentOracle
+    from dasp_gb300.screens import gaussian_psf
+    w = WORKLOAD
+    pup = make_pupil()
+    nsx, p = w["nsubx"], w["p"]
+    orc = CentOracle(nsubx=nsx, phasesize=p, fftsize=w["N"], clipsize=w["C"], nimg=w["m"], ncen=w["ncen"],
+                     pupfn=pup.perSubap(nsx, 0), subflag=pup.getSubapFlag(nsx, 0.5),
+                     fracSubArea=(pup.getSubarea(nsx) / (p * p)).astype(np.float32), sig=w["sig"],
+                     noiseFloor=w["floor"], skybrightness=w["sky"], spotpsf=gaussian_psf(w["C"], w["psf_fwhm"]),
+                     threshType=w["threshType"], mode="f64")
+    cents = np.zeros(nsx * nsx * 2, np.float32)
+    bimg = np.zeros((nsx * nsx, w["m"], w["m"]), np.float32)
+    orc.run(phs, cents, bimg)
+    return float(np.abs(cents - eng_cents.reshape(-1)).max())
+
+
+# ---------------------------------------------------------------- reference arm
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    fpw = 1
+    for _ in range(args.warmup):
+        cpu_parallel(fpw, cores)
+    walls = []
+    total_sf = 0.0
+    for _ in range(args.steps):
+        wall, nlit, total = cpu_parallel(fpw, cores)
+        walls.append(wall)
+        total_sf += nlit * total
+    t = sum(walls)
+    v = total_sf / t
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic seeded von Karman screens",
+            "config": {"workload": WORKLOAD["name"], "frames_per_step": fpw * cores},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "%d frames per step (one per core, spawn pool), numpy/C restatement of "
+                                       "centroidsFromPhase with the reference's noise streams" % (fpw * cores)},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- our arm
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--frames", type=int, default=FPSTEP, help="frames per step")
+    ap.add_argument("--e2e-frames", type=int, default=400)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+
+    if args.impl == "reference":
+        if ws > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+        run_reference(args, ws, rank)
+        return
+
+    import torch
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        torch.cuda.set_device(0)
+    from dasp_gb300 import build
+    build.build()
+
+    w = WORKLOAD
+    pup = make_pupil()
+    nsx = w["nsubx"]
+    W = nsx * w["p"]
+    nsub = nsx * nsx
+    screens = make_screens(16, 1000 + 97 * rank)
+    F = args.frames
+    batches = [torch.from_numpy(make_frames(screens, F, 10 * rank + b)).cuda() for b in range(2)]
+    dc = torch.zeros((F, nsub * 2), device="cuda")
+    db = torch.zeros((F, nsub, w["m"], w["m"]), device="cuda")
+
+    # engine bound to a host phase frame and host outputs (reference-facing path)
+    host_phs = np.ascontiguousarray(screens[0])
+    host_c = np.zeros(nsub * 2, np.float32)
+    host_b = np.zeros((nsx, nsx, w["m"], w["m"]), np.float32)
+    eng = make_engine(pup, host_phs, host_c, host_b)
+    info = eng.info()
+    nlit = info["nlit"]
+
+    stream = torch.cuda.Stream()
+    # warm-up
+    with torch.cuda.stream(stream):
+        for k in range(args.warmup):
+            eng.run_batch(batches[k % 2], dc, db, stream=stream)
+    stream.synchronize()
+    barrier(ws)
+    torch.cuda.synchronize()
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            t_start.record(stream)
+            for k in range(args.steps):
+                ev[k][0].record(stream)
+                eng.run_batch(batches[k % 2], dc, db, stream=stream)
+                ev[k][1].record(stream)
+            t_end.record(stream)
+        stream.synchronize()
+    torch.cuda.synchronize()
+    barrier(ws)
+    total_ms = t_start.elapsed_time(t_end)
+    total_ms = reduce_max(total_ms, ws)
+    per_launch_ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    ms_per_step = total_ms / args.steps
+    value = ws * nlit * F * args.steps / (total_ms / 1e3)
+
+    # e2e through the reference-facing call: host phase in, host cents/bimg out
+    host_frames = make_frames(screens, 8, 99 + rank)
+    lat = []
+    for k in range(3):
+        host_phs[...] = host_frames[k % 8]
+        eng.run(0)
+    barrier(ws)
+    t0 = time.perf_counter()
+    for k in range(args.e2e_frames):
+        host_phs[...] = host_frames[k % 8]
+        t1 = time.perf_counter()
+        eng.run(0)
+        lat.append(time.perf_counter() - t1)
+    e2e_s = time.perf_counter() - t0
+    e2e_s = reduce_max(e2e_s, ws)
+    e2e_value = ws * nlit * args.e2e_frames / e2e_s
+    lat_ms = np.array(lat) * 1e3
+
+    F_alg, B_alg = algorithmic_per_subap()
+    bytes_per_launch = B_alg * nlit * F
+    hbm_gbs = bytes_per_launch / (per_launch_ms / 1e3) / 1e9
+    flops_per_launch = F_alg * nlit * F
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            peaks = json.load(fh)
+        peak_src = "measured"
+    except Exception:
+        peak_src = "fallback"
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    sm_count = torch.cuda.get_device_properties(0).multi_processor_count
+    clocks = clk.summary()
+    fp32_peak_tf = sm_count * 128 * 2 * (clocks["sm_max_mhz"] or 2070.0) * 1e6 / 1e12
+    if rank != 0:
+        eng.free()
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic: seeded von Karman phase screens (r0 0.157 m @500 nm, L0 25 m, 589 nm)",
+        "config": {"workload": w["name"], "nsubx": nsx, "lit_subaps": nlit, "phasesize": w["p"], "fftsize": w["N"],
+                   "clipsize": w["C"], "nimg": w["m"], "psf": "2-D Gaussian FWHM 1.5 px (20x20)",
+                   "noise": "Poisson + 3 e- read noise, sky 10, floor 6 (counter-based streams)",
+                   "frames_per_step": F, "replicas": ws,
+                   "l2": "inputs larger than L2: two rotating %d-frame phase batches of %.0f MB"
+                         % (F, F * W * W * 4 / 1e6),
+                   "tile_subaps": info["tile_subaps"], "smem_bytes": info["smem_bytes"],
+                   "grid_ctas_per_frame": info["grid_ctas"]},
+        "roofline": {"bound": "hbm", "achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": hbm_gbs / hbm_peak, "traffic": None, "peak_source": peak_src,
+                     "algorithmic_bytes_per_subap_frame": B_alg, "kernel_ms_per_launch": per_launch_ms},
+        "fp32_compute": {"achieved_tflops": flops_per_launch / (per_launch_ms / 1e3) / 1e12,
+                         "peak_tflops": fp32_peak_tf, "frac": flops_per_launch / (per_launch_ms / 1e3) / 1e12 / fp32_peak_tf,
+                         "algorithmic_flops_per_subap_frame": F_alg,
+                         "peak_basis": "SMs x 128 FP32 lanes x 2 x max SM clock"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(W * W * 4),
+                "d2h_bytes_per_step": int(nsub * 2 * 4 + nsub * w["m"] * w["m"] * 4),
+                "path": "centcmod.run -> shwfs_run, host numpy phase/cents/bimg, one synchronous frame per step",
+                "frames": args.e2e_frames},
+        "latency_ms": {"p50": float(np.percentile(lat_ms, 50)), "p99": float(np.percentile(lat_ms, 99)),
+                       "mean": float(lat_ms.mean()), "path": "shwfs_run, host I/O"},
+        "clocks": clocks,
+        "gpu_launches": 2 * args.steps,
+    }
+    if ws == 1 and not args.no_cpu_baseline:
+        # CPU restatement of the path on a bounded sample, single thread
+        frames = 8
+        dt, nl = cpu_sample(frames, 1)
+        line["cpu_baseline"] = {"value": nl * frames / dt, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": "%d noisy frames of the same workload through the numpy/C restatement "
+                                          "(%.1f s)" % (frames, dt)}
+        # accuracy of a noiseless frame vs the float64 oracle
+        nph = np.ascontiguousarray(screens[3])
+        nc = np.zeros(nsub * 2, np.float32)
+        nb = np.zeros((nsx, nsx, w["m"], w["m"]), np.float32)
+        e2 = make_engine(pup, nph, nc, nb, noiseless=True)
+        e2.run(0)
+        line["centroid_err_px_vs_fp64"] = accuracy_vs_fp64(nc, nph)
+        e2.free()
+    eng.free()
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

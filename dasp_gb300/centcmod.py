@@ -1,0 +1,301 @@
+"""Drop-in replacement for the reference's ``util.centcmod`` module.
+
+``centcmod`` has the constructor, methods and update codes of
+``util/centcmod.py`` (:19-40, :41-145): the caller hands over a pupil object
+(anything with ``perSubap``/``getSubapFlag``/``getSubarea``, e.g.
+``dasp_gb300.tel.Pupil`` or the reference's ``util.tel.Pupil``), the phase
+array and the ``cents``/``bimg`` output arrays, then calls ``run`` every
+frame.  The arrays are borrowed exactly as the reference borrows them: the
+engine re-reads ``phs`` and overwrites ``cents``/``bimg`` in place on every
+readout frame.  They may be numpy arrays (host; copied to and from the GPU
+inside ``run``) or CUDA torch tensors (used in place).
+
+The work itself runs in hand-written sm_103a CUDA behind the C ABI of
+``include/shwfs.h``; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import (NOISE_COUNTER, NOISE_REFERENCE, NOISEMODE, VAL_ARRAY, VAL_FLOAT, VAL_INT, VAL_NONE,
+                   VAL_TUPLE3, ShwfsArray, ShwfsInfo, ShwfsInit, ShwfsValue, as_array, check)
+
+CALSOURCE = 1
+SIG = 2
+ADDPOISSON = 3
+NCEN = 4
+READNOISE = 5
+READBG = 6
+NOISEFLOOR = 7
+SKYBRIGHTNESS = 8
+PXLPOWER = 9
+SPOTPSF = 10
+NTHREADS = 11
+OPTICALBINNING = 12
+CENTWEIGHT = 13
+CORRELATIONCENTROIDING = 14
+CORRTHRESH = 15
+CORRPATTERN = 16
+CALDATA = 17
+REFCENTS = 18
+CALCOEFF = 19
+USEBRIGHTEST = 20
+INTEGSTEPS = 21  # should never be changed to something larger than the initial value
+OUTPUTPHASEARR = 22
+
+_INT_CODES = {CALSOURCE, ADDPOISSON, NCEN, NTHREADS, OPTICALBINNING, CORRELATIONCENTROIDING, INTEGSTEPS,
+              NOISEMODE}
+_INT_ARRAY_CODES = {USEBRIGHTEST}
+
+
+def _is_array(x) -> bool:
+    return isinstance(x, np.ndarray) or type(x).__module__.startswith("torch")
+
+
+class centcmod:
+    """Shack-Hartmann WFS engine handle with the ``util.centcmod`` interface."""
+
+    def __init__(self, nthreads, nsubx, ncen, fftsize, clipsize, nimg, phasesize, readnoise, readbg,
+                 addPoisson, noiseFloor, sig, skybrightness, calsource, pxlPower, nintegrations, nlatency, seed,
+                 phs, pup, spotpsf, cents, bimg, minarea, opticalBinning, centWeight, correlationCentroiding,
+                 corrThresh, corrPattern, corrimg, threshType, imageOnly, useBrightest, preBinningFactor,
+                 parabolicFit, gaussianFitVals, inputImage=None, subapLocation=None):
+        """Here, sig can be a float or a float array (one value per subaperture)."""
+        self.centstruct = None
+        self.nthreads = nthreads
+        self.nsubx = nsubx
+        self.nsubaps = nsubx * nsubx
+        self.ncen = ncen
+        self.fftsize = fftsize
+        self.clipsize = clipsize
+        self.nimg = nimg
+        self.phasesize = phasesize
+        self.readnoise = readnoise
+        self.readbg = readbg
+        self.addPoisson = addPoisson
+        self.noiseFloor = noiseFloor
+        self.sig = sig
+        self.skybrightness = skybrightness
+        self.calsource = calsource
+        self.minarea = minarea
+        self.opticalBinning = opticalBinning
+        if pxlPower is None:
+            pxlPower = 1.0
+        self.pxlPower = pxlPower
+        self.nintegrations = nintegrations
+        self.nlatency = nlatency
+        self.seed = seed
+        self.phs = phs
+        self.pup = pup
+        # input derivations of util/centcmod.py:76-78
+        self.pupfn = np.ascontiguousarray(pup.perSubap(nsubx, vectorAlign=0), dtype=np.float32)
+        self.subflag = np.ascontiguousarray(pup.getSubapFlag(nsubx, minarea), dtype=np.int32)
+        self.fracSubArea = np.ascontiguousarray(pup.getSubarea(nsubx) / (phasesize * phasesize), dtype=np.float32)
+        self.spotpsf = spotpsf
+        self.cents = cents
+        self.bimg = bimg
+        if isinstance(centWeight, str):  # will be created later
+            centWeight = None
+        self.centWeight = centWeight
+        self.correlationCentroiding = correlationCentroiding
+        self.corrThresh = corrThresh
+        self.corrPattern = corrPattern
+        self.corrimg = corrimg
+        self.threshType = threshType
+        self.imageOnly = imageOnly
+        self.useBrightest = useBrightest
+        self.preBinningFactor = preBinningFactor
+        self.parabolicFit = parabolicFit
+        if gaussianFitVals is None:
+            self.gaussianFit = 0
+            self.gaussianMinVal = 0.0
+            self.gaussianReplaceVal = 0.0
+        else:
+            self.gaussianFit = 1
+            self.gaussianMinVal = gaussianFitVals[0]
+            self.gaussianReplaceVal = gaussianFitVals[1]
+        self.inputImage = inputImage
+        self.subapLocation = subapLocation
+        if correlationCentroiding and corrPattern is not None:
+            cp = np.asarray(corrPattern) if not _is_array(corrPattern) else corrPattern
+            if (cp.dtype != np.float32 or tuple(cp.shape[:2]) != (nsubx, nsubx) or cp.shape[2] < nimg
+                    or cp.shape[3] != cp.shape[2]):
+                raise ValueError("corrPattern wrong shape or type: %s - should be (%d,%d,>=%d,>=%d), f"
+                                 % (str(cp.shape), nsubx, nsubx, nimg, nimg))
+
+        keep: list = []
+        ini = ShwfsInit()
+        ini.nthreads = int(nthreads)
+        ini.nsubaps = int(self.nsubaps)
+        ini.ncen = int(ncen)
+        ini.fftsize = int(fftsize)
+        ini.clipsize = int(clipsize)
+        ini.nimg = int(nimg)
+        ini.phasesize = int(phasesize)
+        ini.readnoise = float(readnoise)
+        ini.readbg = float(readbg)
+        ini.addPoisson = int(addPoisson)
+        ini.noiseFloor = float(noiseFloor)
+        if _is_array(sig):
+            ini.sigArr = as_array(sig, "f", "sig array", keep)
+        else:
+            ini.sig = float(sig)
+        if _is_array(skybrightness):
+            ini.skybrightnessArr = as_array(skybrightness, "f", "skybrightness", keep)
+        else:
+            ini.skybrightness = float(skybrightness)
+        ini.calsource = int(calsource)
+        ini.pxlPower = float(pxlPower)
+        ini.nintegrations = int(nintegrations)
+        ini.nlatency = int(nlatency)
+        ini.seed = int(seed) & (2 ** 64 - 1)
+        ini.phs = as_array(phs, "f", "phs", keep)
+        ini.pupfn = as_array(self.pupfn, "f", "pupfn", keep)
+        ini.spotpsf = as_array(spotpsf, "f", "spotpsf", keep)
+        ini.cents = as_array(cents, "f", "cents", keep)
+        ini.subflag = as_array(self.subflag, "i", "subflag", keep)
+        ini.bimg = as_array(bimg, "f", "bimg", keep)
+        ini.fracSubArea = as_array(self.fracSubArea, "f", "fracSubArea", keep)
+        ini.opticalBinning = int(opticalBinning)
+        ini.centWeight = as_array(centWeight, "f", "centWeight", keep)
+        ini.correlationCentroiding = int(correlationCentroiding)
+        ini.corrThresh = float(corrThresh)
+        ini.corrPattern = as_array(corrPattern, "f", "corrPattern", keep)
+        ini.corrimg = as_array(corrimg, "f", "corrimg", keep)
+        ini.threshType = int(threshType)
+        ini.imageOnly = int(imageOnly)
+        if _is_array(useBrightest):
+            ini.useBrightestArr = as_array(useBrightest, "i", "useBrightest", keep)
+        else:
+            ini.useBrightest = int(useBrightest)
+        ini.preBinningFactor = int(preBinningFactor)
+        ini.parabolicFit = int(parabolicFit)
+        ini.gaussianFit = int(self.gaussianFit)
+        ini.gaussianMinVal = float(self.gaussianMinVal)
+        ini.gaussianReplaceVal = float(self.gaussianReplaceVal)
+        ini.inputImage = as_array(inputImage, "f", "inputImage", keep)
+        ini.subapLocation = as_array(subapLocation, "i", "subapLocation", keep)
+        handle = ctypes.c_void_p()
+        check(_lib.lib().shwfs_initialise(ctypes.byref(ini), ctypes.byref(handle)), "initialise")
+        self.centstruct = handle
+        self._keep = keep  # borrowed arrays stay referenced while the handle lives
+
+    # -- util/centcmod.py:119-145 --
+    def run(self, calsource):
+        if calsource != self.calsource:
+            self.update(CALSOURCE, calsource)
+            self.calsource = calsource
+        t = ctypes.c_float(0.0)
+        check(_lib.lib().shwfs_run(self.centstruct, ctypes.byref(t)), "run")
+        return t.value
+
+    def runSlope(self, calsource):
+        if calsource != self.calsource:
+            self.update(CALSOURCE, calsource)
+            self.calsource = calsource
+        t = ctypes.c_float(0.0)
+        check(_lib.lib().shwfs_run_slope(self.centstruct, ctypes.byref(t)), "runSlope")
+        return t.value
+
+    def free(self):
+        if self.centstruct is not None:
+            _lib.lib().shwfs_free(self.centstruct)
+            self.centstruct = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def update(self, what, val):
+        """what is one of the codes at the top of this module; val the new value.
+
+        As in the reference this does not update the Python-side attributes.
+        Arrays passed here are copied into the engine at call time.
+        """
+        keep: list = []
+        v = ShwfsValue()
+        if val is None:
+            v.kind = VAL_NONE
+        elif isinstance(val, tuple):
+            if len(val) != 3:
+                raise ValueError("calibration data must be a (calData, calBounds, calSteps) tuple")
+            v.kind = VAL_TUPLE3
+            v.arr[0] = as_array(val[0], "f", "calData", keep)
+            v.arr[1] = as_array(val[1], "i", "calBounds", keep)
+            v.arr[2] = as_array(val[2], "f", "calSteps", keep)
+        elif _is_array(val):
+            v.kind = VAL_ARRAY
+            v.arr[0] = as_array(val, "i" if what in _INT_ARRAY_CODES else "f", "value", keep)
+        elif isinstance(val, (bool, int, np.integer)):
+            v.kind = VAL_INT
+            v.ival = int(val)
+        elif isinstance(val, (float, np.floating)):
+            if what in _INT_CODES:
+                if float(val) != int(val):
+                    raise ValueError("centmodule: Error extracting integer value")
+                v.kind = VAL_INT
+                v.ival = int(val)
+            else:
+                v.kind = VAL_FLOAT
+                v.dval = float(val)
+        else:
+            raise ValueError("unsupported update value of type %s" % type(val))
+        check(_lib.lib().shwfs_update(self.centstruct, int(what), ctypes.byref(v)), "update(%d)" % what)
+
+    # -- extensions (no reference counterpart) --
+    def set_noise_mode(self, mode):
+        """``"counter"`` (default, parallel Philox streams) or ``"reference"``
+        (the reference's per-thread PCG32/MT19937 streams)."""
+        code = {"counter": NOISE_COUNTER, "reference": NOISE_REFERENCE}[mode]
+        self.update(NOISEMODE, code)
+
+    def run_batch(self, phs_frames, cents_frames, bimg_frames, stream=None):
+        """Independent readout frames from CUDA tensors in one launch.
+
+        ``phs_frames`` (F, W, W) [or (F, 2, W, W)], ``cents_frames``
+        (F, nsubaps*2), ``bimg_frames`` (F, nsubaps, nimg, nimg); work is
+        queued on ``stream`` (a torch.cuda.Stream or raw handle; default: the
+        handle's own stream) and not waited for.
+        """
+        for t, n in ((phs_frames, "phs_frames"), (cents_frames, "cents_frames"), (bimg_frames, "bimg_frames")):
+            if not (_is_array(t) and getattr(t, "is_cuda", False)):
+                raise ValueError("%s must be a CUDA tensor" % n)
+            if not t.is_contiguous() or str(t.dtype) != "torch.float32":
+                raise ValueError("%s must be float32 and contiguous" % n)
+        nf = phs_frames.shape[0]
+        if cents_frames.numel() < nf * self.nsubaps * 2 or bimg_frames.numel() < nf * self.nsubaps * self.nimg ** 2:
+            raise ValueError("output tensors too small for %d frames" % nf)
+        s = getattr(stream, "cuda_stream", stream)
+        check(_lib.lib().shwfs_run_batch(self.centstruct, int(nf), phs_frames.data_ptr(),
+                                         int(phs_frames[0].numel()), cents_frames.data_ptr(),
+                                         bimg_frames.data_ptr(), s), "run_batch")
+
+    def run_async(self, stream=None):
+        """``run`` without the final wait; outputs are valid once ``stream`` drains."""
+        s = getattr(stream, "cuda_stream", stream)
+        check(_lib.lib().shwfs_run_async(self.centstruct, s), "run_async")
+
+    def set_io(self, phs=None, cents=None, bimg=None):
+        """Rebind the borrowed phase/output arrays (same shapes)."""
+        keep: list = []
+        args = []
+        for x, n in ((phs, "phs"), (cents, "cents"), (bimg, "bimg")):
+            args.append(None if x is None else ctypes.byref(as_array(x, "f", n, keep)))
+        check(_lib.lib().shwfs_set_io(self.centstruct, *args), "set_io")
+        if phs is not None:
+            self.phs = phs
+        if cents is not None:
+            self.cents = cents
+        if bimg is not None:
+            self.bimg = bimg
+        self._keep.extend(keep)
+
+    def info(self) -> dict:
+        inf = ShwfsInfo()
+        check(_lib.lib().shwfs_get_info(self.centstruct, ctypes.byref(inf)), "get_info")
+        return {f: getattr(inf, f) for f, _ in ShwfsInfo._fields_}

@@ -1,0 +1,51 @@
+// Reference-stream noise state and launcher (see wfs_refnoise.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace shwfs {
+
+constexpr int kMtN = 624, kMtM = 397;
+
+// one reference worker thread's generators: PCG32 (Poisson) + MT19937 (read noise)
+struct RefRng {
+  uint64_t pcg_state, pcg_inc;
+  uint32_t mt[kMtN];
+  int mti;
+  int pad;
+};
+
+struct RefNoiseArgs {
+  int nthreads;
+  const int* subapStart;  // nthreads + 1
+  const int* subflag;
+  const unsigned char* poisFlag;
+  float* bimg;
+  int m, nexp;
+  float readNoise, readBg, floorv;
+  int threshType, addPoisson, calsource, imageOnly;
+};
+
+// host-side seeding: pcg32_srandom_r(seed_t, 1) and gsl_rng_set(mt, seed_t)
+// (cmod/src/centmodule.c:91-98, 2556-2562)
+inline void seed_ref_rng(RefRng* r, uint64_t seed_t) {
+  auto next = [r]() {
+    uint64_t old = r->pcg_state;
+    r->pcg_state = old * 6364136223846793005ULL + r->pcg_inc;
+  };
+  r->pcg_state = 0u;
+  r->pcg_inc = (1ull << 1u) | 1u;
+  next();
+  r->pcg_state += seed_t;
+  next();
+  uint64_t s = seed_t;
+  if (s == 0) s = 4357;
+  r->mt[0] = (uint32_t)(s & 0xffffffffULL);
+  for (int i = 1; i < kMtN; i++) r->mt[i] = (uint32_t)(1812433253UL * (r->mt[i - 1] ^ (r->mt[i - 1] >> 30)) + i);
+  r->mti = kMtN;
+  r->pad = 0;
+}
+
+cudaError_t launch_refnoise(const RefNoiseArgs& a, RefRng* rng, int* status, cudaStream_t stream);
+
+}  // namespace shwfs

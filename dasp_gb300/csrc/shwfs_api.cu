@@ -1,0 +1,1033 @@
+// Host side of the C ABI declared in include/shwfs.h.
+//
+// A handle holds what the reference's centstruct holds (cmod/src/
+// centmodule.c:139-249): scalar parameters, the integration state, the
+// borrowed phase/cents/bimg arrays, and device-resident copies of every
+// constant (pupil, flags, area fractions, normalisation totals, PSF spectra,
+// binning tables, weights, calibration data, reference centroids).  A run
+// queues: [H2D phase] -> fused kernel (+ unlit kernel) -> [D2H outputs].
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <ctime>
+#include <string>
+#include <vector>
+
+#include "../../include/shwfs.h"
+#include "refnoise.h"
+#include "wfs_launch.cuh"
+
+using namespace shwfs;
+
+namespace {
+
+thread_local std::string g_err;
+
+shwfs_status fail(shwfs_status st, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return st;
+}
+
+#define CK(call)                                                                                    \
+  do {                                                                                              \
+    cudaError_t e_ = (call);                                                                        \
+    if (e_ != cudaSuccess) return fail(SHWFS_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { reset(); }
+  void reset() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t alloc(size_t count) {
+    reset();
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc((void**)&p, count * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    return e;
+  }
+  cudaError_t upload(const T* src, size_t count) {
+    cudaError_t e = alloc(count);
+    if (e != cudaSuccess || count == 0) return e;
+    return cudaMemcpy(p, src, count * sizeof(T), cudaMemcpyDefault);
+  }
+};
+
+int64_t numel(const shwfs_array& a) {
+  if (!a.data) return 0;
+  int64_t n = 1;
+  for (int i = 0; i < a.ndim; i++) n *= a.shape[i];
+  return n;
+}
+
+bool is_none(const shwfs_array& a) { return a.data == nullptr; }
+
+// copy an array (host or device) to host memory
+template <typename T>
+std::vector<T> to_host(const shwfs_array& a) {
+  std::vector<T> v((size_t)numel(a));
+  if (!v.empty()) cudaMemcpy(v.data(), a.data, v.size() * sizeof(T), cudaMemcpyDefault);
+  return v;
+}
+
+}  // namespace
+
+struct shwfs_handle {
+  // parameters (names as in centstruct)
+  int nthreads = 1, nsubaps = 0, nsubx = 0, ncen = 0, fftsize = 0, clipsize = 0, nimg = 0, phasesize = 0;
+  float readNoise = 0, readBg = 0, noiseFloor = 0;
+  int addPoisson = 0;
+  float sig = 0;
+  bool sigIsArr = false;
+  float sky = 0;
+  bool skyIsArr = false;
+  int calsource = 0;
+  float pxlPower = 1;
+  int nintegrations = 1, nlatency = 0, curInteg = 0;
+  uint64_t seed = 0;
+  int opticalBinning = 0, correlationCentroiding = 0, threshType = 0, imageOnly = 0;
+  int useBrightest = 0;
+  bool ubIsArr = false;
+  int preBinOrig = 1, preBin = 1, parabolicFit = 0, gaussianFit = 0;
+  float gMin = 0, gRep = 0, corrThresh = 0;
+  int psfDim = 0, psfsize = 0, padded = 0, phaseAmp = 0, W = 0;
+  int centWeightDim = 0;
+  int noiseMode = SHWFS_NOISE_COUNTER;
+  uint64_t framesRead = 0;
+  bool haveCalData = false, haveCalCoeff = false, haveRef = false;
+  int calNSteps = 0, calNCoeff = 0;
+  int fitMxParam = 0;
+
+  std::vector<int> subflag, lit, unlit;
+  std::vector<float> pup, frac, psfSums;  // host copies for totsig
+  std::vector<int> subapStart;
+
+  // borrowed I/O
+  shwfs_array phs{}, cents{}, bimg{};
+  std::vector<void*> registered;  // host ranges pinned by the engine
+
+  // device state
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  DevBuf<float> d_pup, d_tilt, d_frac, d_totsig, d_sigArr, d_skyArr, d_cw, d_ref, d_calData, d_calSteps,
+      d_calCoeff, d_fitMx, d_binT, d_binN, d_psf;
+  DevBuf<int> d_lit, d_unlit, d_binII, d_binLo, d_binHi, d_ubArr, d_calBounds, d_subflag, d_subapStart, d_status;
+  DevBuf<float2> d_psfSpec;
+  DevBuf<float> d_phs, d_cents, d_bimg;  // mirrors of host I/O
+  DevBuf<unsigned char> d_poisFlag;
+  DevBuf<RefRng> d_rng;
+  const PlainEntry* entry = nullptr;
+  int TS = 1, smem = 0, ctasPerSM = 1, numSMs = 1;
+
+  ~shwfs_handle() {
+    for (void* p : registered) cudaHostUnregister(p);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+shwfs_status check_f32(const shwfs_array& a, const char* name) {
+  if (a.dtype != SHWFS_F32) return fail(SHWFS_ERR_INVALID, "%s must be float32 and contiguous", name);
+  return SHWFS_OK;
+}
+
+// bind a borrowed array; host pages are pinned in place (once) so the
+// per-frame copies are asynchronous DMA
+shwfs_status bind_io(shwfs_handle* h, shwfs_array& slot, const shwfs_array& a, DevBuf<float>& mirror, size_t count,
+                     bool copy_initial) {
+  slot = a;
+  if (a.on_device) {
+    mirror.reset();
+    return SHWFS_OK;
+  }
+  if (mirror.n != count) {
+    cudaError_t e = mirror.alloc(count);
+    if (e != cudaSuccess) return fail(SHWFS_ERR_NOMEM, "device mirror allocation failed: %s", cudaGetErrorString(e));
+  }
+  cudaPointerAttributes attr;
+  if (cudaPointerGetAttributes(&attr, a.data) == cudaSuccess && attr.type == cudaMemoryTypeUnregistered) {
+    if (cudaHostRegister((void*)a.data, count * sizeof(float), cudaHostRegisterDefault) == cudaSuccess)
+      h->registered.push_back((void*)a.data);
+  }
+  cudaGetLastError();  // a refused registration only costs copy speed
+  // outputs start from the caller's contents: entries the engine does not
+  // write (unlit subapertures, non-readout frames) come back unchanged
+  if (copy_initial) CK(cudaMemcpy(mirror.p, a.data, count * sizeof(float), cudaMemcpyHostToDevice));
+  return SHWFS_OK;
+}
+
+// updateTotSigArr (cmod/src/centmodule.c:2403-2427): float accumulation in
+// the reference's order
+shwfs_status update_totsig(shwfs_handle* h) {
+  const int pp = h->phasesize * h->phasesize;
+  std::vector<float> tot(h->nsubaps);
+  for (int i = 0; i < h->nsubaps; i++) {
+    float t = 0.f;
+    for (int j = 0; j < pp; j++) t += h->pup[(size_t)i * pp + j];
+    t *= (float)(h->fftsize * h->fftsize);
+    if (h->psfDim) {
+      float s = h->psfSums[h->psfDim == 2 ? 0 : i];
+      t *= s * h->psfsize * h->psfsize;
+    }
+    tot[i] = t;
+  }
+  CK(h->d_totsig.upload(tot.data(), tot.size()));
+  return SHWFS_OK;
+}
+
+// prepareBinImage (cmod/src/centmodule.c:565-608) plus the gather ranges of
+// the fused kernel's binning stage
+shwfs_status prepare_bin(shwfs_handle* h) {
+  const int C = h->clipsize, m = h->nimg;
+  std::vector<float> t(C), n(C);
+  std::vector<int> idx(C), ii(C), lo(m, C), hi(m, -1);
+  int cnt = 0;
+  for (int i = 0; i < C; i++) {
+    cnt += m;
+    if (cnt >= C) {
+      int excess = cnt - C;
+      t[i] = (m - excess) / (float)m;
+      n[i] = excess / (float)m;
+      idx[i] = 1;
+      cnt = excess;
+    } else {
+      t[i] = 1.f;
+      n[i] = 0.f;
+      idx[i] = 0;
+    }
+  }
+  int acc = 0;
+  for (int i = 0; i < C; i++) {
+    ii[i] = acc;
+    if (i < C - 1) acc += idx[i];
+  }
+  for (int i = 0; i < C; i++) {
+    // row i feeds output ii[i] (this share) and, through the next-pixel
+    // share of row i-1, output ii[i-1]+1
+    if (ii[i] < m) {
+      lo[ii[i]] = std::min(lo[ii[i]], i);
+      hi[ii[i]] = std::max(hi[ii[i]], i);
+    }
+    if (i < C - 1 && n[i] != 0.f && ii[i] + 1 < m) {
+      lo[ii[i] + 1] = std::min(lo[ii[i] + 1], i);
+      hi[ii[i] + 1] = std::max(hi[ii[i] + 1], i);
+    }
+  }
+  for (int I = 0; I < m; I++)
+    if (hi[I] < lo[I]) {
+      lo[I] = 0;
+      hi[I] = -1;
+    }
+  CK(h->d_binT.upload(t.data(), C));
+  CK(h->d_binN.upload(n.data(), C));
+  CK(h->d_binII.upload(ii.data(), C));
+  CK(h->d_binLo.upload(lo.data(), m));
+  CK(h->d_binHi.upload(hi.data(), m));
+  return SHWFS_OK;
+}
+
+// setSpotPsf + prepareSpotPsf (cmod/src/centmodule.c:2255-2375)
+shwfs_status set_spot_psf(shwfs_handle* h, const shwfs_array& psf) {
+  int dim = 0, P = h->clipsize, preBin = 1, padded = h->clipsize;
+  if (!is_none(psf)) {
+    if (psf.ndim == 2) {
+      dim = 2;
+      P = (int)psf.shape[0];
+      if (psf.shape[1] != P) return fail(SHWFS_ERR_INVALID, "spotpsf must be square");
+    } else if (psf.ndim == 4) {
+      dim = 4;
+      P = (int)psf.shape[2];
+      if (psf.shape[0] * psf.shape[1] != h->nsubaps || psf.shape[3] != P)
+        return fail(SHWFS_ERR_INVALID, "spotpsf 4d must be (nsubx,nsubx,P,P)");
+    } else {
+      return fail(SHWFS_ERR_INVALID, "spotpsf not 2d or 4d");
+    }
+    preBin = h->preBinOrig;
+    padded = preBin <= 1 ? P : h->fftsize;
+    if (preBin > 0 && padded % preBin != 0)
+      return fail(SHWFS_ERR_INVALID, "paddedsize(%d) modulo preBinningFactor(%d) should be zero", padded, preBin);
+    if (preBin > 1 && P > padded)
+      return fail(SHWFS_ERR_INVALID, "spotpsf dimensions should be equal to or less than paddedsize (%d)", padded);
+    if (P < h->clipsize) return fail(SHWFS_ERR_INVALID, "spotpsf dimensions should be at least clipsize");
+    shwfs_status st = check_f32(psf, "spotpsf");
+    if (st) return st;
+  }
+  if (preBin < 1) preBin = 1;
+  const PlainEntry* entry = nullptr;
+  auto& reg = plain_registry();
+  auto it = reg.find({h->fftsize, dim ? P : 0});
+  if (it == reg.end())
+    return fail(SHWFS_ERR_UNSUPPORTED, "no compiled kernel for fftsize %d with psfsize %d", h->fftsize, dim ? P : 0);
+  entry = &it->second;
+  if (dim) {
+    std::vector<float> hp = to_host<float>(psf);
+    const int npsf = dim == 2 ? 1 : h->nsubaps;
+    h->psfSums.assign(npsf, 0.f);
+    for (int k = 0; k < npsf; k++) {
+      float s = 0.f;
+      for (int j = 0; j < P * P; j++) s += hp[(size_t)k * P * P + j];
+      h->psfSums[k] = s;
+    }
+    CK(h->d_psf.upload(hp.data(), hp.size()));
+    CK(h->d_psfSpec.alloc((size_t)npsf * P * (P / 2 + 1)));
+    CK(entry->psf_spectra(h->d_psf.p, npsf, h->d_psfSpec.p, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    h->d_psf.reset();
+  } else {
+    h->d_psfSpec.reset();
+    h->psfSums.clear();
+  }
+  h->psfDim = dim;
+  h->psfsize = P;
+  h->preBin = preBin;
+  h->padded = padded;
+  h->entry = entry;
+  return SHWFS_OK;
+}
+
+// launch geometry: tile size, shared memory, persistent grid
+shwfs_status plan(shwfs_handle* h) {
+  const int P = h->psfDim ? h->psfsize : 0;
+  const int per = persub_floats(h->phasesize, h->fftsize, P, h->padded, h->clipsize, h->nimg);
+  const int cst = const_floats(h->phasesize, h->clipsize, h->nimg, P, h->centWeightDim == 2, h->psfDim == 2);
+  int TS = std::max(1, std::min(64, (kThreads + h->phasesize - 1) / h->phasesize));
+  while (TS > 1 && (size_t)(cst + TS * per) * 4 > 100 * 1024) TS--;
+  const int smem = (cst + TS * per) * 4;
+  if (smem > 227 * 1024) return fail(SHWFS_ERR_UNSUPPORTED, "subaperture too large for shared memory (%d bytes)", smem);
+  int ctas = 0;
+  CK(h->entry->occupancy(&ctas, smem));
+  if (ctas < 1) return fail(SHWFS_ERR_UNSUPPORTED, "kernel cannot be resident with %d bytes of shared memory", smem);
+  h->TS = TS;
+  h->smem = smem;
+  h->ctasPerSM = ctas;
+  return SHWFS_OK;
+}
+
+shwfs_status set_cent_weight(shwfs_handle* h, const shwfs_array& cw) {
+  h->centWeightDim = 0;
+  h->d_cw.reset();
+  if (is_none(cw)) return SHWFS_OK;
+  const int corr = h->nimg;
+  if (cw.ndim != 2 && cw.ndim != 4) return fail(SHWFS_ERR_INVALID, "centWeight not 2d or 4d");
+  if (check_f32(cw, "centWeight")) return SHWFS_ERR_INVALID;
+  if (cw.shape[cw.ndim - 2] != corr || cw.shape[cw.ndim - 1] != corr)
+    return fail(SHWFS_ERR_INVALID, "centweight array not correct dimensions (need to be nsubx,nsubx,corrsize,corrsize)");
+  if (cw.ndim == 4 && cw.shape[0] * cw.shape[1] != h->nsubaps)
+    return fail(SHWFS_ERR_INVALID, "centWeight 4d must be (nsubx,nsubx,corrsize,corrsize)");
+  std::vector<float> v = to_host<float>(cw);
+  CK(h->d_cw.upload(v.data(), v.size()));
+  h->centWeightDim = cw.ndim;
+  return SHWFS_OK;
+}
+
+shwfs_status set_sig(shwfs_handle* h, double sig, const shwfs_array* arr) {
+  if (arr && !is_none(*arr)) {
+    if (check_f32(*arr, "sig array")) return SHWFS_ERR_INVALID;
+    if (arr->ndim != 1 || arr->shape[0] != h->nsubaps)
+      return fail(SHWFS_ERR_INVALID, "sig arr dimensions must be 1D (nsubx^2)");
+    std::vector<float> v = to_host<float>(*arr);
+    CK(h->d_sigArr.upload(v.data(), v.size()));
+    h->sigIsArr = true;
+  } else {
+    h->sig = (float)sig;
+    // a scalar update keeps a previously set array, as py_update does
+  }
+  return SHWFS_OK;
+}
+
+shwfs_status set_sky(shwfs_handle* h, double sky, const shwfs_array* arr) {
+  if (arr && !is_none(*arr)) {
+    if (check_f32(*arr, "skybrightness")) return SHWFS_ERR_INVALID;
+    if (arr->ndim != 3 || arr->shape[0] != h->nsubaps || arr->shape[1] != h->nimg || arr->shape[2] != h->nimg)
+      return fail(SHWFS_ERR_INVALID, "skybrightness should be 3D array shape nsubaps,nimg,nimg");
+    std::vector<float> v = to_host<float>(*arr);
+    CK(h->d_skyArr.upload(v.data(), v.size()));
+    h->sky = 0.f;
+    h->skyIsArr = true;
+  } else {
+    h->sky = (float)sky;
+    h->skyIsArr = false;
+    h->d_skyArr.reset();
+  }
+  return SHWFS_OK;
+}
+
+shwfs_status set_use_brightest(shwfs_handle* h, int ub, const shwfs_array* arr) {
+  if (arr && !is_none(*arr)) {
+    if (arr->dtype != SHWFS_I32) return fail(SHWFS_ERR_INVALID, "useBrightest must be int or int contiguous array");
+    if (arr->ndim != 1 || arr->shape[0] != h->nsubaps)
+      return fail(SHWFS_ERR_INVALID, "useBrightest array should be 1D of shape nsubaps (nsubx^2)");
+    std::vector<int> v = to_host<int>(*arr);
+    CK(h->d_ubArr.upload(v.data(), v.size()));
+    h->useBrightest = 0;
+    h->ubIsArr = true;
+  } else {
+    h->useBrightest = ub;
+    h->ubIsArr = false;
+    h->d_ubArr.reset();
+  }
+  return SHWFS_OK;
+}
+
+// setupThreads (cmod/src/centmodule.c:2457-2571): partition + RNG seeding
+shwfs_status setup_threads(shwfs_handle* h, int nthreads) {
+  if (nthreads < 1) return fail(SHWFS_ERR_INVALID, "nthreads must be >= 1");
+  h->nthreads = nthreads;
+  h->subapStart.assign(nthreads + 1, 0);
+  int cnt = 0, left = h->nsubaps;
+  for (int i = 0; i < nthreads; i++) {
+    h->subapStart[i] = cnt;
+    cnt += left / (nthreads - i);
+    left -= left / (nthreads - i);
+  }
+  h->subapStart[nthreads] = h->nsubaps;
+  std::vector<RefRng> rng(nthreads);
+  const uint64_t base = h->seed == 0 ? (uint64_t)time(nullptr) : h->seed;
+  for (int i = 0; i < nthreads; i++) seed_ref_rng(&rng[i], base + i);
+  CK(h->d_rng.upload(rng.data(), rng.size()));
+  CK(h->d_subapStart.upload(h->subapStart.data(), h->subapStart.size()));
+  return SHWFS_OK;
+}
+
+// 6x6 normal-matrix inverse for the parabolic/Gaussian fit (makeFitMx,
+// cmod/src/centmodule.c:997-1056), Gauss-Jordan with partial pivoting
+shwfs_status make_fit_mx(shwfs_handle* h, int ncen) {
+  double a[6][12];
+  memset(a, 0, sizeof(a));
+  for (int y = 0; y < ncen; y++)
+    for (int x = 0; x < ncen; x++) {
+      double v[6] = {(double)x * x, (double)x * y, (double)y * y, (double)x, (double)y, 1.0};
+      for (int r = 0; r < 6; r++)
+        for (int c = 0; c < 6; c++) a[r][c] += v[r] * v[c];
+    }
+  for (int r = 0; r < 6; r++) a[r][6 + r] = 1.0;
+  for (int c = 0; c < 6; c++) {
+    int piv = c;
+    for (int r = c + 1; r < 6; r++)
+      if (fabs(a[r][c]) > fabs(a[piv][c])) piv = r;
+    if (a[piv][c] == 0.0) return fail(SHWFS_ERR_INVALID, "singular fit matrix for fit size %d", ncen);
+    if (piv != c)
+      for (int k = 0; k < 12; k++) std::swap(a[c][k], a[piv][k]);
+    double d = a[c][c];
+    for (int k = 0; k < 12; k++) a[c][k] /= d;
+    for (int r = 0; r < 6; r++)
+      if (r != c) {
+        double f = a[r][c];
+        for (int k = 0; k < 12; k++) a[r][k] -= f * a[c][k];
+      }
+  }
+  float mx[30];
+  for (int r = 0; r < 5; r++)
+    for (int c = 0; c < 6; c++) mx[r * 6 + c] = (float)a[r][6 + c];
+  CK(h->d_fitMx.upload(mx, 30));
+  h->fitMxParam = ncen;
+  return SHWFS_OK;
+}
+
+WfsArgs make_args(shwfs_handle* h, const float* phs, float* cents, float* bimg, int nframes, long long phsStride,
+                  int mode) {
+  WfsArgs a;
+  memset(&a, 0, sizeof(a));
+  a.nsubx = h->nsubx;
+  a.nsubaps = h->nsubaps;
+  a.p = h->phasesize;
+  a.N = h->fftsize;
+  a.C = h->clipsize;
+  a.m = h->nimg;
+  a.ncen = h->ncen;
+  a.P = h->psfsize;
+  a.padded = h->padded;
+  a.preBin = h->preBin;
+  a.psfDim = h->psfDim;
+  a.phaseAmp = h->phaseAmp;
+  a.W = h->W;
+  a.phsFrameStride = phsStride;
+  a.phsAmpOffset = (long long)h->W * h->W;
+  a.nlit = (int)h->lit.size();
+  a.nframes = nframes;
+  a.TS = h->TS;
+  a.lit = h->d_lit.p;
+  a.phs = phs;
+  a.pup = h->d_pup.p;
+  a.tilt = h->d_tilt.p;
+  a.frac = h->d_frac.p;
+  a.totsig = h->d_totsig.p;
+  a.sig = h->sig;
+  a.sigArr = h->sigIsArr ? h->d_sigArr.p : nullptr;
+  a.sky = h->sky;
+  a.skyArr = h->skyIsArr ? h->d_skyArr.p : nullptr;
+  a.psfSpec = h->d_psfSpec.p;
+  a.binT = h->d_binT.p;
+  a.binN = h->d_binN.p;
+  a.binII = h->d_binII.p;
+  a.binLo = h->d_binLo.p;
+  a.binHi = h->d_binHi.p;
+  a.readNoise = h->readNoise;
+  a.readBg = h->readBg;
+  a.floorv = h->noiseFloor;
+  a.threshType = h->threshType;
+  a.addPoisson = h->addPoisson;
+  a.calsource = h->calsource;
+  a.opticalBinning = h->opticalBinning;
+  a.imageOnly = h->imageOnly;
+  a.useBrightest = h->useBrightest;
+  a.useBrightestArr = h->ubIsArr ? h->d_ubArr.p : nullptr;
+  a.pxlPower = h->pxlPower;
+  a.centWeight = h->d_cw.p;
+  a.centWeightDim = h->centWeightDim;
+  a.cob = h->correlationCentroiding == 5 ? 1 : h->correlationCentroiding;
+  a.fitSize = h->parabolicFit + h->gaussianFit;
+  a.gaussianFit = h->gaussianFit;
+  a.gMin = h->gMin;
+  a.gRep = h->gRep;
+  a.fitMx = h->d_fitMx.p;
+  a.calData = h->haveCalData ? h->d_calData.p : nullptr;
+  a.calBounds = h->d_calBounds.p;
+  a.calSteps = h->d_calSteps.p;
+  a.calNSteps = h->calNSteps;
+  a.calCoeff = h->haveCalCoeff ? h->d_calCoeff.p : nullptr;
+  a.calNCoeff = h->calNCoeff;
+  a.refCents = h->haveRef ? h->d_ref.p : nullptr;
+  a.bimg = bimg;
+  a.bimgFrameStride = (long long)h->nsubaps * h->nimg * h->nimg;
+  a.cents = cents;
+  a.centsFrameStride = (long long)h->nsubaps * 2;
+  a.poisFlag = h->d_poisFlag.p;
+  a.seed = h->seed;
+  a.frame0 = h->framesRead;
+  a.mode = mode;
+  return a;
+}
+
+// queue one readout over nframes frames (device pointers)
+shwfs_status enqueue_readout(shwfs_handle* h, const float* phs, float* cents, float* bimg, int nframes,
+                             long long phsStride, cudaStream_t st) {
+  const int nlit = (int)h->lit.size();
+  const long long nwork = (long long)nlit * nframes;
+  const long long ntiles = (nwork + h->TS - 1) / h->TS;
+  const int grid = (int)std::max<long long>(1, std::min<long long>(ntiles, (long long)h->numSMs * h->ctasPerSM));
+  if (h->fitMxParam != h->parabolicFit + h->gaussianFit && (h->parabolicFit || h->gaussianFit > 0)) {
+    int fs = h->parabolicFit + h->gaussianFit;
+    shwfs_status s = make_fit_mx(h, fs < 0 ? 3 : (fs < 3 ? 3 : fs));
+    if (s) return s;
+    h->fitMxParam = h->parabolicFit + h->gaussianFit;
+  }
+  if (h->noiseMode == SHWFS_NOISE_REFERENCE) {
+    if (nframes != 1) return fail(SHWFS_ERR_UNSUPPORTED, "reference-stream noise runs one frame at a time");
+    if (nlit) {
+      WfsArgs a = make_args(h, phs, cents, bimg, 1, phsStride, kForm | kStorePreNoise);
+      CK(h->entry->launch(a, grid, h->smem, st));
+    }
+    RefNoiseArgs r;
+    r.nthreads = h->nthreads;
+    r.subapStart = h->d_subapStart.p;
+    r.subflag = h->d_subflag.p;
+    r.poisFlag = h->d_poisFlag.p;
+    r.bimg = bimg;
+    r.m = h->nimg;
+    r.nexp = h->opticalBinning == 1 ? 2 * h->ncen : h->nimg * h->nimg;
+    r.readNoise = h->readNoise;
+    r.readBg = h->readBg;
+    r.floorv = h->noiseFloor;
+    r.threshType = h->threshType;
+    r.addPoisson = h->addPoisson;
+    r.calsource = h->calsource;
+    r.imageOnly = h->imageOnly;
+    CK(launch_refnoise(r, h->d_rng.p, h->d_status.p, st));
+    if (nlit) {
+      WfsArgs a = make_args(h, phs, cents, bimg, 1, phsStride, kPost);
+      CK(h->entry->launch(a, grid, h->smem, st));
+    }
+    if (!h->unlit.empty() && !h->imageOnly) {
+      WfsArgs a = make_args(h, phs, cents, bimg, 1, phsStride, 0);
+      CK(launch_unlit(a, h->d_unlit.p, (int)h->unlit.size(), st));
+    }
+  } else {
+    if (nlit) {
+      WfsArgs a = make_args(h, phs, cents, bimg, nframes, phsStride, kForm | kNoiseCounter | kPost);
+      CK(h->entry->launch(a, grid, h->smem, st));
+    }
+    if (!h->unlit.empty()) {
+      WfsArgs a = make_args(h, phs, cents, bimg, nframes, phsStride, 0);
+      CK(launch_unlit(a, h->d_unlit.p, (int)h->unlit.size(), st));
+    }
+  }
+  return SHWFS_OK;
+}
+
+// the integration state machine of centroidsFromPhase (cmod/src/centmodule.c:
+// 1774-1788) and py_run's advance (:3221-3223); returns 1 on a readout frame
+int readout_frame(const shwfs_handle* h) {
+  if (h->curInteg == 0) return 1 == h->nintegrations + h->nlatency ? 1 : 0;
+  if (h->curInteg + 1 < h->nintegrations) return 0;
+  if (h->curInteg + 1 < h->nintegrations + h->nlatency) return 0;
+  return 1;
+}
+
+shwfs_status run_impl(shwfs_handle* h, cudaStream_t st, bool sync, float* elapsed) {
+  auto t0 = std::chrono::steady_clock::now();
+  CK(cudaSetDevice(h->device));
+  if (!st) st = h->stream;
+  const bool readout = readout_frame(h);
+  if (readout) {
+    const size_t nph = (size_t)numel(h->phs);
+    const float* phs = (const float*)h->phs.data;
+    if (!h->phs.on_device) {
+      CK(cudaMemcpyAsync(h->d_phs.p, h->phs.data, nph * sizeof(float), cudaMemcpyHostToDevice, st));
+      phs = h->d_phs.p;
+    }
+    float* cents = h->cents.on_device ? (float*)h->cents.data : h->d_cents.p;
+    float* bimg = h->bimg.on_device ? (float*)h->bimg.data : h->d_bimg.p;
+    shwfs_status s = enqueue_readout(h, phs, cents, bimg, 1, 0, st);
+    if (s) return s;
+    if (!h->cents.on_device)
+      CK(cudaMemcpyAsync((void*)h->cents.data, h->d_cents.p, (size_t)h->nsubaps * 2 * sizeof(float),
+                         cudaMemcpyDeviceToHost, st));
+    if (!h->bimg.on_device)
+      CK(cudaMemcpyAsync((void*)h->bimg.data, h->d_bimg.p, (size_t)h->nsubaps * h->nimg * h->nimg * sizeof(float),
+                         cudaMemcpyDeviceToHost, st));
+    h->framesRead++;
+  }
+  h->curInteg++;
+  if (h->curInteg >= h->nintegrations + h->nlatency) h->curInteg = 0;
+  if (sync) {
+    CK(cudaStreamSynchronize(st));
+    if (h->noiseMode == SHWFS_NOISE_REFERENCE && readout) {
+      int status = 0;
+      CK(cudaMemcpy(&status, h->d_status.p, sizeof(int), cudaMemcpyDeviceToHost));
+      if (status) return fail(SHWFS_ERR_STATE, "reference-stream Poisson sampler hit its iteration limit");
+    }
+  }
+  if (elapsed) *elapsed = std::chrono::duration<float>(std::chrono::steady_clock::now() - t0).count();
+  return SHWFS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* shwfs_last_error(void) { return g_err.c_str(); }
+
+const char* shwfs_version(void) { return "shwfs-gb300 0.1 (sm_103a)"; }
+
+shwfs_status shwfs_initialise(const shwfs_init* in, shwfs_handle** out) {
+  g_err.clear();
+  if (!in || !out) return fail(SHWFS_ERR_INVALID, "null argument");
+  *out = nullptr;
+  auto h = new (std::nothrow) shwfs_handle();
+  if (!h) return fail(SHWFS_ERR_NOMEM, "handle allocation failed");
+  struct Guard {
+    shwfs_handle* h;
+    ~Guard() { delete h; }
+  } guard{h};
+
+  if (in->nsubaps <= 0 || in->phasesize <= 0 || in->fftsize <= 0 || in->clipsize <= 0 || in->nimg <= 0)
+    return fail(SHWFS_ERR_INVALID, "sizes must be positive");
+  h->nsubaps = in->nsubaps;
+  h->nsubx = (int)sqrtf((float)in->nsubaps);
+  if (h->nsubx * h->nsubx != h->nsubaps) return fail(SHWFS_ERR_INVALID, "nsubaps must be nsubx^2");
+  h->ncen = in->ncen;
+  h->fftsize = in->fftsize;
+  h->clipsize = in->clipsize;
+  h->nimg = in->nimg;
+  h->phasesize = in->phasesize;
+  h->preBinOrig = in->preBinningFactor;
+  h->parabolicFit = in->parabolicFit;
+  h->gaussianFit = in->gaussianFit;
+  h->gMin = in->gaussianMinVal;
+  h->gRep = in->gaussianReplaceVal;
+  if (h->phasesize > h->fftsize) return fail(SHWFS_ERR_INVALID, "phasesize must not exceed fftsize");
+  if (h->nimg > h->clipsize) return fail(SHWFS_ERR_INVALID, "nimg must not exceed clipsize");
+  if (h->ncen < 1 || h->ncen > h->nimg) return fail(SHWFS_ERR_INVALID, "ncen must be in [1, nimg]");
+  if (in->correlationCentroiding != 0)
+    return fail(SHWFS_ERR_UNSUPPORTED, "correlation centroiding is not implemented by this engine yet");
+  if (!is_none(in->inputImage) || !is_none(in->subapLocation))
+    return fail(SHWFS_ERR_UNSUPPORTED, "image input (runSlope) is not implemented by this engine yet");
+
+  // arrays: validation as py_initialise, plus size checks the C code trusts;
+  // everything that needs no GPU is checked before the first CUDA call
+  const int p = h->phasesize, nsa = h->nsubaps, m = h->nimg;
+  if (is_none(in->cents) || check_f32(in->cents, "cents")) return fail(SHWFS_ERR_INVALID, "cents must be float and contiguous");
+  if (numel(in->cents) < 2LL * nsa) return fail(SHWFS_ERR_INVALID, "cents must hold nsubaps*2 values");
+  if (is_none(in->phs)) return fail(SHWFS_ERR_UNSUPPORTED, "phase input is required (image input not implemented)");
+  if (check_f32(in->phs, "phs")) return SHWFS_ERR_INVALID;
+  if (in->phs.ndim == 2)
+    h->phaseAmp = 0;
+  else if (in->phs.ndim == 3 && in->phs.shape[0] == 2)
+    h->phaseAmp = 1;
+  else
+    return fail(SHWFS_ERR_INVALID, "phase should be 2D or 3D (for phase+amp)");
+  const int W = h->nsubx * p;
+  if (in->phs.shape[h->phaseAmp] != W || in->phs.shape[h->phaseAmp + 1] != W)
+    return fail(SHWFS_ERR_UNSUPPORTED, "phase of size %lldx%lld needs interpolation to %dx%d (not implemented yet)",
+                (long long)in->phs.shape[h->phaseAmp], (long long)in->phs.shape[h->phaseAmp + 1], W, W);
+  h->W = W;
+  if (is_none(in->pupfn) || check_f32(in->pupfn, "pupfn")) return fail(SHWFS_ERR_INVALID, "pupfn must be float and contiguous");
+  if (numel(in->pupfn) != (int64_t)nsa * p * p) return fail(SHWFS_ERR_INVALID, "pupfn must be (nsubx,nsubx,phasesize,phasesize)");
+  if (is_none(in->subflag) || in->subflag.dtype != SHWFS_I32) return fail(SHWFS_ERR_INVALID, "subflag must be int32 and contiguous");
+  if (numel(in->subflag) != nsa) return fail(SHWFS_ERR_INVALID, "subflag must have nsubaps entries");
+  if (is_none(in->bimg) || check_f32(in->bimg, "bimg")) return fail(SHWFS_ERR_INVALID, "bimg must be float and contiguous");
+  if (numel(in->bimg) < (int64_t)nsa * m * m) return fail(SHWFS_ERR_INVALID, "bimg must hold nsubaps*nimg*nimg values");
+  if (is_none(in->fracSubArea) || check_f32(in->fracSubArea, "fracSubArea"))
+    return fail(SHWFS_ERR_INVALID, "fracSubArea must be float and contiguous");
+  if (numel(in->fracSubArea) != nsa) return fail(SHWFS_ERR_INVALID, "fracSubArea must have nsubaps entries");
+
+  h->readNoise = in->readnoise;
+  h->readBg = in->readbg;
+  h->threshType = in->threshType;
+  h->addPoisson = in->addPoisson;
+  h->noiseFloor = in->noiseFloor;
+  h->calsource = in->calsource;
+  h->pxlPower = in->pxlPower;
+  h->nintegrations = in->nintegrations;
+  h->nlatency = in->nlatency;
+  h->seed = in->seed;
+  h->opticalBinning = in->opticalBinning;
+  h->imageOnly = in->imageOnly;
+  h->corrThresh = in->corrThresh;
+  h->correlationCentroiding = in->correlationCentroiding;
+  if (h->nintegrations < 1) return fail(SHWFS_ERR_INVALID, "nintegrations must be >= 1");
+  if (h->nlatency < 0) return fail(SHWFS_ERR_INVALID, "nlatency must be >= 0");
+  if (in->nthreads < 1) return fail(SHWFS_ERR_INVALID, "nthreads must be >= 1");
+  if (!is_none(in->sigArr) && (check_f32(in->sigArr, "sig array") || in->sigArr.ndim != 1 ||
+                               in->sigArr.shape[0] != nsa))
+    return fail(SHWFS_ERR_INVALID, "sig arr dimensions must be 1D (nsubx^2)");
+  if (!is_none(in->skybrightnessArr) &&
+      (check_f32(in->skybrightnessArr, "skybrightness") || in->skybrightnessArr.ndim != 3 ||
+       in->skybrightnessArr.shape[0] != nsa || in->skybrightnessArr.shape[1] != m ||
+       in->skybrightnessArr.shape[2] != m))
+    return fail(SHWFS_ERR_INVALID, "skybrightness should be 3D array shape nsubaps,nimg,nimg");
+  if (!is_none(in->useBrightestArr) && (in->useBrightestArr.dtype != SHWFS_I32 ||
+                                        in->useBrightestArr.ndim != 1 || in->useBrightestArr.shape[0] != nsa))
+    return fail(SHWFS_ERR_INVALID, "useBrightest array should be 1D int32 of shape nsubaps (nsubx^2)");
+  if (!is_none(in->spotpsf)) {
+    const shwfs_array& ps = in->spotpsf;
+    if (ps.ndim != 2 && ps.ndim != 4) return fail(SHWFS_ERR_INVALID, "spotpsf not 2d or 4d");
+    if (check_f32(ps, "spotpsf")) return SHWFS_ERR_INVALID;
+    const int P = (int)ps.shape[ps.ndim - 1];
+    if (ps.shape[ps.ndim - 2] != P) return fail(SHWFS_ERR_INVALID, "spotpsf must be square");
+    if (ps.ndim == 4 && ps.shape[0] * ps.shape[1] != nsa)
+      return fail(SHWFS_ERR_INVALID, "spotpsf 4d must be (nsubx,nsubx,P,P)");
+    if (P < h->clipsize) return fail(SHWFS_ERR_INVALID, "spotpsf dimensions should be at least clipsize");
+  }
+  if (!is_none(in->centWeight)) {
+    const shwfs_array& cw = in->centWeight;
+    if (cw.ndim != 2 && cw.ndim != 4) return fail(SHWFS_ERR_INVALID, "centWeight not 2d or 4d");
+    if (check_f32(cw, "centWeight")) return SHWFS_ERR_INVALID;
+    if (cw.shape[cw.ndim - 2] != m || cw.shape[cw.ndim - 1] != m)
+      return fail(SHWFS_ERR_INVALID, "centweight array not correct dimensions (need to be nsubx,nsubx,corrsize,corrsize)");
+  }
+
+  CK(cudaGetDevice(&h->device));
+  CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  CK(cudaDeviceGetAttribute(&h->numSMs, cudaDevAttrMultiProcessorCount, h->device));
+
+  shwfs_status s;
+  if ((s = set_sig(h, in->sig, &in->sigArr))) return s;
+  if ((s = set_sky(h, in->skybrightness, &in->skybrightnessArr))) return s;
+  if ((s = set_use_brightest(h, in->useBrightest, &in->useBrightestArr))) return s;
+
+  h->subflag = to_host<int>(in->subflag);
+  h->pup = to_host<float>(in->pupfn);
+  h->frac = to_host<float>(in->fracSubArea);
+  for (int i = 0; i < nsa; i++) (h->subflag[i] == 1 ? h->lit : h->unlit).push_back(i);
+  CK(h->d_subflag.upload(h->subflag.data(), nsa));
+  CK(h->d_lit.upload(h->lit.data(), h->lit.size()));
+  CK(h->d_unlit.upload(h->unlit.data(), h->unlit.size()));
+  CK(h->d_pup.upload(h->pup.data(), h->pup.size()));
+  CK(h->d_frac.upload(h->frac.data(), nsa));
+  CK(h->d_poisFlag.alloc(nsa));
+  CK(h->d_status.alloc(1));
+  CK(cudaMemset(h->d_status.p, 0, sizeof(int)));
+
+  // tiltfn (cmod/src/centmodule.c:3074-3081)
+  std::vector<float> tilt((size_t)p * p);
+  const float tmp = (float)(M_PI / h->fftsize * (h->fftsize + 1.));
+  for (int i = 0; i < p; i++)
+    for (int j = 0; j < p; j++) tilt[i * p + j] = tmp * (float)(i + j + 1 - p);
+  CK(h->d_tilt.upload(tilt.data(), tilt.size()));
+
+  if ((s = set_spot_psf(h, in->spotpsf))) return s;
+  if ((s = set_cent_weight(h, in->centWeight))) return s;
+  if ((s = setup_threads(h, in->nthreads))) return s;
+  if ((s = prepare_bin(h))) return s;
+  if ((s = update_totsig(h))) return s;
+  if ((s = plan(h))) return s;
+
+  const size_t nph = (size_t)numel(in->phs);
+  if ((s = bind_io(h, h->phs, in->phs, h->d_phs, nph, false))) return s;
+  if ((s = bind_io(h, h->cents, in->cents, h->d_cents, (size_t)nsa * 2, true))) return s;
+  if ((s = bind_io(h, h->bimg, in->bimg, h->d_bimg, (size_t)nsa * m * m, true))) return s;
+
+  guard.h = nullptr;
+  *out = h;
+  return SHWFS_OK;
+}
+
+shwfs_status shwfs_run(shwfs_handle* h, float* elapsed_s) {
+  if (!h) return fail(SHWFS_ERR_INVALID, "null handle");
+  return run_impl(h, nullptr, true, elapsed_s);
+}
+
+shwfs_status shwfs_run_async(shwfs_handle* h, void* stream) {
+  if (!h) return fail(SHWFS_ERR_INVALID, "null handle");
+  return run_impl(h, (cudaStream_t)stream, false, nullptr);
+}
+
+shwfs_status shwfs_run_slope(shwfs_handle* h, float* elapsed_s) {
+  if (!h) return fail(SHWFS_ERR_INVALID, "null handle");
+  (void)elapsed_s;
+  return fail(SHWFS_ERR_STATE, "centmodule - inputImage is NULL");
+}
+
+shwfs_status shwfs_run_batch(shwfs_handle* h, int nframes, const float* phs, int64_t phs_frame_stride, float* cents,
+                             float* bimg, void* stream) {
+  if (!h) return fail(SHWFS_ERR_INVALID, "null handle");
+  if (nframes < 1 || !phs || !cents || !bimg) return fail(SHWFS_ERR_INVALID, "bad batch arguments");
+  if (h->noiseMode == SHWFS_NOISE_REFERENCE && nframes != 1)
+    return fail(SHWFS_ERR_UNSUPPORTED, "reference-stream noise runs one frame at a time");
+  cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
+  shwfs_status s = enqueue_readout(h, phs, cents, bimg, nframes, phs_frame_stride, st);
+  if (s) return s;
+  h->framesRead += nframes;
+  return SHWFS_OK;
+}
+
+shwfs_status shwfs_set_io(shwfs_handle* h, const shwfs_array* phs, const shwfs_array* cents, const shwfs_array* bimg) {
+  if (!h) return fail(SHWFS_ERR_INVALID, "null handle");
+  shwfs_status s;
+  if (phs) {
+    if (numel(*phs) != numel(h->phs) || phs->dtype != SHWFS_F32) return fail(SHWFS_ERR_INVALID, "phs shape mismatch");
+    if ((s = bind_io(h, h->phs, *phs, h->d_phs, (size_t)numel(*phs), false))) return s;
+  }
+  if (cents) {
+    if (numel(*cents) < 2LL * h->nsubaps || cents->dtype != SHWFS_F32) return fail(SHWFS_ERR_INVALID, "cents shape mismatch");
+    if ((s = bind_io(h, h->cents, *cents, h->d_cents, (size_t)h->nsubaps * 2, true))) return s;
+  }
+  if (bimg) {
+    if (numel(*bimg) < (int64_t)h->nsubaps * h->nimg * h->nimg || bimg->dtype != SHWFS_F32)
+      return fail(SHWFS_ERR_INVALID, "bimg shape mismatch");
+    if ((s = bind_io(h, h->bimg, *bimg, h->d_bimg, (size_t)h->nsubaps * h->nimg * h->nimg, true))) return s;
+  }
+  return SHWFS_OK;
+}
+
+shwfs_status shwfs_update(shwfs_handle* h, int code, const shwfs_value* v) {
+  if (!h || !v) return fail(SHWFS_ERR_INVALID, "null argument");
+  g_err.clear();
+  CK(cudaSetDevice(h->device));
+  auto need = [&](int kind, const char* what) -> shwfs_status {
+    if (v->kind != kind) return fail(SHWFS_ERR_INVALID, "centmodule: Error extracting %s value", what);
+    return SHWFS_OK;
+  };
+  auto num = [&](const char* what, double* out) -> shwfs_status {
+    if (v->kind == SHWFS_VAL_FLOAT) {
+      *out = v->dval;
+      return SHWFS_OK;
+    }
+    if (v->kind == SHWFS_VAL_INT) {
+      *out = (double)v->ival;
+      return SHWFS_OK;
+    }
+    return fail(SHWFS_ERR_INVALID, "centmodule: Error extracting float value for %s", what);
+  };
+  shwfs_status s = SHWFS_OK;
+  double d = 0;
+  switch (code) {
+    case SHWFS_CALSOURCE:
+      if ((s = need(SHWFS_VAL_INT, "integer"))) return s;
+      h->calsource = (int)v->ival;
+      break;
+    case SHWFS_SIG:
+      if (v->kind == SHWFS_VAL_ARRAY) return set_sig(h, 0, &v->arr[0]);
+      if ((s = num("sig", &d))) return s;
+      h->sig = (float)d;
+      return update_totsig(h);
+    case SHWFS_ADDPOISSON:
+      if ((s = need(SHWFS_VAL_INT, "integer"))) return s;
+      h->addPoisson = (int)v->ival;
+      break;
+    case SHWFS_NCEN:
+      if ((s = need(SHWFS_VAL_INT, "integer"))) return s;
+      if (v->ival < 1 || v->ival > h->nimg) return fail(SHWFS_ERR_INVALID, "ncen must be in [1, nimg]");
+      h->ncen = (int)v->ival;
+      break;
+    case SHWFS_READNOISE:
+      if ((s = num("readnoise", &d))) return s;
+      h->readNoise = (float)d;
+      break;
+    case SHWFS_READBG:
+      if ((s = num("readbg", &d))) return s;
+      h->readBg = (float)d;
+      break;
+    case SHWFS_NOISEFLOOR:
+      if ((s = num("noisefloor", &d))) return s;
+      h->noiseFloor = (float)d;
+      break;
+    case SHWFS_SKYBRIGHTNESS:
+      if (v->kind == SHWFS_VAL_ARRAY) return set_sky(h, 0, &v->arr[0]);
+      if ((s = num("skybrightness", &d))) return s;
+      return set_sky(h, d, nullptr);
+    case SHWFS_PXLPOWER:
+      if ((s = num("pxlpower", &d))) return s;
+      h->pxlPower = (float)d;
+      break;
+    case SHWFS_SPOTPSF: {
+      shwfs_array none{};
+      if ((s = set_spot_psf(h, v->kind == SHWFS_VAL_ARRAY ? v->arr[0] : none))) return s;
+      if ((s = update_totsig(h))) return s;
+      return plan(h);
+    }
+    case SHWFS_NTHREADS:
+      if ((s = need(SHWFS_VAL_INT, "int"))) return s;
+      return setup_threads(h, (int)v->ival);
+    case SHWFS_OPTICALBINNING:
+      if ((s = need(SHWFS_VAL_INT, "int"))) return s;
+      h->opticalBinning = (int)v->ival;
+      break;
+    case SHWFS_CENTWEIGHT: {
+      shwfs_array none{};
+      if ((s = set_cent_weight(h, v->kind == SHWFS_VAL_ARRAY ? v->arr[0] : none))) return s;
+      return plan(h);
+    }
+    case SHWFS_CORRELATIONCENTROIDING:
+      if ((s = need(SHWFS_VAL_INT, "int"))) return s;
+      if (v->ival != 0) return fail(SHWFS_ERR_UNSUPPORTED, "correlation centroiding is not implemented by this engine yet");
+      h->correlationCentroiding = 0;
+      break;
+    case SHWFS_CORRTHRESH:
+      if ((s = num("corrThresh", &d))) return s;
+      h->corrThresh = (float)d;
+      break;
+    case SHWFS_CORRPATTERN:
+      if (v->kind == SHWFS_VAL_ARRAY)
+        return fail(SHWFS_ERR_UNSUPPORTED, "correlation centroiding is not implemented by this engine yet");
+      break;
+    case SHWFS_CALDATA: {
+      if (v->kind == SHWFS_VAL_NONE) {
+        h->haveCalData = false;
+        h->calNSteps = 0;
+        break;
+      }
+      if (v->kind != SHWFS_VAL_TUPLE3) return fail(SHWFS_ERR_INVALID, "centmodule - calibration stuff not a tuple");
+      const shwfs_array &cd = v->arr[0], &cb = v->arr[1], &cs = v->arr[2];
+      if (check_f32(cd, "calData") || check_f32(cs, "calStep")) return fail(SHWFS_ERR_INVALID, "calData/calStep should be float32 contiguous");
+      if (cb.dtype != SHWFS_I32) return fail(SHWFS_ERR_INVALID, "calBounds should be int32 contiguous");
+      if (cs.ndim != 1) return fail(SHWFS_ERR_INVALID, "calStep should be 1d");
+      const int nsteps = (int)cs.shape[0];
+      if (cd.ndim != 4 || cd.shape[0] != 2 || cd.shape[1] * cd.shape[2] != h->nsubaps || cd.shape[3] != nsteps)
+        return fail(SHWFS_ERR_INVALID, "calData should be 4d, (2,nsubx,nsubx,steps)");
+      if (cb.ndim != 4 || cb.shape[0] != 2 || cb.shape[1] * cb.shape[2] != h->nsubaps || cb.shape[3] != 2)
+        return fail(SHWFS_ERR_INVALID, "calBounds should be 4d (2,nsubx,nsubx,2)");
+      std::vector<float> vd = to_host<float>(cd), vs = to_host<float>(cs);
+      std::vector<int> vb = to_host<int>(cb);
+      for (int k : vb)
+        if (k < 0 || k >= nsteps) return fail(SHWFS_ERR_INVALID, "calBounds entries must index calSteps");
+      CK(h->d_calData.upload(vd.data(), vd.size()));
+      CK(h->d_calSteps.upload(vs.data(), vs.size()));
+      CK(h->d_calBounds.upload(vb.data(), vb.size()));
+      h->calNSteps = nsteps;
+      h->haveCalData = true;
+      break;
+    }
+    case SHWFS_REFCENTS:
+      if (v->kind == SHWFS_VAL_ARRAY) {
+        if (check_f32(v->arr[0], "refCents")) return fail(SHWFS_ERR_INVALID, "refCents must be float contig array");
+        if (numel(v->arr[0]) < 2LL * h->nsubaps) return fail(SHWFS_ERR_INVALID, "refCents must hold nsubaps*2 values");
+        std::vector<float> r = to_host<float>(v->arr[0]);
+        CK(h->d_ref.upload(r.data(), (size_t)h->nsubaps * 2));
+        h->haveRef = true;
+      } else {
+        h->haveRef = false;
+      }
+      break;
+    case SHWFS_CALCOEFF:
+      if (v->kind == SHWFS_VAL_ARRAY) {
+        const shwfs_array& c = v->arr[0];
+        if (check_f32(c, "calCoeff")) return fail(SHWFS_ERR_INVALID, "calCoeff should be float32 contiguous");
+        if (c.ndim != 4 || c.shape[2] != 2 || c.shape[0] * c.shape[1] != h->nsubaps)
+          return fail(SHWFS_ERR_INVALID, "calCoeff should be 4d (nsubx,nsubx,2,ncoeff)");
+        std::vector<float> vc = to_host<float>(c);
+        CK(h->d_calCoeff.upload(vc.data(), vc.size()));
+        h->calNCoeff = (int)c.shape[3];
+        h->haveCalCoeff = true;
+      } else if (v->kind == SHWFS_VAL_NONE) {
+        h->haveCalCoeff = false;
+        h->calNCoeff = 0;
+      } else {
+        return fail(SHWFS_ERR_INVALID, "centmodule: Error in setCalCoeff");
+      }
+      break;
+    case SHWFS_USEBRIGHTEST:
+      if (v->kind == SHWFS_VAL_INT) return set_use_brightest(h, (int)v->ival, nullptr);
+      if (v->kind == SHWFS_VAL_ARRAY) return set_use_brightest(h, 0, &v->arr[0]);
+      return fail(SHWFS_ERR_INVALID, "centmodule: Error in set useBrightest");
+    case SHWFS_INTEGSTEPS:
+      if ((s = need(SHWFS_VAL_INT, "int"))) return fail(SHWFS_ERR_INVALID, "centmodule: Error in set integsteps");
+      if (v->ival < 1) return fail(SHWFS_ERR_INVALID, "integsteps must be >= 1");
+      h->nintegrations = (int)v->ival;
+      break;
+    case SHWFS_OUTPUTPHASEARR:
+      if (v->kind == SHWFS_VAL_ARRAY)
+        return fail(SHWFS_ERR_UNSUPPORTED, "interpolated-phase output is not implemented by this engine yet");
+      break;
+    case SHWFS_NOISEMODE:
+      if ((s = need(SHWFS_VAL_INT, "int"))) return s;
+      if (v->ival != SHWFS_NOISE_COUNTER && v->ival != SHWFS_NOISE_REFERENCE)
+        return fail(SHWFS_ERR_INVALID, "unknown noise mode %lld", (long long)v->ival);
+      h->noiseMode = (int)v->ival;
+      break;
+    default:
+      return fail(SHWFS_ERR_INVALID, "centmodule: Code %d not recognised, nothing updated", code);
+  }
+  return SHWFS_OK;
+}
+
+shwfs_status shwfs_free(shwfs_handle* h) {
+  if (!h) return SHWFS_OK;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  delete h;
+  return SHWFS_OK;
+}
+
+shwfs_status shwfs_get_info(const shwfs_handle* h, shwfs_info* info) {
+  if (!h || !info) return fail(SHWFS_ERR_INVALID, "null argument");
+  info->nsubx = h->nsubx;
+  info->nsubaps = h->nsubaps;
+  info->nlit = (int)h->lit.size();
+  info->fftsize = h->fftsize;
+  info->psfsize = h->psfsize;
+  info->clipsize = h->clipsize;
+  info->nimg = h->nimg;
+  info->phasesize = h->phasesize;
+  info->tile_subaps = h->TS;
+  info->smem_bytes = h->smem;
+  const long long ntiles = ((long long)h->lit.size() + h->TS - 1) / h->TS;
+  info->grid_ctas = (int)std::max<long long>(1, std::min<long long>(ntiles, (long long)h->numSMs * h->ctasPerSM));
+  info->noise_mode = h->noiseMode;
+  info->cur_integ = h->curInteg;
+  info->frames_read = h->framesRead;
+  return SHWFS_OK;
+}
+
+}  // extern "C"

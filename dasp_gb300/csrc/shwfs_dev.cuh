@@ -1,0 +1,205 @@
+// Device-side definitions shared by the WFS kernels: the per-launch argument
+// block, the counter-based noise generator and the twiddle table.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fft_reg.cuh"
+
+namespace shwfs {
+
+// pipeline pieces a launch performs (bit mask)
+enum : int {
+  kForm = 1,        // field -> FFT -> |F|^2 -> [prebin] -> [PSF] -> bin -> normalise -> sky
+  kNoiseCounter = 2,  // Poisson + read noise from the counter-based stream
+  kPost = 4,        // threshold .. centroids, bimg/cents written
+  kStorePreNoise = 8  // write the pre-noise image (and Poisson flag) to global memory
+};
+
+struct WfsArgs {
+  // geometry
+  int nsubx, nsubaps, p, N, C, m, ncen, P, padded, preBin;
+  int psfDim;    // 0 none, 2 one PSF, 4 one PSF per subaperture
+  int phaseAmp;  // 0 phase only, 1 phase + amplitude planes
+  int W;         // phase row width (elements)
+  long long phsFrameStride;
+  long long phsAmpOffset;  // elements from phase plane to amplitude plane
+  int nlit, nframes;
+  int TS;  // subapertures per CTA tile
+  const int* lit;
+  const float* phs;
+  const float* pup;
+  const float* tilt;
+  const float* frac;
+  const float* totsig;
+  float sig;
+  const float* sigArr;
+  float sky;
+  const float* skyArr;
+  const float2* psfSpec;  // [npsf][P][P/2+1]
+  const float* binT;
+  const float* binN;
+  const int* binII;  // output row of each input row
+  const int* binLo;  // first contributing input row per output row
+  const int* binHi;  // last contributing input row per output row
+  float readNoise, readBg, floorv;
+  int threshType, addPoisson, calsource;
+  int opticalBinning, imageOnly;
+  int useBrightest;
+  const int* useBrightestArr;
+  float pxlPower;
+  const float* centWeight;
+  int centWeightDim;
+  int cob;  // centre-on-brightest: 0 window, 1 brightest, other faintest
+  int fitSize, gaussianFit;
+  float gMin, gRep;
+  const float* fitMx;  // 5 x 6
+  const float* calData;
+  const int* calBounds;
+  const float* calSteps;
+  int calNSteps;
+  const float* calCoeff;
+  int calNCoeff;
+  const float* refCents;
+  float* bimg;
+  long long bimgFrameStride;
+  float* cents;
+  long long centsFrameStride;
+  unsigned char* poisFlag;  // per subap: Poisson applies (reference-stream mode)
+  unsigned long long seed;
+  unsigned long long frame0;
+  int mode;
+};
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as
+// easy as 1, 2, 3", SC'11): 10 rounds of two 32x32->64 multiplies with a
+// Weyl-sequence key schedule.
+// ---------------------------------------------------------------------------
+struct U4 {
+  uint32_t x, y, z, w;
+};
+
+__device__ __forceinline__ U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+    uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+    U4 n;
+    n.x = hi1 ^ c.y ^ k0;
+    n.y = lo1;
+    n.z = hi0 ^ c.w ^ k1;
+    n.w = lo0;
+    c = n;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return c;
+}
+
+// Sequential uniform stream for one (frame, subap, pixel, purpose).
+struct CounterStream {
+  U4 ctr;
+  uint32_t k0, k1;
+  U4 buf;
+  int avail;
+  __device__ __forceinline__ CounterStream(unsigned long long seed, unsigned long long frame, int subap,
+                                           int pixel, int purpose) {
+    k0 = (uint32_t)seed;
+    k1 = (uint32_t)(seed >> 32);
+    ctr.x = 0;
+    ctr.y = (uint32_t)pixel | ((uint32_t)purpose << 24);
+    ctr.z = (uint32_t)subap;
+    ctr.w = (uint32_t)frame;
+    avail = 0;
+  }
+  __device__ __forceinline__ uint32_t next_u32() {
+    if (avail == 0) {
+      buf = philox4x32_10(ctr, k0, k1);
+      ctr.x++;
+      avail = 4;
+    }
+    uint32_t v = avail == 4 ? buf.x : (avail == 3 ? buf.y : (avail == 2 ? buf.z : buf.w));
+    avail--;
+    return v;
+  }
+  // uniform in (0, 1): 24 random bits, centred in their bin
+  __device__ __forceinline__ float uniform() {
+    return ((float)(next_u32() >> 8) + 0.5f) * (1.0f / 16777216.0f);
+  }
+};
+
+// Poisson deviate with the reference's two regimes (cmod/src/centmodule.c:
+// 722-775): multiplication method below lambda 10, Hormann's PTRS
+// transformed rejection above; log-gamma by the Stirling series of :683-721.
+__device__ __forceinline__ float loggam_f(float x) {
+  const float a[10] = {8.333333333333333e-02f, -2.777777777777778e-03f, 7.936507936507937e-04f,
+                       -5.952380952380952e-04f, 8.417508417508418e-04f, -1.917526917526918e-03f,
+                       6.410256410256410e-03f, -2.955065359477124e-02f, 1.796443723688307e-01f,
+                       -1.39243221690590e+00f};
+  if (x == 1.0f || x == 2.0f) return 0.0f;
+  int n = 0;
+  float x0 = x;
+  if (x <= 7.0f) {
+    n = (int)(7.0f - x);
+    x0 = x + n;
+  }
+  float x2 = 1.0f / (x0 * x0);
+  float gl0 = a[9];
+#pragma unroll
+  for (int k = 8; k >= 0; k--) gl0 = gl0 * x2 + a[k];
+  float gl = gl0 / x0 + 0.918938533204672742f + (x0 - 0.5f) * logf(x0) - x0;
+  for (int k = 1; k <= n; k++) {
+    gl -= logf(x0 - 1.0f);
+    x0 -= 1.0f;
+  }
+  return gl;
+}
+
+__device__ __forceinline__ float poisson_counter(CounterStream& st, float lam) {
+  if (!(lam > 0.0f)) return 0.0f;
+  if (lam < 10.0f) {
+    float enlam = expf(-lam);
+    float prod = 1.0f;
+    int X = 0;
+    do {
+      prod *= st.uniform();
+      X++;
+    } while (prod > enlam && X < 1000);
+    return (float)(X - 1);
+  }
+  float slam = sqrtf(lam), loglam = logf(lam);
+  float b = 0.931f + 2.53f * slam;
+  float a = -0.059f + 0.02483f * b;
+  float invalpha = 1.1239f + 1.1328f / (b - 3.4f);
+  float vr = 0.9277f - 3.6224f / (b - 2.0f);
+  for (int it = 0; it < 1000; it++) {
+    float U = st.uniform() - 0.5f;
+    float V = st.uniform();
+    float us = 0.5f - fabsf(U);
+    float kf = floorf((2.0f * a / us + b) * U + lam + 0.43f);
+    if (us >= 0.07f && V <= vr) return kf;
+    if (kf < 0.0f || (us < 0.013f && V > us)) continue;
+    if (logf(V) + logf(invalpha) - logf(a / (us * us) + b) <= -lam + kf * loglam - loggam_f(kf + 1.0f))
+      return kf;
+  }
+  return floorf(lam + 0.5f);  // unreachable in practice: bounded loop
+}
+
+// one standard normal deviate (Box-Muller, cosine branch)
+__device__ __forceinline__ float normal_counter(CounterStream& st) {
+  float u1 = st.uniform(), u2 = st.uniform();
+  float r = sqrtf(-2.0f * logf(u1));
+  float s, c;
+  sincospif(2.0f * u2, &s, &c);
+  return r * c;
+}
+
+// readCCD threshold (cmod/src/centmodule.c:785-817)
+__device__ __forceinline__ float threshold_px(float v, float floorv, int threshType) {
+  if (threshType == 0) return v < floorv ? 0.0f : v - floorv;
+  if (threshType == 1) return v < floorv ? 0.0f : v;
+  return v;
+}
+
+}  // namespace shwfs

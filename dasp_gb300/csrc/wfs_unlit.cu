@@ -1,0 +1,41 @@
+// Unlit-subaperture kernel of the WFS step.
+#include "wfs_plain.cuh"
+
+namespace shwfs {
+
+// Unlit subapertures on a readout frame (cmod/src/centmodule.c:1964-1981):
+// centroids zeroed, or with imageOnly a noise-only image.
+__global__ void wfs_unlit_kernel(const WfsArgs a, const int* unlit, int nunlit) {
+  const int mm = a.m * a.m;
+  const long long total = (long long)nunlit * a.nframes * (a.imageOnly ? mm : 1);
+  for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < total;
+       w += (long long)gridDim.x * blockDim.x) {
+    if (!a.imageOnly) {
+      const int f = (int)(w / nunlit), i = unlit[w % nunlit];
+      float* c = a.cents + (long long)f * a.centsFrameStride;
+      c[2 * i] = 0.f;
+      c[2 * i + 1] = 0.f;
+    } else {
+      const long long q = w / mm;
+      const int pix = (int)(w - q * mm);
+      const int f = (int)(q / nunlit), i = unlit[q % nunlit];
+      float v = a.readBg;
+      const float rn = a.calsource == 0 ? a.readNoise : 0.f;
+      if (rn != 0.f) {
+        CounterStream st(a.seed, a.frame0 + f, i, pix, 1);
+        v = rn * normal_counter(st) + a.readBg;
+      }
+      a.bimg[(long long)f * a.bimgFrameStride + (long long)i * mm + pix] = threshold_px(v, a.floorv, a.threshType);
+    }
+  }
+}
+
+cudaError_t launch_unlit(const WfsArgs& a, const int* unlit, int nunlit, cudaStream_t stream) {
+  const long long total = (long long)nunlit * a.nframes * (a.imageOnly ? a.m * a.m : 1);
+  if (total == 0) return cudaSuccess;
+  const int blocks = (int)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
+  wfs_unlit_kernel<<<blocks, 256, 0, stream>>>(a, unlit, nunlit);
+  return cudaGetLastError();
+}
+
+}  // namespace shwfs

@@ -1,0 +1,219 @@
+/*
+ * shwfs.h -- C ABI of the GB300 Shack-Hartmann wavefront-sensor engine.
+ *
+ * Drop-in native boundary for the reference's per-frame WFS step, the
+ * Python extension ``cmod.cent`` built from cmod/src/centmodule.c and wrapped
+ * by util/centcmod.py.  Each entry point below names the reference function it
+ * replaces.  Signatures use plain pointers, sizes and status codes only; no
+ * Python, numpy or torch types cross this boundary.
+ *
+ * Arrays are described by ``shwfs_array`` (float32 or int32, C-contiguous).
+ * Like the reference, the phase input and the ``cents``/``bimg`` outputs are
+ * BORROWED: the engine keeps the pointers and reads/writes them on every
+ * run (cmod/src/centmodule.c:2934,3055-3058).  They may be host memory
+ * (copied to/from the GPU inside run) or CUDA device memory (used in place).
+ * Every other array is copied into device memory at initialise/update time,
+ * so a caller that edits one of them in place must call shwfs_update again.
+ *
+ * All calls return a shwfs_status; SHWFS_OK is 0.  shwfs_last_error() returns
+ * the message of the most recent failure on the calling thread.
+ */
+#ifndef SHWFS_H
+#define SHWFS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum shwfs_status {
+  SHWFS_OK = 0,
+  SHWFS_ERR_INVALID = 1,     /* bad argument: shape, dtype, value */
+  SHWFS_ERR_UNSUPPORTED = 2, /* valid in the reference, not implemented here */
+  SHWFS_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+  SHWFS_ERR_NOMEM = 4,       /* device or host allocation failed */
+  SHWFS_ERR_STATE = 5        /* call not valid in the handle's current state */
+} shwfs_status;
+
+/* update codes: identical values to util/centcmod.py:19-40 and
+ * cmod/src/centmodule.c:109-130 */
+enum {
+  SHWFS_CALSOURCE = 1,
+  SHWFS_SIG = 2,
+  SHWFS_ADDPOISSON = 3,
+  SHWFS_NCEN = 4,
+  SHWFS_READNOISE = 5,
+  SHWFS_READBG = 6,
+  SHWFS_NOISEFLOOR = 7,
+  SHWFS_SKYBRIGHTNESS = 8,
+  SHWFS_PXLPOWER = 9,
+  SHWFS_SPOTPSF = 10,
+  SHWFS_NTHREADS = 11,
+  SHWFS_OPTICALBINNING = 12,
+  SHWFS_CENTWEIGHT = 13,
+  SHWFS_CORRELATIONCENTROIDING = 14,
+  SHWFS_CORRTHRESH = 15,
+  SHWFS_CORRPATTERN = 16,
+  SHWFS_CALDATA = 17,
+  SHWFS_REFCENTS = 18,
+  SHWFS_CALCOEFF = 19,
+  SHWFS_USEBRIGHTEST = 20,
+  SHWFS_INTEGSTEPS = 21,
+  SHWFS_OUTPUTPHASEARR = 22,
+  /* extension (no reference counterpart): noise generator selection,
+   * ival = SHWFS_NOISE_COUNTER or SHWFS_NOISE_REFERENCE */
+  SHWFS_NOISEMODE = 100
+};
+
+/* noise generators */
+enum {
+  /* default: counter-based Philox4x32-10 streams keyed by (seed, frame,
+   * subaperture, pixel); fully parallel; matches the reference in
+   * distribution, not draw for draw */
+  SHWFS_NOISE_COUNTER = 0,
+  /* the reference's own streams: one PCG32 (Poisson) and one MT19937
+   * (read noise) per reference worker thread, seeded seed+t, walking the
+   * same static subaperture partition (cmod/src/centmodule.c:2535-2563) */
+  SHWFS_NOISE_REFERENCE = 1
+};
+
+enum { SHWFS_F32 = 0, SHWFS_I32 = 1 };
+
+typedef struct shwfs_array {
+  const void* data; /* NULL means None */
+  int ndim;
+  int64_t shape[4];
+  int dtype;     /* SHWFS_F32 or SHWFS_I32 */
+  int on_device; /* 1: CUDA device pointer; 0: host pointer */
+} shwfs_array;
+
+/* The 41 positional arguments of cmod.cent.initialise
+ * (cmod/src/centmodule.c:2876-2883, util/centcmod.py:115), in order.
+ * ``sig`` and ``skybrightness`` are either scalars or arrays: a non-NULL
+ * ``sigArr.data`` / ``skybrightnessArr.data`` selects the array form. */
+typedef struct shwfs_init {
+  int nthreads;
+  int nsubaps;
+  int ncen;
+  int fftsize;
+  int clipsize;
+  int nimg;
+  int phasesize;
+  float readnoise;
+  float readbg;
+  int addPoisson;
+  float noiseFloor;
+  double sig;
+  shwfs_array sigArr; /* float32 (nsubaps,) */
+  double skybrightness;
+  shwfs_array skybrightnessArr; /* float32 (nsubaps, nimg, nimg) */
+  int calsource;
+  float pxlPower;
+  int nintegrations;
+  int nlatency;
+  uint64_t seed;
+  shwfs_array phs;    /* float32 (W, W) phase or (2, W, W) phase + amplitude */
+  shwfs_array pupfn;  /* float32 (nsubx, nsubx, p, p) */
+  shwfs_array spotpsf; /* None, float32 (P, P) or (nsubx, nsubx, P, P) */
+  shwfs_array cents;  /* float32 output, nsubaps*2 values */
+  shwfs_array subflag; /* int32 (nsubx, nsubx) */
+  shwfs_array bimg;   /* float32 output (nsubx, nsubx, nimg, nimg) */
+  shwfs_array fracSubArea; /* float32 (nsubx, nsubx) */
+  int opticalBinning;
+  shwfs_array centWeight; /* None, float32 (corr, corr) or (nsubx, nsubx, corr, corr) */
+  int correlationCentroiding;
+  float corrThresh;
+  shwfs_array corrPattern;
+  shwfs_array corrimg;
+  int threshType;
+  int imageOnly;
+  int useBrightest;
+  shwfs_array useBrightestArr; /* None or int32 (nsubaps,) */
+  int preBinningFactor;
+  int parabolicFit;
+  int gaussianFit;
+  float gaussianMinVal;
+  float gaussianReplaceVal;
+  shwfs_array inputImage;
+  shwfs_array subapLocation;
+} shwfs_init;
+
+/* value passed to shwfs_update */
+enum {
+  SHWFS_VAL_NONE = 0,
+  SHWFS_VAL_INT = 1,
+  SHWFS_VAL_FLOAT = 2,
+  SHWFS_VAL_ARRAY = 3,
+  SHWFS_VAL_TUPLE3 = 4 /* (calData, calBounds, calSteps) for SHWFS_CALDATA */
+};
+typedef struct shwfs_value {
+  int kind;
+  int64_t ival;
+  double dval;
+  shwfs_array arr[3];
+} shwfs_value;
+
+typedef struct shwfs_info {
+  int nsubx, nsubaps, nlit;
+  int fftsize, psfsize, clipsize, nimg, phasesize;
+  int tile_subaps;      /* subapertures per CTA tile of the fused kernel */
+  int smem_bytes;       /* dynamic shared memory per CTA */
+  int grid_ctas;        /* CTAs launched per frame */
+  int noise_mode;
+  int cur_integ;
+  uint64_t frames_read; /* readout frames processed (noise counter) */
+} shwfs_info;
+
+typedef struct shwfs_handle shwfs_handle;
+
+/* cmod.cent.initialise: py_initialise, cmod/src/centmodule.c:2858-3161.
+ * Validates like the reference and uploads the constants. */
+shwfs_status shwfs_initialise(const shwfs_init* init, shwfs_handle** out);
+
+/* cmod.cent.run: py_run, cmod/src/centmodule.c:3188-3229.  One frame through
+ * the integration state machine; blocks until cents/bimg are written;
+ * *elapsed_s (may be NULL) receives the wall time in seconds. */
+shwfs_status shwfs_run(shwfs_handle* h, float* elapsed_s);
+
+/* cmod.cent.runSlope: py_runSlope, cmod/src/centmodule.c:3230-3272. */
+shwfs_status shwfs_run_slope(shwfs_handle* h, float* elapsed_s);
+
+/* cmod.cent.update: py_update, cmod/src/centmodule.c:2573-2856. */
+shwfs_status shwfs_update(shwfs_handle* h, int code, const shwfs_value* val);
+
+/* cmod.cent.free: py_free, cmod/src/centmodule.c:3163-3186. */
+shwfs_status shwfs_free(shwfs_handle* h);
+
+/* Message of the last failure on this thread ("" if none). */
+const char* shwfs_last_error(void);
+
+/* ---- extensions (no reference counterpart) ---- */
+
+/* shwfs_run without the final synchronisation: work is queued on ``stream``
+ * (a cudaStream_t; NULL = the handle's own stream).  Host outputs are valid
+ * once the stream has drained. */
+shwfs_status shwfs_run_async(shwfs_handle* h, void* stream);
+
+/* Independent readout frames in one launch, all pointers device memory:
+ * phase frames ``phs + f*phs_frame_stride`` (elements), outputs
+ * ``cents + f*nsubaps*2`` and ``bimg + f*nsubaps*nimg*nimg``.  The
+ * integration state is not consulted or advanced; the noise frame counter
+ * advances by nframes. */
+shwfs_status shwfs_run_batch(shwfs_handle* h, int nframes, const float* phs, int64_t phs_frame_stride,
+                             float* cents, float* bimg, void* stream);
+
+/* Rebind the borrowed phase / output arrays (same shapes as at initialise). */
+shwfs_status shwfs_set_io(shwfs_handle* h, const shwfs_array* phs, const shwfs_array* cents,
+                          const shwfs_array* bimg);
+
+shwfs_status shwfs_get_info(const shwfs_handle* h, shwfs_info* info);
+
+/* Library version string. */
+const char* shwfs_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SHWFS_H */

@@ -1,0 +1,113 @@
+"""The C ABI without a GPU: the library loads, exports every entry point that
+include/shwfs.h declares, the ctypes layouts match the header, and argument
+validation fails cleanly before any device work."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from tests.conftest import ROOT, gpu_available
+
+HEADER = os.path.join(ROOT, "include", "shwfs.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:shwfs_status|const char\*)\s+(shwfs_\w+)\s*\(", src, re.M)))
+
+
+def test_header_declares_reference_entry_points():
+    names = declared_functions()
+    for ref in ("shwfs_initialise", "shwfs_run", "shwfs_run_slope", "shwfs_update", "shwfs_free"):
+        assert ref in names
+
+
+def test_library_exports_every_declared_symbol(engine_lib):
+    from dasp_gb300 import _lib
+    names = declared_functions()
+    assert sorted(_lib.EXPORTS) == names
+    for n in names:
+        assert hasattr(engine_lib, n), n
+
+
+def test_version_string(engine_lib):
+    assert b"sm_103a" in engine_lib.shwfs_version()
+
+
+def test_update_codes_match_reference_module():
+    import dasp_gb300.centcmod as cc
+    src = open(HEADER).read()
+    for name in ("CALSOURCE", "SIG", "ADDPOISSON", "NCEN", "READNOISE", "READBG", "NOISEFLOOR", "SKYBRIGHTNESS",
+                 "PXLPOWER", "SPOTPSF", "NTHREADS", "OPTICALBINNING", "CENTWEIGHT", "CORRELATIONCENTROIDING",
+                 "CORRTHRESH", "CORRPATTERN", "CALDATA", "REFCENTS", "CALCOEFF", "USEBRIGHTEST", "INTEGSTEPS",
+                 "OUTPUTPHASEARR"):
+        m = re.search(r"SHWFS_%s\s*=\s*(\d+)" % name, src)
+        assert m and int(m.group(1)) == getattr(cc, name)
+    assert (cc.CALSOURCE, cc.REFCENTS, cc.OUTPUTPHASEARR) == (1, 18, 22)
+
+
+def _c_struct_sizes():
+    """sizeof the header's structs, from a tiny C program compiled here."""
+    import subprocess
+    import tempfile
+    d = tempfile.mkdtemp()
+    c = os.path.join(d, "s.c")
+    with open(c, "w") as fh:
+        fh.write('#include <stdio.h>\n#include "shwfs.h"\n#include <stddef.h>\nint main(){printf("%zu %zu %zu %zu %zu",'
+                 'sizeof(shwfs_array),sizeof(shwfs_init),sizeof(shwfs_value),sizeof(shwfs_info),'
+                 'offsetof(shwfs_init,subapLocation));return 0;}\n')
+    exe = os.path.join(d, "s")
+    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", exe])
+    return [int(x) for x in subprocess.check_output([exe]).split()]
+
+
+def test_ctypes_layout_matches_header():
+    from dasp_gb300._lib import ShwfsArray, ShwfsInfo, ShwfsInit, ShwfsValue
+    sa, si, sv, sinfo, off = _c_struct_sizes()
+    assert ctypes.sizeof(ShwfsArray) == sa
+    assert ctypes.sizeof(ShwfsInit) == si
+    assert ctypes.sizeof(ShwfsValue) == sv
+    assert ctypes.sizeof(ShwfsInfo) == sinfo
+    assert ShwfsInit.subapLocation.offset == off
+
+
+def _base_kwargs():
+    from tests.wfs_cases import Case
+    c = Case(nsubx=4, p=4, N=8, sig=100.0)
+    return c
+
+
+@pytest.mark.parametrize("mutate,exc", [
+    (lambda c: setattr(c, "phs", c.phs.astype(np.float64)), ValueError),
+    (lambda c: setattr(c, "phs", np.asfortranarray(np.zeros((16, 17), np.float32))[:, :16]), ValueError),
+    (lambda c: setattr(c, "psf", np.zeros((2, 2, 2), np.float32)), ValueError),
+    (lambda c: setattr(c, "psf", np.zeros((4, 4), np.float32)), ValueError),  # smaller than clipsize
+    (lambda c: c.params.update(sig=np.ones(5, np.float32)), ValueError),
+    (lambda c: c.params.update(skybrightness=np.ones((16, 4, 3), np.float32)), ValueError),
+    (lambda c: c.params.update(useBrightest=np.ones(16, np.int64)), ValueError),
+    (lambda c: c.params.update(centWeight=np.ones((3, 3), np.float32)), ValueError),
+    (lambda c: c.params.update(nthreads=0), ValueError),
+    (lambda c: c.params.update(nintegrations=0), ValueError),
+])
+def test_invalid_arguments_rejected_without_gpu(engine_lib, mutate, exc):
+    c = _base_kwargs()
+    mutate(c)
+    with pytest.raises(exc):
+        c.engine()
+
+
+def test_unsupported_paths_are_reported(engine_lib):
+    c = _base_kwargs()
+    c.params.update(correlationCentroiding=1)
+    with pytest.raises(NotImplementedError):
+        c.engine()
+
+
+@pytest.mark.skipif(gpu_available(), reason="checks the no-GPU error path")
+def test_valid_arguments_fail_loudly_without_gpu(engine_lib):
+    from dasp_gb300._lib import ShwfsError
+    c = _base_kwargs()
+    with pytest.raises(ShwfsError):
+        c.engine()
