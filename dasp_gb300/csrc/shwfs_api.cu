@@ -658,6 +658,11 @@ shwfs_status shwfs_initialise(const shwfs_init* in, shwfs_handle** out) {
   if (h->phasesize > h->fftsize) return fail(SHWFS_ERR_INVALID, "phasesize must not exceed fftsize");
   if (h->nimg > h->clipsize) return fail(SHWFS_ERR_INVALID, "nimg must not exceed clipsize");
   if (h->ncen < 1 || h->ncen > h->nimg) return fail(SHWFS_ERR_INVALID, "ncen must be in [1, nimg]");
+  if ((h->parabolicFit != 0 || h->gaussianFit > 0) && h->parabolicFit + h->gaussianFit > h->ncen)
+    return fail(SHWFS_ERR_INVALID, "fit size %d larger than the centroid window %d", h->parabolicFit + h->gaussianFit,
+                h->ncen);
+  if ((h->parabolicFit < 0 || h->gaussianFit > 0) && h->ncen < 3)
+    return fail(SHWFS_ERR_INVALID, "a fit needs a centroid window of at least 3 pixels");
   if (in->correlationCentroiding != 0)
     return fail(SHWFS_ERR_UNSUPPORTED, "correlation centroiding is not implemented by this engine yet");
   if (!is_none(in->inputImage) || !is_none(in->subapLocation))
