@@ -46,8 +46,10 @@ USEBRIGHTEST = 20
 INTEGSTEPS = 21  # should never be changed to something larger than the initial value
 OUTPUTPHASEARR = 22
 
+TILESUBAPS = 101  # extension: subapertures per CTA tile (0 = default)
+
 _INT_CODES = {CALSOURCE, ADDPOISSON, NCEN, NTHREADS, OPTICALBINNING, CORRELATIONCENTROIDING, INTEGSTEPS,
-              NOISEMODE}
+              NOISEMODE, TILESUBAPS}
 _INT_ARRAY_CODES = {USEBRIGHTEST}
 
 

@@ -24,6 +24,7 @@ struct RefNoiseArgs {
   int m, nexp;
   float readNoise, readBg, floorv;
   int threshType, addPoisson, calsource, imageOnly;
+  int imageInput;  // 1: runSlope frame -- lit subapertures draw nothing
 };
 
 // host-side seeding: pcg32_srandom_r(seed_t, 1) and gsl_rng_set(mt, seed_t)

@@ -122,6 +122,12 @@ struct shwfs_handle {
 
   // borrowed I/O
   shwfs_array phs{}, cents{}, bimg{};
+  shwfs_array inputImage{};           // borrowed detector image (runSlope)
+  int imageDims = 0, imageRows = 0, imageCols = 0;
+  std::vector<int> subapLoc;
+  float* bimgMapped = nullptr;        // device alias of a pinned host bimg
+  std::vector<float> bimgStage;       // fallback: full copy, then host scatter
+  bool scatterPending = false;
   std::vector<void*> registered;  // host ranges pinned by the engine
 
   // device state
@@ -131,11 +137,13 @@ struct shwfs_handle {
       d_calCoeff, d_fitMx, d_binT, d_binN, d_psf;
   DevBuf<int> d_lit, d_unlit, d_binII, d_binLo, d_binHi, d_ubArr, d_calBounds, d_subflag, d_subapStart, d_status;
   DevBuf<float2> d_psfSpec;
-  DevBuf<float> d_phs, d_cents, d_bimg;  // mirrors of host I/O
+  DevBuf<float> d_phs, d_cents, d_bimg, d_image;  // mirrors of host I/O
+  DevBuf<int> d_subapLoc;
   DevBuf<unsigned char> d_poisFlag;
   DevBuf<RefRng> d_rng;
   const PlainEntry* entry = nullptr;
   int TS = 1, smem = 0, ctasPerSM = 1, numSMs = 1;
+  int tileOverride = 0;  // SHWFS_TILESUBAPS; 0 = default
 
   ~shwfs_handle() {
     for (void* p : registered) cudaHostUnregister(p);
@@ -169,6 +177,13 @@ shwfs_status bind_io(shwfs_handle* h, shwfs_array& slot, const shwfs_array& a, D
       h->registered.push_back((void*)a.data);
   }
   cudaGetLastError();  // a refused registration only costs copy speed
+  if (&slot == &h->bimg) {
+    h->bimgMapped = nullptr;
+    if (cudaPointerGetAttributes(&attr, a.data) == cudaSuccess && attr.type == cudaMemoryTypeHost &&
+        attr.devicePointer)
+      h->bimgMapped = (float*)attr.devicePointer;
+    cudaGetLastError();
+  }
   // outputs start from the caller's contents: entries the engine does not
   // write (unlit subapertures, non-readout frames) come back unchanged
   if (copy_initial) CK(cudaMemcpy(mirror.p, a.data, count * sizeof(float), cudaMemcpyHostToDevice));
@@ -310,6 +325,7 @@ shwfs_status plan(shwfs_handle* h) {
   const int per = persub_floats(h->phasesize, h->fftsize, P, h->padded, h->clipsize, h->nimg);
   const int cst = const_floats(h->phasesize, h->clipsize, h->nimg, P, h->centWeightDim == 2, h->psfDim == 2);
   int TS = std::max(1, std::min(64, (kThreads + h->phasesize - 1) / h->phasesize));
+  if (h->tileOverride > 0) TS = std::min(64, h->tileOverride);
   while (TS > 1 && (size_t)(cst + TS * per) * 4 > 100 * 1024) TS--;
   const int smem = (cst + TS * per) * 4;
   if (smem > 227 * 1024) return fail(SHWFS_ERR_UNSUPPORTED, "subaperture too large for shared memory (%d bytes)", smem);
@@ -537,7 +553,7 @@ shwfs_status enqueue_readout(shwfs_handle* h, const float* phs, float* cents, fl
       WfsArgs a = make_args(h, phs, cents, bimg, 1, phsStride, kForm | kStorePreNoise);
       CK(h->entry->launch(a, grid, h->smem, st));
     }
-    RefNoiseArgs r;
+    RefNoiseArgs r{};
     r.nthreads = h->nthreads;
     r.subapStart = h->d_subapStart.p;
     r.subflag = h->d_subflag.p;
@@ -583,34 +599,110 @@ int readout_frame(const shwfs_handle* h) {
   return 1;
 }
 
-shwfs_status run_impl(shwfs_handle* h, cudaStream_t st, bool sync, float* elapsed) {
+// publish exactly what the reference writes on a readout frame: every
+// centroid unless imageOnly; every image with imageOnly, else the lit ones
+shwfs_status publish_outputs(shwfs_handle* h, cudaStream_t st, bool* sync) {
+  if (!h->cents.on_device && !h->imageOnly)
+    CK(cudaMemcpyAsync((void*)h->cents.data, h->d_cents.p, (size_t)h->nsubaps * 2 * sizeof(float),
+                       cudaMemcpyDeviceToHost, st));
+  if (!h->bimg.on_device) {
+    const size_t nb = (size_t)h->nsubaps * h->nimg * h->nimg;
+    if (h->imageOnly || h->unlit.empty()) {
+      CK(cudaMemcpyAsync((void*)h->bimg.data, h->d_bimg.p, nb * sizeof(float), cudaMemcpyDeviceToHost, st));
+    } else if (h->bimgMapped) {
+      CK(launch_publish(h->d_bimg.p, h->bimgMapped, h->d_lit.p, (int)h->lit.size(), h->nimg * h->nimg, st));
+    } else {
+      h->bimgStage.resize(nb);
+      CK(cudaMemcpyAsync(h->bimgStage.data(), h->d_bimg.p, nb * sizeof(float), cudaMemcpyDeviceToHost, st));
+      h->scatterPending = true;
+      *sync = true;
+    }
+  }
+  return SHWFS_OK;
+}
+
+// queue one image-input frame (centroidsFromImage)
+shwfs_status enqueue_slope(shwfs_handle* h, cudaStream_t st) {
+  const float* img = (const float*)h->inputImage.data;
+  if (!h->inputImage.on_device) {
+    CK(cudaMemcpyAsync(h->d_image.p, h->inputImage.data, (size_t)numel(h->inputImage) * sizeof(float),
+                       cudaMemcpyHostToDevice, st));
+    img = h->d_image.p;
+  }
+  float* cents = h->cents.on_device ? (float*)h->cents.data : h->d_cents.p;
+  float* bimg = h->bimg.on_device ? (float*)h->bimg.data : h->d_bimg.p;
+  const int mm = h->nimg * h->nimg;
+  if (!h->lit.empty()) {
+    WfsArgs a = make_args(h, nullptr, cents, bimg, 1, 0, kPost);
+    a.TS = std::max(1, std::min(64, 4096 / mm));
+    CK(launch_image(a, img, h->imageDims, h->imageCols, h->d_subapLoc.p, h->numSMs, st));
+  }
+  if (!h->unlit.empty()) {
+    WfsArgs a = make_args(h, nullptr, cents, bimg, 1, 0, 0);
+    if (h->noiseMode == SHWFS_NOISE_REFERENCE && h->imageOnly) {
+      RefNoiseArgs r{};
+      r.nthreads = h->nthreads;
+      r.subapStart = h->d_subapStart.p;
+      r.subflag = h->d_subflag.p;
+      r.poisFlag = h->d_poisFlag.p;
+      r.bimg = bimg;
+      r.m = h->nimg;
+      r.nexp = mm;
+      r.readNoise = h->readNoise;
+      r.readBg = h->readBg;
+      r.floorv = h->noiseFloor;
+      r.threshType = h->threshType;
+      r.addPoisson = h->addPoisson;
+      r.calsource = h->calsource;
+      r.imageOnly = h->imageOnly;
+      r.imageInput = 1;
+      CK(launch_refnoise(r, h->d_rng.p, h->d_status.p, st));
+    } else {
+      CK(launch_unlit(a, h->d_unlit.p, (int)h->unlit.size(), st));
+    }
+  }
+  return SHWFS_OK;
+}
+
+shwfs_status run_impl(shwfs_handle* h, cudaStream_t st, bool sync, float* elapsed, bool slope = false) {
   auto t0 = std::chrono::steady_clock::now();
   CK(cudaSetDevice(h->device));
   if (!st) st = h->stream;
-  const bool readout = readout_frame(h);
+  if (slope && is_none(h->inputImage)) return fail(SHWFS_ERR_STATE, "centmodule - inputImage is NULL");
+  if (!slope && is_none(h->phs)) return fail(SHWFS_ERR_STATE, "no phase array is bound (image-input handle)");
+  const bool readout = slope || readout_frame(h);
   if (readout) {
-    const size_t nph = (size_t)numel(h->phs);
-    const float* phs = (const float*)h->phs.data;
-    if (!h->phs.on_device) {
-      CK(cudaMemcpyAsync(h->d_phs.p, h->phs.data, nph * sizeof(float), cudaMemcpyHostToDevice, st));
-      phs = h->d_phs.p;
+    shwfs_status s;
+    if (slope) {
+      s = enqueue_slope(h, st);
+    } else {
+      const size_t nph = (size_t)numel(h->phs);
+      const float* phs = (const float*)h->phs.data;
+      if (!h->phs.on_device) {
+        CK(cudaMemcpyAsync(h->d_phs.p, h->phs.data, nph * sizeof(float), cudaMemcpyHostToDevice, st));
+        phs = h->d_phs.p;
+      }
+      float* cents = h->cents.on_device ? (float*)h->cents.data : h->d_cents.p;
+      float* bimg = h->bimg.on_device ? (float*)h->bimg.data : h->d_bimg.p;
+      s = enqueue_readout(h, phs, cents, bimg, 1, 0, st);
     }
-    float* cents = h->cents.on_device ? (float*)h->cents.data : h->d_cents.p;
-    float* bimg = h->bimg.on_device ? (float*)h->bimg.data : h->d_bimg.p;
-    shwfs_status s = enqueue_readout(h, phs, cents, bimg, 1, 0, st);
     if (s) return s;
-    if (!h->cents.on_device)
-      CK(cudaMemcpyAsync((void*)h->cents.data, h->d_cents.p, (size_t)h->nsubaps * 2 * sizeof(float),
-                         cudaMemcpyDeviceToHost, st));
-    if (!h->bimg.on_device)
-      CK(cudaMemcpyAsync((void*)h->bimg.data, h->d_bimg.p, (size_t)h->nsubaps * h->nimg * h->nimg * sizeof(float),
-                         cudaMemcpyDeviceToHost, st));
+    if ((s = publish_outputs(h, st, &sync))) return s;
     h->framesRead++;
   }
-  h->curInteg++;
-  if (h->curInteg >= h->nintegrations + h->nlatency) h->curInteg = 0;
+  if (!slope) {
+    // py_run advances the integration counter; py_runSlope does not
+    h->curInteg++;
+    if (h->curInteg >= h->nintegrations + h->nlatency) h->curInteg = 0;
+  }
   if (sync) {
     CK(cudaStreamSynchronize(st));
+    if (h->scatterPending) {
+      const size_t mm = (size_t)h->nimg * h->nimg;
+      float* dst = (float*)h->bimg.data;
+      for (int i : h->lit) memcpy(dst + i * mm, h->bimgStage.data() + i * mm, mm * sizeof(float));
+      h->scatterPending = false;
+    }
     if (h->noiseMode == SHWFS_NOISE_REFERENCE && readout) {
       int status = 0;
       CK(cudaMemcpy(&status, h->d_status.p, sizeof(int), cudaMemcpyDeviceToHost));
@@ -665,27 +757,73 @@ shwfs_status shwfs_initialise(const shwfs_init* in, shwfs_handle** out) {
     return fail(SHWFS_ERR_INVALID, "a fit needs a centroid window of at least 3 pixels");
   if (in->correlationCentroiding != 0)
     return fail(SHWFS_ERR_UNSUPPORTED, "correlation centroiding is not implemented by this engine yet");
-  if (!is_none(in->inputImage) || !is_none(in->subapLocation))
-    return fail(SHWFS_ERR_UNSUPPORTED, "image input (runSlope) is not implemented by this engine yet");
-
   // arrays: validation as py_initialise, plus size checks the C code trusts;
   // everything that needs no GPU is checked before the first CUDA call
   const int p = h->phasesize, nsa = h->nsubaps, m = h->nimg;
   if (is_none(in->cents) || check_f32(in->cents, "cents")) return fail(SHWFS_ERR_INVALID, "cents must be float and contiguous");
   if (numel(in->cents) < 2LL * nsa) return fail(SHWFS_ERR_INVALID, "cents must hold nsubaps*2 values");
-  if (is_none(in->phs)) return fail(SHWFS_ERR_UNSUPPORTED, "phase input is required (image input not implemented)");
-  if (check_f32(in->phs, "phs")) return SHWFS_ERR_INVALID;
-  if (in->phs.ndim == 2)
-    h->phaseAmp = 0;
-  else if (in->phs.ndim == 3 && in->phs.shape[0] == 2)
-    h->phaseAmp = 1;
-  else
-    return fail(SHWFS_ERR_INVALID, "phase should be 2D or 3D (for phase+amp)");
   const int W = h->nsubx * p;
-  if (in->phs.shape[h->phaseAmp] != W || in->phs.shape[h->phaseAmp + 1] != W)
-    return fail(SHWFS_ERR_UNSUPPORTED, "phase of size %lldx%lld needs interpolation to %dx%d (not implemented yet)",
-                (long long)in->phs.shape[h->phaseAmp], (long long)in->phs.shape[h->phaseAmp + 1], W, W);
   h->W = W;
+  if (!is_none(in->phs)) {
+    if (check_f32(in->phs, "phs")) return SHWFS_ERR_INVALID;
+    if (in->phs.ndim == 2)
+      h->phaseAmp = 0;
+    else if (in->phs.ndim == 3 && in->phs.shape[0] == 2)
+      h->phaseAmp = 1;
+    else
+      return fail(SHWFS_ERR_INVALID, "phase should be 2D or 3D (for phase+amp)");
+    if (in->phs.shape[h->phaseAmp] != W || in->phs.shape[h->phaseAmp + 1] != W)
+      return fail(SHWFS_ERR_UNSUPPORTED, "phase of size %lldx%lld needs interpolation to %dx%d (not implemented yet)",
+                  (long long)in->phs.shape[h->phaseAmp], (long long)in->phs.shape[h->phaseAmp + 1], W, W);
+  }
+  // image input (cmod/src/centmodule.c:3117-3157)
+  if (!is_none(in->inputImage)) {
+    const shwfs_array& im = in->inputImage;
+    if (check_f32(im, "inputImage")) return fail(SHWFS_ERR_INVALID, "inputImage array must be float and contiguous");
+    if (im.ndim == 2) {
+      if (im.shape[0] * im.shape[1] != (int64_t)m * m * nsa)
+        return fail(SHWFS_ERR_INVALID, "inputImage should be %d x %d (is %lld x %lld)", m * h->nsubx, m * h->nsubx,
+                    (long long)im.shape[0], (long long)im.shape[1]);
+      h->imageDims = 2;
+      h->imageRows = (int)im.shape[0];
+      h->imageCols = (int)im.shape[1];
+    } else if (im.ndim == 4) {
+      if (im.shape[0] * im.shape[1] != nsa || im.shape[2] != m || im.shape[3] != m)
+        return fail(SHWFS_ERR_INVALID, "inputImage should be %dx%dx%dx%d", h->nsubx, h->nsubx, m, m);
+      h->imageDims = 4;
+      h->imageRows = h->imageCols = m;
+    } else {
+      return fail(SHWFS_ERR_INVALID, "inputImage should be 2D or 4D");
+    }
+  }
+  if (!is_none(in->subapLocation)) {
+    const shwfs_array& sl = in->subapLocation;
+    if (sl.dtype != SHWFS_I32) return fail(SHWFS_ERR_INVALID, "subapLocation array must be int32 and contiguous");
+    if (numel(sl) != 4LL * nsa)
+      return fail(SHWFS_ERR_INVALID, "subapLocation array should be of size %d (is %lld)", nsa * 4, (long long)numel(sl));
+    h->subapLoc = to_host<int>(sl);
+  }
+  if (h->imageDims == 2) {
+    // every window must lie inside the image and fit the nimg x nimg image
+    for (int i = 0; i < nsa; i++) {
+      int r0, r1, c0, c1;
+      if (!h->subapLoc.empty()) {
+        r0 = h->subapLoc[i * 4];
+        r1 = h->subapLoc[i * 4 + 1];
+        c0 = h->subapLoc[i * 4 + 2];
+        c1 = h->subapLoc[i * 4 + 3];
+      } else {
+        r0 = (i / h->nsubx) * m;
+        r1 = r0 + m;
+        c0 = (i % h->nsubx) * m;
+        c1 = c0 + m;
+      }
+      if (r0 < 0 || c0 < 0 || r1 < r0 || c1 < c0 || r1 - r0 > m || c1 - c0 > m || r1 > h->imageRows ||
+          c1 > h->imageCols)
+        return fail(SHWFS_ERR_INVALID, "subaperture %d window [%d:%d,%d:%d] does not fit the image or nimg", i, r0, r1,
+                    c0, c1);
+    }
+  }
   if (is_none(in->pupfn) || check_f32(in->pupfn, "pupfn")) return fail(SHWFS_ERR_INVALID, "pupfn must be float and contiguous");
   if (numel(in->pupfn) != (int64_t)nsa * p * p) return fail(SHWFS_ERR_INVALID, "pupfn must be (nsubx,nsubx,phasesize,phasesize)");
   if (is_none(in->subflag) || in->subflag.dtype != SHWFS_I32) return fail(SHWFS_ERR_INVALID, "subflag must be int32 and contiguous");
@@ -778,8 +916,14 @@ shwfs_status shwfs_initialise(const shwfs_init* in, shwfs_handle** out) {
   if ((s = update_totsig(h))) return s;
   if ((s = plan(h))) return s;
 
-  const size_t nph = (size_t)numel(in->phs);
-  if ((s = bind_io(h, h->phs, in->phs, h->d_phs, nph, false))) return s;
+  if (!is_none(in->phs)) {
+    const size_t nph = (size_t)numel(in->phs);
+    if ((s = bind_io(h, h->phs, in->phs, h->d_phs, nph, false))) return s;
+  }
+  if (!is_none(in->inputImage)) {
+    if ((s = bind_io(h, h->inputImage, in->inputImage, h->d_image, (size_t)numel(in->inputImage), false))) return s;
+  }
+  if (!h->subapLoc.empty()) CK(h->d_subapLoc.upload(h->subapLoc.data(), h->subapLoc.size()));
   if ((s = bind_io(h, h->cents, in->cents, h->d_cents, (size_t)nsa * 2, true))) return s;
   if ((s = bind_io(h, h->bimg, in->bimg, h->d_bimg, (size_t)nsa * m * m, true))) return s;
 
@@ -800,8 +944,7 @@ shwfs_status shwfs_run_async(shwfs_handle* h, void* stream) {
 
 shwfs_status shwfs_run_slope(shwfs_handle* h, float* elapsed_s) {
   if (!h) return fail(SHWFS_ERR_INVALID, "null handle");
-  (void)elapsed_s;
-  return fail(SHWFS_ERR_STATE, "centmodule - inputImage is NULL");
+  return run_impl(h, nullptr, true, elapsed_s, true);
 }
 
 shwfs_status shwfs_run_batch(shwfs_handle* h, int nframes, const float* phs, int64_t phs_frame_stride, float* cents,
@@ -995,6 +1138,11 @@ shwfs_status shwfs_update(shwfs_handle* h, int code, const shwfs_value* v) {
       if (v->kind == SHWFS_VAL_ARRAY)
         return fail(SHWFS_ERR_UNSUPPORTED, "interpolated-phase output is not implemented by this engine yet");
       break;
+    case SHWFS_TILESUBAPS:
+      if ((s = need(SHWFS_VAL_INT, "int"))) return s;
+      if (v->ival < 0 || v->ival > 64) return fail(SHWFS_ERR_INVALID, "tile size must be in [0, 64]");
+      h->tileOverride = (int)v->ival;
+      return plan(h);
     case SHWFS_NOISEMODE:
       if ((s = need(SHWFS_VAL_INT, "int"))) return s;
       if (v->ival != SHWFS_NOISE_COUNTER && v->ival != SHWFS_NOISE_REFERENCE)

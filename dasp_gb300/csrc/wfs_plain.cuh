@@ -192,6 +192,179 @@ __device__ inline void fit_centroid(const WfsArgs& a, float* img, float& ocx, fl
   ocy = cy;
 }
 
+// Stages 7-9 on a tile of ns subapertures whose images are in shared memory
+// (img_of(s)): brightest-pixel selection, pixel power, bimg write, centroids
+// with calibration and reference subtraction.  nexp_of(s) is the number of
+// exposed pixels of subaperture s (cmod/src/centmodule.c:1883-1961,
+// 2033-2107).
+template <class ImgOf, class NexpOf>
+__device__ __forceinline__ void post_tile(const WfsArgs& a, int ns, const int* s_subap, const int* s_frame,
+                                          const float* s_cw, ImgOf img_of, NexpOf nexp_of) {
+    const int tid = threadIdx.x;
+    const int m = a.m, mm = m * m;
+    // ---- 7: brightest-pixel selection (one warp per subap) ----
+    if (a.calsource == 0 && (a.useBrightest != 0 || a.useBrightestArr)) {
+      const int warp = tid >> 5, lane = tid & 31, nwarps = blockDim.x >> 5;
+      for (int s = warp; s < ns; s += nwarps) {
+        int ub = a.useBrightestArr ? a.useBrightestArr[s_subap[s]] : a.useBrightest;
+        bool subtract = false;
+        if (ub < 0) {
+          ub = -ub;
+          subtract = true;
+        }
+        if (!(ub > 0 && ub < nexp_of(s))) continue;
+        float* img = img_of(s);
+        const int pos = nexp_of(s) - ub;  // ascending sorted index of the threshold
+        float thr = 0.f;
+        bool found = false;
+        for (int j = lane; j < nexp_of(s); j += 32) {
+          const float xj = img[j];
+          int lt = 0, le = 0;
+          for (int k = 0; k < nexp_of(s); k++) {
+            lt += img[k] < xj;
+            le += img[k] <= xj;
+          }
+          if (lt <= pos && pos < le) {
+            thr = xj;
+            found = true;
+          }
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, found);
+        if (bal == 0u) continue;  // only with NaN pixels: leave the image as is
+        thr = __shfl_sync(0xffffffffu, thr, __ffs(bal) - 1);
+        float sub = 0.f;
+        if (subtract) {
+          float best = -INFINITY;
+          for (int j = lane; j < nexp_of(s); j += 32)
+            if (img[j] < thr) best = fmaxf(best, img[j]);
+          for (int o = 16; o; o >>= 1) best = fmaxf(best, __shfl_xor_sync(0xffffffffu, best, o));
+          sub = best == -INFINITY ? 0.f : best;
+        }
+        __syncwarp();
+        for (int j = lane; j < nexp_of(s); j += 32) {
+          const float v = img[j];
+          img[j] = v < thr ? 0.f : (subtract ? v - sub : v);
+        }
+      }
+      __syncthreads();
+    }
+
+    // ---- 8: pixel power, bimg write ----
+    for (int w = tid; w < ns * mm; w += blockDim.x) {
+      const int s = w / mm, pix = w - (w / mm) * mm;
+      float v = img_of(s)[pix];
+      if (pix < nexp_of(s)) {
+        if (a.pxlPower == 2.f)
+          v = v * v;
+        else if (a.pxlPower != 1.f && a.pxlPower != 0.f)
+          v = powf(v, a.pxlPower);
+        img_of(s)[pix] = v;
+      }
+      a.bimg[(long long)s_frame[s] * a.bimgFrameStride + (long long)s_subap[s] * mm + pix] = v;
+    }
+    if (a.imageOnly != 0) return;
+    __syncthreads();
+
+    // ---- 9: centroids, calibration, reference subtraction ----
+    const bool seqMode = a.opticalBinning == 1 || a.fitSize != 0 || a.gaussianFit > 0 || a.cob != 0;
+    if (seqMode) {
+      for (int s = tid; s < ns; s += blockDim.x) {
+        float* img = img_of(s);
+        const int i = s_subap[s];
+        float cx = 0.f, cy = 0.f;
+        if (a.opticalBinning == 1) {
+          const int ncen = a.ncen;
+          float sx = 0.f, sy = 0.f;
+          for (int k = 0; k < ncen; k++) {
+            sx += img[k];
+            cx += img[k] * k;
+            sy += img[k + ncen];
+            cy += img[k + ncen] * k;
+          }
+          if (sx > 0) cx = (float)(cx / sx - (ncen - 1) / 2.);
+          if (sy > 0) cy = (float)(cy / sy - (ncen - 1) / 2.);
+        } else if (a.fitSize != 0 || a.gaussianFit > 0) {
+          fit_centroid(a, img, cx, cy);
+        } else {
+          const int n = m, ncen = a.ncen;
+          float mx = 0.f;
+          int mpos = 0;
+          if (a.cob == 1) {
+            for (int k = 0; k < n * n; k++)
+              if (img[k] > mx) {
+                mx = img[k];
+                mpos = k;
+              }
+          } else {
+            for (int k = 0; k < n * n; k++)
+              if (img[k] < mx || mx == 0) {
+                mx = img[k];
+                mpos = k;
+              }
+          }
+          int sx = (int)(mpos % n - ncen / 2. + 0.5), sy = (int)(mpos / n - ncen / 2. + 0.5);
+          sx = max(0, min(sx, n - ncen));
+          sy = max(0, min(sy, n - ncen));
+          const float* wt = a.centWeightDim == 2 ? s_cw
+                            : (a.centWeightDim == 4 ? a.centWeight + (long long)i * mm : nullptr);
+          const float sgn = (wt == nullptr && a.cob != 1) ? -1.f : 1.f;
+          float sum = 0.f;
+          for (int r = sy; r < sy + ncen; r++)
+            for (int c = sx; c < sx + ncen; c++) {
+              float t = wt ? img[r * n + c] * wt[r * n + c] : img[r * n + c];
+              sum += t;
+              cx += sgn * t * c;
+              cy += sgn * t * r;
+            }
+          if (sum > 0) {
+            cx = cx / sum + sx;
+            cy = cy / sum + sy;
+            cx = (float)(cx - (n - 1) / 2.);
+            cy = (float)(cy - (n - 1) / 2.);
+          } else {
+            cx = cy = 0.f;
+          }
+        }
+        calibrate_and_store(a, i, s_frame[s], cx, cy);
+      }
+    } else {
+      // centred-window CoG: one warp per subap, lanes over window pixels
+      const int warp = tid >> 5, lane = tid & 31, nwarps = blockDim.x >> 5;
+      const int ncen = a.ncen;
+      const int sx = (m - ncen) / 2;
+      const int nwin = ncen * ncen;
+      for (int s = warp; s < ns; s += nwarps) {
+        const float* img = img_of(s);
+        const int i = s_subap[s];
+        const float* wt = a.centWeightDim == 2 ? s_cw
+                          : (a.centWeightDim == 4 ? a.centWeight + (long long)i * mm : nullptr);
+        float sum = 0.f, sxv = 0.f, syv = 0.f;
+        for (int k = lane; k < nwin; k += 32) {
+          const int r = sx + k / ncen, c = sx + k % ncen;
+          float t = img[r * m + c];
+          if (wt) t *= wt[r * m + c];
+          sum += t;
+          sxv += t * c;
+          syv += t * r;
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+          sum += __shfl_xor_sync(0xffffffffu, sum, o);
+          sxv += __shfl_xor_sync(0xffffffffu, sxv, o);
+          syv += __shfl_xor_sync(0xffffffffu, syv, o);
+        }
+        if (lane == 0) {
+          float cx = 0.f, cy = 0.f;
+          if (sum > 0.f) {
+            cx = (float)(sxv / sum - (m - 1) / 2.);
+            cy = (float)(syv / sum - (m - 1) / 2.);
+          }
+          calibrate_and_store(a, i, s_frame[s], cx, cy);
+        }
+      }
+    }
+}
+
 template <int N, int P>
 __global__ void __launch_bounds__(kThreads) wfs_plain_kernel(const WfsArgs a) {
   extern __shared__ float4 smem4[];
@@ -358,17 +531,28 @@ __global__ void __launch_bounds__(kThreads) wfs_plain_kernel(const WfsArgs a) {
           }
           __syncthreads();
         }
-        // ---- 3a: r2c rows of hll (P x P, stride P) -> spectrum rows in BUF_A ----
-        for (int w = tid; w < ns * P; w += blockDim.x) {
-          const int s = w / P, row = w - (w / P) * P;
-          const float* hll = BUF_B(s) + row * P;
-          float2 y[P];
+        // ---- 3a: r2c rows of hll (P x P, stride P) -> spectrum rows in BUF_A;
+        // two real rows per complex FFT: z = x + i y, X = (Z + conj Z(-k))/2,
+        // Y = (Z - conj Z(-k))/(2i) ----
+        constexpr int PH = (P + 1) / 2;
+        for (int w = tid; w < ns * PH; w += blockDim.x) {
+          const int s = w / PH, q = w - (w / PH) * PH;
+          const int r0 = 2 * q, r1 = 2 * q + 1;
+          const bool two = r1 < P;
+          const float* h0 = BUF_B(s) + r0 * P;
+          const float* h1 = h0 + P;
+          float2 z[P];
 #pragma unroll
-          for (int n = 0; n < P; n++) y[n] = make_float2(hll[n], 0.f);
-          fft<P, -1>(y);
-          float2* sp = reinterpret_cast<float2*>(BUF_A(s)) + row * HSS;
+          for (int n = 0; n < P; n++) z[n] = make_float2(h0[n], two ? h1[n] : 0.f);
+          fft<P, -1>(z);
+          float2* s0 = reinterpret_cast<float2*>(BUF_A(s)) + r0 * HSS;
+          float2* s1 = s0 + HSS;
 #pragma unroll
-          for (int k = 0; k < HS; k++) sp[k] = y[k];
+          for (int k = 0; k < HS; k++) {
+            const float2 a = z[k], b = z[(P - k) % P];
+            s0[k] = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
+            if (two) s1[k] = make_float2(0.5f * (a.y + b.y), -0.5f * (a.x - b.x));
+          }
         }
         __syncthreads();
         // ---- 3b: column FFT, * PSF spectrum, inverse column FFT ----
@@ -388,18 +572,37 @@ __global__ void __launch_bounds__(kThreads) wfs_plain_kernel(const WfsArgs a) {
         }
         __syncthreads();
         // ---- 3c: c2r rows of the clip window -> C x C in BUF_B ----
+        // two half-spectrum rows per complex inverse FFT (z = X + iY gives
+        // x + iy); the imaginary parts of the DC and Nyquist bins are
+        // ignored, as a c2r transform does
         const int off = (P - C) / 2;
-        for (int w = tid; w < ns * C; w += blockDim.x) {
-          const int s = w / C, orow = w - (w / C) * C;
-          const float2* sp = reinterpret_cast<const float2*>(BUF_A(s)) + (orow + off) * HSS;
+        const int CH = (C + 1) / 2;
+        for (int w = tid; w < ns * CH; w += blockDim.x) {
+          const int s = w / CH, q = w - (w / CH) * CH;
+          const int o0 = 2 * q, o1 = 2 * q + 1;
+          const bool two = o1 < C;
+          const float2* s0 = reinterpret_cast<const float2*>(BUF_A(s)) + (o0 + off) * HSS;
+          const float2* s1 = s0 + HSS;
           float2 z[P];
 #pragma unroll
-          for (int k = 0; k < P; k++) z[k] = k < HS ? sp[k] : cconj(sp[P - k]);
+          for (int k = 0; k < P; k++) {
+            float2 X = k < HS ? s0[k] : cconj(s0[P - k]);
+            float2 Y = two ? (k < HS ? s1[k] : cconj(s1[P - k])) : make_float2(0.f, 0.f);
+            if (k == 0 || 2 * k == P) {
+              X.y = 0.f;
+              Y.y = 0.f;
+            }
+            z[k] = make_float2(X.x - Y.y, X.y + Y.x);
+          }
           fft<P, 1>(z);
-          float* out = BUF_B(s) + orow * C;
+          float* out0 = BUF_B(s) + o0 * C;
+          float* out1 = out0 + C;
 #pragma unroll
           for (int n = 0; n < P; n++)
-            if (n >= off && n < off + C) out[n - off] = z[n].x;
+            if (n >= off && n < off + C) {
+              out0[n - off] = z[n].x;
+              if (two) out1[n - off] = z[n].y;
+            }
         }
         __syncthreads();
       }
@@ -506,16 +709,15 @@ __global__ void __launch_bounds__(kThreads) wfs_plain_kernel(const WfsArgs a) {
         const int i = s_subap[s];
         const unsigned long long fr = a.frame0 + s_frame[s];
         float v = IMG(s)[pix];
-        if (pois && SCAL(s)[0] != 0.f) {
-          CounterStream st(a.seed, fr, i, pix, 0);
-          v = poisson_counter(st, v);
-        }
-        if (rn != 0.f) {
-          CounterStream st(a.seed, fr, i, pix, 1);
-          v += rn * normal_counter(st) + a.readBg;
-        } else {
+        // one stream per pixel: the read-noise normal takes the first two
+        // uniforms, the Poisson sampler continues from the third
+        CounterStream st(a.seed, fr, i, pix, 0);
+        const float g = rn != 0.f ? normal_counter(st) : 0.f;
+        if (pois && SCAL(s)[0] != 0.f) v = poisson_counter(st, v);
+        if (rn != 0.f)
+          v += rn * g + a.readBg;
+        else
           v += a.readBg;
-        }
         IMG(s)[pix] = threshold_px(v, a.floorv, a.threshType);
       }
       __syncthreads();
@@ -523,167 +725,7 @@ __global__ void __launch_bounds__(kThreads) wfs_plain_kernel(const WfsArgs a) {
 
     if (!doPost) continue;
 
-    // ---- 7: brightest-pixel selection (one warp per subap) ----
-    if (a.calsource == 0 && (a.useBrightest != 0 || a.useBrightestArr)) {
-      const int warp = tid >> 5, lane = tid & 31, nwarps = blockDim.x >> 5;
-      for (int s = warp; s < ns; s += nwarps) {
-        int ub = a.useBrightestArr ? a.useBrightestArr[s_subap[s]] : a.useBrightest;
-        bool subtract = false;
-        if (ub < 0) {
-          ub = -ub;
-          subtract = true;
-        }
-        if (!(ub > 0 && ub < nexp)) continue;
-        float* img = IMG(s);
-        const int pos = nexp - ub;  // ascending sorted index of the threshold
-        float thr = 0.f;
-        bool found = false;
-        for (int j = lane; j < nexp; j += 32) {
-          const float xj = img[j];
-          int lt = 0, le = 0;
-          for (int k = 0; k < nexp; k++) {
-            lt += img[k] < xj;
-            le += img[k] <= xj;
-          }
-          if (lt <= pos && pos < le) {
-            thr = xj;
-            found = true;
-          }
-        }
-        const unsigned bal = __ballot_sync(0xffffffffu, found);
-        if (bal == 0u) continue;  // only with NaN pixels: leave the image as is
-        thr = __shfl_sync(0xffffffffu, thr, __ffs(bal) - 1);
-        float sub = 0.f;
-        if (subtract) {
-          float best = -INFINITY;
-          for (int j = lane; j < nexp; j += 32)
-            if (img[j] < thr) best = fmaxf(best, img[j]);
-          for (int o = 16; o; o >>= 1) best = fmaxf(best, __shfl_xor_sync(0xffffffffu, best, o));
-          sub = best == -INFINITY ? 0.f : best;
-        }
-        __syncwarp();
-        for (int j = lane; j < nexp; j += 32) {
-          const float v = img[j];
-          img[j] = v < thr ? 0.f : (subtract ? v - sub : v);
-        }
-      }
-      __syncthreads();
-    }
-
-    // ---- 8: pixel power, bimg write ----
-    for (int w = tid; w < ns * mm; w += blockDim.x) {
-      const int s = w / mm, pix = w - (w / mm) * mm;
-      float v = IMG(s)[pix];
-      if (pix < nexp) {
-        if (a.pxlPower == 2.f)
-          v = v * v;
-        else if (a.pxlPower != 1.f && a.pxlPower != 0.f)
-          v = powf(v, a.pxlPower);
-        IMG(s)[pix] = v;
-      }
-      a.bimg[(long long)s_frame[s] * a.bimgFrameStride + (long long)s_subap[s] * mm + pix] = v;
-    }
-    if (a.imageOnly != 0) continue;
-    __syncthreads();
-
-    // ---- 9: centroids, calibration, reference subtraction ----
-    const bool seqMode = a.opticalBinning == 1 || a.fitSize != 0 || a.gaussianFit > 0 || a.cob != 0;
-    if (seqMode) {
-      for (int s = tid; s < ns; s += blockDim.x) {
-        float* img = IMG(s);
-        const int i = s_subap[s];
-        float cx = 0.f, cy = 0.f;
-        if (a.opticalBinning == 1) {
-          const int ncen = a.ncen;
-          float sx = 0.f, sy = 0.f;
-          for (int k = 0; k < ncen; k++) {
-            sx += img[k];
-            cx += img[k] * k;
-            sy += img[k + ncen];
-            cy += img[k + ncen] * k;
-          }
-          if (sx > 0) cx = (float)(cx / sx - (ncen - 1) / 2.);
-          if (sy > 0) cy = (float)(cy / sy - (ncen - 1) / 2.);
-        } else if (a.fitSize != 0 || a.gaussianFit > 0) {
-          fit_centroid(a, img, cx, cy);
-        } else {
-          const int n = m, ncen = a.ncen;
-          float mx = 0.f;
-          int mpos = 0;
-          if (a.cob == 1) {
-            for (int k = 0; k < n * n; k++)
-              if (img[k] > mx) {
-                mx = img[k];
-                mpos = k;
-              }
-          } else {
-            for (int k = 0; k < n * n; k++)
-              if (img[k] < mx || mx == 0) {
-                mx = img[k];
-                mpos = k;
-              }
-          }
-          int sx = (int)(mpos % n - ncen / 2. + 0.5), sy = (int)(mpos / n - ncen / 2. + 0.5);
-          sx = max(0, min(sx, n - ncen));
-          sy = max(0, min(sy, n - ncen));
-          const float* wt = a.centWeightDim == 2 ? s_cw
-                            : (a.centWeightDim == 4 ? a.centWeight + (long long)i * mm : nullptr);
-          const float sgn = (wt == nullptr && a.cob != 1) ? -1.f : 1.f;
-          float sum = 0.f;
-          for (int r = sy; r < sy + ncen; r++)
-            for (int c = sx; c < sx + ncen; c++) {
-              float t = wt ? img[r * n + c] * wt[r * n + c] : img[r * n + c];
-              sum += t;
-              cx += sgn * t * c;
-              cy += sgn * t * r;
-            }
-          if (sum > 0) {
-            cx = cx / sum + sx;
-            cy = cy / sum + sy;
-            cx = (float)(cx - (n - 1) / 2.);
-            cy = (float)(cy - (n - 1) / 2.);
-          } else {
-            cx = cy = 0.f;
-          }
-        }
-        calibrate_and_store(a, i, s_frame[s], cx, cy);
-      }
-    } else {
-      // centred-window CoG: one warp per subap, lanes over window pixels
-      const int warp = tid >> 5, lane = tid & 31, nwarps = blockDim.x >> 5;
-      const int ncen = a.ncen;
-      const int sx = (m - ncen) / 2;
-      const int nwin = ncen * ncen;
-      for (int s = warp; s < ns; s += nwarps) {
-        const float* img = IMG(s);
-        const int i = s_subap[s];
-        const float* wt = a.centWeightDim == 2 ? s_cw
-                          : (a.centWeightDim == 4 ? a.centWeight + (long long)i * mm : nullptr);
-        float sum = 0.f, sxv = 0.f, syv = 0.f;
-        for (int k = lane; k < nwin; k += 32) {
-          const int r = sx + k / ncen, c = sx + k % ncen;
-          float t = img[r * m + c];
-          if (wt) t *= wt[r * m + c];
-          sum += t;
-          sxv += t * c;
-          syv += t * r;
-        }
-#pragma unroll
-        for (int o = 16; o; o >>= 1) {
-          sum += __shfl_xor_sync(0xffffffffu, sum, o);
-          sxv += __shfl_xor_sync(0xffffffffu, sxv, o);
-          syv += __shfl_xor_sync(0xffffffffu, syv, o);
-        }
-        if (lane == 0) {
-          float cx = 0.f, cy = 0.f;
-          if (sum > 0.f) {
-            cx = (float)(sxv / sum - (m - 1) / 2.);
-            cy = (float)(syv / sum - (m - 1) / 2.);
-          }
-          calibrate_and_store(a, i, s_frame[s], cx, cy);
-        }
-      }
-    }
+    post_tile(a, ns, s_subap, s_frame, s_cw, [&](int s) { return IMG(s); }, [&](int) { return nexp; });
 #undef SUB
 #undef BUF_A
 #undef BUF_B
@@ -695,5 +737,10 @@ __global__ void __launch_bounds__(kThreads) wfs_plain_kernel(const WfsArgs a) {
 
 // launcher of the unlit-subaperture kernel (wfs_unlit.cu)
 cudaError_t launch_unlit(const WfsArgs& a, const int* unlit, int nunlit, cudaStream_t stream);
+// image-input (runSlope) kernel over the lit subapertures (wfs_image.cu)
+cudaError_t launch_image(const WfsArgs& a, const float* img, int dims, int npxlx, const int* loc, int numSMs,
+                         cudaStream_t stream);
+// copy the listed subapertures' images src -> dst (dst: mapped host memory)
+cudaError_t launch_publish(const float* src, float* dst, const int* list, int n, int mm, cudaStream_t stream);
 
 }  // namespace shwfs

@@ -166,6 +166,8 @@ __global__ void refnoise_walker_kernel(RefNoiseArgs a, RefRng* rng, int* status)
   for (int i = a.subapStart[t]; i < a.subapStart[t + 1]; i++) {
     float* img = a.bimg + (long long)i * mm;
     if (a.subflag[i] == 1) {
+      // centroidsFromImage: readCCD without noise on lit subapertures (no draws)
+      if (a.imageInput) continue;
       if (pois && a.poisFlag[i])
         for (int k = 0; k < a.nexp; k++) img[k] = (float)poisson_ref(st, img[k], &guard);
       readccd_ref(st, img, a.nexp, a.readBg, rn, a.floorv, a.threshType);

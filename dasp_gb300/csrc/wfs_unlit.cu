@@ -30,6 +30,27 @@ __global__ void wfs_unlit_kernel(const WfsArgs a, const int* unlit, int nunlit) 
   }
 }
 
+// Copy the images of the listed subapertures from the device mirror to the
+// caller's host array (pinned and mapped, written through its device alias).
+__global__ void publish_subaps_kernel(const float* __restrict__ src, float* dst, const int* __restrict__ list, int n,
+                                      int mm) {
+  const long long total = (long long)n * mm;
+  for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < total;
+       w += (long long)gridDim.x * blockDim.x) {
+    const long long k = w / mm;
+    const long long off = (long long)list[k] * mm + (w - k * mm);
+    dst[off] = src[off];
+  }
+}
+
+cudaError_t launch_publish(const float* src, float* dst, const int* list, int n, int mm, cudaStream_t stream) {
+  const long long total = (long long)n * mm;
+  if (total == 0) return cudaSuccess;
+  const int blocks = (int)((total + 255) / 256 < 2048 ? (total + 255) / 256 : 2048);
+  publish_subaps_kernel<<<blocks, 256, 0, stream>>>(src, dst, list, n, mm);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_unlit(const WfsArgs& a, const int* unlit, int nunlit, cudaStream_t stream) {
   const long long total = (long long)nunlit * a.nframes * (a.imageOnly ? a.m * a.m : 1);
   if (total == 0) return cudaSuccess;

@@ -86,8 +86,7 @@ def lgs_psfs(nsubx: int, spotsize: int, fwhm_across: float = 1.2, max_elong: flo
     lx = launch_dist_frac * nsubx / 2.0 * np.cos(theta)
     ly = launch_dist_frac * nsubx / 2.0 * np.sin(theta)
     pos = np.arange(nsubx) - nsubx / 2.0 + 0.5
-    xs = pos[:, None] + lx
-    ys = pos[None, :] + ly
+    xs, ys = np.meshgrid(pos + lx, pos + ly, indexing="ij")
     r = np.sqrt(xs * xs + ys * ys)
     rmax = r.max() if r.max() > 0 else 1.0
     out = np.zeros((nsubx, nsubx, spotsize, spotsize), np.float32)

@@ -64,7 +64,10 @@ enum {
   SHWFS_OUTPUTPHASEARR = 22,
   /* extension (no reference counterpart): noise generator selection,
    * ival = SHWFS_NOISE_COUNTER or SHWFS_NOISE_REFERENCE */
-  SHWFS_NOISEMODE = 100
+  SHWFS_NOISEMODE = 100,
+  /* extension: subapertures per CTA tile of the fused kernel, ival = 0 picks
+   * the default for the geometry */
+  SHWFS_TILESUBAPS = 101
 };
 
 /* noise generators */

@@ -889,6 +889,77 @@ class CentOracle:
         ry = (ry - dt((n - 1) / 2.0)).astype(dt)
         return np.where(pos, rx, dt(0)), np.where(pos, ry, dt(0))
 
+    def run_slope(self, image, cents, bimg, subapLocation=None):
+        """py_runSlope -> centroidsFromImage (cmod/src/centmodule.c:1987-2127).
+
+        ``image`` is the 2-D detector image or a (nsubx,nsubx,nimg,nimg)
+        array; bimg/cents are updated in place as the reference does
+        (including keeping old bimg pixels outside a smaller window).
+        """
+        m, npxl = self.m, self.m * self.m
+        cents = cents.reshape(-1)
+        bimg = bimg.reshape(self.nsubaps, m, m)
+        lib = noise_lib()
+        readNoise = np.float32(self.readNoise * (self.calsource == 0))
+        loc = None if subapLocation is None else np.asarray(subapLocation, np.int32).reshape(-1)
+        for t in range(self.nthreads):
+            for i in range(self.subapStart[t], self.subapStart[t + 1]):
+                if self.subflag[i] == 1:
+                    b = np.ascontiguousarray(bimg[i].reshape(-1).astype(np.float32))
+                    if image.ndim == 2:
+                        if loc is None:
+                            r0 = (i // self.nsubx) * m
+                            r1 = r0 + m
+                            c0 = (i % self.nsubx) * m
+                            c1 = c0 + m
+                        else:
+                            r0, r1, c0, c1 = (int(x) for x in loc[i * 4:i * 4 + 4])
+                        for j in range(r1 - r0):
+                            b[j * m:j * m + (c1 - c0)] = image[r0 + j, c0:c1]
+                        nexp = (r1 - r0) * (c1 - c0)
+                    else:
+                        b[:] = image.reshape(self.nsubaps, npxl)[i]
+                        nexp = npxl
+                    if self.calsource == 0:
+                        lib.orc_readccd(self.mt[t].buf, b.ctypes.data, nexp, np.float32(0), np.float32(0),
+                                        self.noiseFloor, self.threshType)
+                        ub = self.useBrightest if self.useBrightestArr is None else int(self.useBrightestArr[i])
+                        sub = b[:nexp].astype(self.dt)
+                        self._brightest(sub, ub)
+                        b[:nexp] = sub
+                    if self.pxlPower == 2:
+                        b[:nexp] = b[:nexp] * b[:nexp]
+                    elif self.pxlPower != 1 and self.pxlPower != 0:
+                        b[:nexp] = np.power(b[:nexp], np.float32(self.pxlPower))
+                    bimg[i] = b.reshape(m, m)
+                    if self.imageOnly == 0:
+                        img = b.reshape(m, m).astype(self.dt)
+                        if self.opticalBinning == 1:
+                            cx, cy = self._ob_cents(img.reshape(-1))
+                        elif self.parabolicFit != 0 or self.gaussianFit > 0:
+                            cx, cy = self._fit(img, self.parabolicFit + self.gaussianFit, self.gaussianFit,
+                                               self.correlationCentroiding)
+                        else:
+                            if self.centWeightDim == 2:
+                                w = self.centWeight
+                            elif self.centWeightDim == 4:
+                                w = self.centWeight[i]
+                            else:
+                                w = None
+                            cx, cy = self._cog(img, w, self.correlationCentroiding)
+                        cx, cy = self._calibrate(i, cx, cy)
+                        cents[2 * i] = cx
+                        cents[2 * i + 1] = cy
+                else:
+                    if self.imageOnly == 0:
+                        cents[2 * i] = 0
+                        cents[2 * i + 1] = 0
+                    else:
+                        buf = np.zeros(npxl, np.float32)
+                        lib.orc_readccd(self.mt[t].buf, buf.ctypes.data, npxl, self.readBg, readNoise,
+                                        self.noiseFloor, self.threshType)
+                        bimg[i] = buf.reshape(m, m)
+
     def _ob_cents(self, flat):
         """computeOBCents: cmod/src/centmodule.c:853-872."""
         ncen = self.ncen

@@ -58,7 +58,7 @@ class Case:
         return ph
 
     # -- engine --
-    def engine(self, phs=None, cents=None, bimg=None):
+    def engine(self, phs=None, cents=None, bimg=None, inputImage=None, subapLocation=None, no_phase=False):
         from dasp_gb300.centcmod import centcmod
         p = self.params
         self.cents = np.zeros((self.nsubaps * 2,), np.float32) if cents is None else cents
@@ -66,10 +66,11 @@ class Case:
         return centcmod(p["nthreads"], self.nsubx, self.ncen, self.N, self.C, self.m, self.p, p["readnoise"],
                         p["readbg"], p["addPoisson"], p["noiseFloor"], p["sig"], p["skybrightness"],
                         p["calsource"], p["pxlPower"], p["nintegrations"], p["nlatency"], p["seed"],
-                        self.phs if phs is None else phs, self.pup, self.psf, self.cents, self.bimg,
-                        p["minarea"], p["opticalBinning"], p["centWeight"], p["correlationCentroiding"],
+                        None if no_phase else (self.phs if phs is None else phs), self.pup, self.psf, self.cents,
+                        self.bimg, p["minarea"], p["opticalBinning"], p["centWeight"], p["correlationCentroiding"],
                         p["corrThresh"], p["corrPattern"], p["corrimg"], p["threshType"], p["imageOnly"],
-                        p["useBrightest"], p["preBinningFactor"], p["parabolicFit"], p["gaussianFitVals"])
+                        p["useBrightest"], p["preBinningFactor"], p["parabolicFit"], p["gaussianFitVals"],
+                        inputImage, subapLocation)
 
     # -- oracle --
     def oracle(self, mode="f32"):
