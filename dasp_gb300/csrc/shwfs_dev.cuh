@@ -129,9 +129,8 @@ struct CounterStream {
   }
 };
 
-// Poisson deviate with the reference's two regimes (cmod/src/centmodule.c:
-// 722-775): multiplication method below lambda 10, Hormann's PTRS
-// transformed rejection above; log-gamma by the Stirling series of :683-721.
+// log Gamma(x) by the Stirling series with upward recursion below 7, as the
+// reference's loggam (cmod/src/centmodule.c:683-721), in float.
 __device__ __forceinline__ float loggam_f(float x) {
   const float a[10] = {8.333333333333333e-02f, -2.777777777777778e-03f, 7.936507936507937e-04f,
                        -5.952380952380952e-04f, 8.417508417508418e-04f, -1.917526917526918e-03f,
@@ -148,39 +147,48 @@ __device__ __forceinline__ float loggam_f(float x) {
   float gl0 = a[9];
 #pragma unroll
   for (int k = 8; k >= 0; k--) gl0 = gl0 * x2 + a[k];
-  float gl = gl0 / x0 + 0.918938533204672742f + (x0 - 0.5f) * logf(x0) - x0;
+  float gl = gl0 / x0 + 0.918938533204672742f + (x0 - 0.5f) * __logf(x0) - x0;
   for (int k = 1; k <= n; k++) {
-    gl -= logf(x0 - 1.0f);
+    gl -= __logf(x0 - 1.0f);
     x0 -= 1.0f;
   }
   return gl;
 }
 
+// Below lambda 10 a single uniform is inverted through the Poisson CDF by
+// sequential search (p_k = p_{k-1} lambda / k); above, Hormann's PTRS
+// transformed rejection as in the reference (cmod/src/centmodule.c:722-758),
+// which accepts on its first (U, V) pair about 90% of the time.  Both draw
+// from the pixel's counter stream, so one Philox block usually suffices.
 __device__ __forceinline__ float poisson_counter(CounterStream& st, float lam) {
   if (!(lam > 0.0f)) return 0.0f;
   if (lam < 10.0f) {
-    float enlam = expf(-lam);
-    float prod = 1.0f;
-    int X = 0;
-    do {
-      prod *= st.uniform();
-      X++;
-    } while (prod > enlam && X < 1000);
-    return (float)(X - 1);
+    const float u = st.uniform();
+    float p = __expf(-lam);
+    float F = p;
+    int k = 0;
+    // the tail bound (lambda < 10) keeps the search finite when float
+    // rounding leaves F just below u
+    while (u > F && k < 64) {
+      k++;
+      p *= __fdividef(lam, (float)k);
+      F += p;
+    }
+    return (float)k;
   }
-  float slam = sqrtf(lam), loglam = logf(lam);
-  float b = 0.931f + 2.53f * slam;
-  float a = -0.059f + 0.02483f * b;
-  float invalpha = 1.1239f + 1.1328f / (b - 3.4f);
-  float vr = 0.9277f - 3.6224f / (b - 2.0f);
+  const float slam = sqrtf(lam), loglam = __logf(lam);
+  const float b = 0.931f + 2.53f * slam;
+  const float a = -0.059f + 0.02483f * b;
+  const float lninvalpha = __logf(1.1239f + 1.1328f / (b - 3.4f));
+  const float vr = 0.9277f - 3.6224f / (b - 2.0f);
   for (int it = 0; it < 1000; it++) {
-    float U = st.uniform() - 0.5f;
-    float V = st.uniform();
-    float us = 0.5f - fabsf(U);
-    float kf = floorf((2.0f * a / us + b) * U + lam + 0.43f);
+    const float U = st.uniform() - 0.5f;
+    const float V = st.uniform();
+    const float us = 0.5f - fabsf(U);
+    const float kf = floorf((2.0f * a / us + b) * U + lam + 0.43f);
     if (us >= 0.07f && V <= vr) return kf;
     if (kf < 0.0f || (us < 0.013f && V > us)) continue;
-    if (logf(V) + logf(invalpha) - logf(a / (us * us) + b) <= -lam + kf * loglam - loggam_f(kf + 1.0f))
+    if (__logf(V) + lninvalpha - __logf(a / (us * us) + b) <= -lam + kf * loglam - loggam_f(kf + 1.0f))
       return kf;
   }
   return floorf(lam + 0.5f);  // unreachable in practice: bounded loop
@@ -188,11 +196,9 @@ __device__ __forceinline__ float poisson_counter(CounterStream& st, float lam) {
 
 // one standard normal deviate (Box-Muller, cosine branch)
 __device__ __forceinline__ float normal_counter(CounterStream& st) {
-  float u1 = st.uniform(), u2 = st.uniform();
-  float r = sqrtf(-2.0f * logf(u1));
-  float s, c;
-  sincospif(2.0f * u2, &s, &c);
-  return r * c;
+  const float u1 = st.uniform(), u2 = st.uniform();
+  const float r = sqrtf(-2.0f * __logf(u1));
+  return r * __cosf(6.28318530717958648f * u2 - 3.14159265358979324f) * -1.0f;
 }
 
 // readCCD threshold (cmod/src/centmodule.c:785-817)

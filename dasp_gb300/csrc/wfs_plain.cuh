@@ -356,8 +356,8 @@ __device__ __forceinline__ void post_tile(const WfsArgs& a, int ns, const int* s
         if (lane == 0) {
           float cx = 0.f, cy = 0.f;
           if (sum > 0.f) {
-            cx = (float)(sxv / sum - (m - 1) / 2.);
-            cy = (float)(syv / sum - (m - 1) / 2.);
+            cx = sxv / sum - 0.5f * (float)(m - 1);
+            cy = syv / sum - 0.5f * (float)(m - 1);
           }
           calibrate_and_store(a, i, s_frame[s], cx, cy);
         }
