@@ -33,7 +33,20 @@ NOISEMODE = 100
 # every entry point declared in include/shwfs.h
 EXPORTS = ("shwfs_initialise", "shwfs_run", "shwfs_run_slope", "shwfs_update", "shwfs_free",
            "shwfs_last_error", "shwfs_run_async", "shwfs_run_batch", "shwfs_set_io",
-           "shwfs_get_info", "shwfs_version")
+           "shwfs_get_info", "shwfs_version", "shwfs_image_centroids_noalloc")
+
+NOALLOC_MAX_SUBAPS = 65536
+
+
+class ShwfsImageJob(ctypes.Structure):
+    """shwfs_image_job: arguments of the allocation-free image centroiding call."""
+    _fields_ = [("nsubx", ctypes.c_int), ("nimg", ctypes.c_int), ("ncen", ctypes.c_int),
+                ("image_ndim", ctypes.c_int), ("image_rows", ctypes.c_int64), ("image_cols", ctypes.c_int64),
+                ("image", ctypes.c_void_p), ("subflag", ctypes.c_void_p), ("refCents", ctypes.c_void_p),
+                ("noiseFloor", ctypes.c_float), ("threshType", ctypes.c_int), ("calsource", ctypes.c_int),
+                ("useBrightest", ctypes.c_int), ("pxlPower", ctypes.c_float), ("imageOnly", ctypes.c_int),
+                ("readNoise", ctypes.c_float), ("readBg", ctypes.c_float), ("seed", ctypes.c_uint64),
+                ("frame", ctypes.c_uint64), ("cents", ctypes.c_void_p), ("bimg", ctypes.c_void_p)]
 
 
 class ShwfsArray(ctypes.Structure):
@@ -100,6 +113,7 @@ def lib() -> ctypes.CDLL:
         L.shwfs_get_info.argtypes = [vp, P(ShwfsInfo)]
         L.shwfs_version.restype = ctypes.c_char_p
         L.shwfs_version.argtypes = []
+        L.shwfs_image_centroids_noalloc.argtypes = [P(ShwfsImageJob), vp, ctypes.c_char_p, ctypes.c_size_t]
         for name in EXPORTS:
             if name not in ("shwfs_last_error", "shwfs_version"):
                 getattr(L, name).restype = ctypes.c_int

@@ -216,6 +216,52 @@ shwfs_status shwfs_get_info(const shwfs_handle* h, shwfs_info* info);
 /* Library version string. */
 const char* shwfs_version(void);
 
+/* ---- allocation-free image centroiding (no counterpart in the reference) ----
+ *
+ * For callers that cannot allocate GPU memory: a real-time control thread
+ * that must never call cudaMalloc/cudaFree while it runs (an allocation may
+ * wait for the whole device to synchronise), or an application whose device
+ * memory is all owned by its own allocator.  Such callers cannot create a
+ * shwfs handle, which allocates device copies of its configuration.
+ *
+ * shwfs_image_centroids_noalloc cuts the nsubx x nsubx subaperture images
+ * out of a detector image (2-D, tiled by nimg, or 4-D nsubx,nsubx,nimg,nimg),
+ * thresholds them and computes centre-of-gravity centroids, exactly as
+ * shwfs_run_slope does for a handle with the same settings and no
+ * subapLocation.  Every array is caller-owned device memory; the call
+ * allocates nothing.  Its only working memory (the lit/unlit subaperture
+ * lists) is a static device array of SHWFS_NOALLOC_MAX_SUBAPS entries each,
+ * about 512 KB held on every GPU that loads the library until the process
+ * exits; larger sensors are rejected with SHWFS_ERR_INVALID.
+ *
+ * The first call on a device looks up that array's device address (once per
+ * device); make that first call before any stream capture.  The call waits
+ * once on ``stream`` to read the subaperture counts.  All calls share the one
+ * array, which keeps the last call's contents (each call rebuilds what it
+ * reads), so calls whose GPU work overlaps -- other streams, other host
+ * threads -- race and must not be issued.  ``err`` (may be NULL) receives a
+ * message on failure. */
+#define SHWFS_NOALLOC_MAX_SUBAPS 65536
+typedef struct shwfs_image_job {
+  int nsubx, nimg, ncen;
+  int image_ndim;        /* 2: (image_rows, image_cols) detector image; 4: (nsubx,nsubx,nimg,nimg) */
+  int64_t image_rows, image_cols;
+  const float* image;    /* device */
+  const int* subflag;    /* device, int32, nsubx*nsubx: 1 = subaperture used */
+  const float* refCents; /* device, nsubx*nsubx*2 reference centroids, or NULL */
+  float noiseFloor;
+  int threshType;
+  int calsource;
+  int useBrightest;
+  float pxlPower;
+  int imageOnly;         /* 1: images only, unused subapertures get read noise */
+  float readNoise, readBg;
+  uint64_t seed, frame;  /* counter-based read-noise stream for imageOnly */
+  float* cents;          /* device output, nsubx*nsubx*2 */
+  float* bimg;           /* device output, nsubx*nsubx*nimg*nimg */
+} shwfs_image_job;
+shwfs_status shwfs_image_centroids_noalloc(const shwfs_image_job* job, void* stream, char* err, size_t errlen);
+
 #ifdef __cplusplus
 }
 #endif
