@@ -84,7 +84,8 @@ class ShwfsInfo(ctypes.Structure):
                 ("fftsize", ctypes.c_int), ("psfsize", ctypes.c_int), ("clipsize", ctypes.c_int),
                 ("nimg", ctypes.c_int), ("phasesize", ctypes.c_int), ("tile_subaps", ctypes.c_int),
                 ("smem_bytes", ctypes.c_int), ("grid_ctas", ctypes.c_int), ("noise_mode", ctypes.c_int),
-                ("cur_integ", ctypes.c_int), ("frames_read", ctypes.c_uint64)]
+                ("cur_integ", ctypes.c_int), ("frames_read", ctypes.c_uint64), ("form", ctypes.c_int),
+                ("form_active", ctypes.c_int)]
 
 
 _lib = None

@@ -47,9 +47,11 @@ INTEGSTEPS = 21  # should never be changed to something larger than the initial 
 OUTPUTPHASEARR = 22
 
 TILESUBAPS = 101  # extension: subapertures per CTA tile (0 = default)
+FORM = 102  # extension: compute form (FORMS below)
+FORMS = {"fp32": 0, "bf16": 1, "bf16x3": 2}
 
 _INT_CODES = {CALSOURCE, ADDPOISSON, NCEN, NTHREADS, OPTICALBINNING, CORRELATIONCENTROIDING, INTEGSTEPS,
-              NOISEMODE, TILESUBAPS}
+              NOISEMODE, TILESUBAPS, FORM}
 _INT_ARRAY_CODES = {USEBRIGHTEST}
 
 
@@ -255,6 +257,13 @@ class centcmod:
         (the reference's per-thread PCG32/MT19937 streams)."""
         code = {"counter": NOISE_COUNTER, "reference": NOISE_REFERENCE}[mode]
         self.update(NOISEMODE, code)
+
+    def set_form(self, form):
+        """Compute form: ``"fp32"`` (fused FP32 kernel, default), ``"bf16"`` or
+        ``"bf16x3"`` (GEMM-DFT on the tensor cores, one pass or split
+        products).  Configurations the GEMM kernel does not cover keep running
+        the FP32 form; ``info()["form_active"]`` tells which one runs."""
+        self.update(FORM, FORMS[form])
 
     def run_batch(self, phs_frames, cents_frames, bimg_frames, stream=None):
         """Independent readout frames from CUDA tensors in one launch.

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "../../include/shwfs.h"
+#include "gemm_form.h"
 #include "refnoise.h"
 #include "wfs_launch.cuh"
 
@@ -144,6 +145,13 @@ struct shwfs_handle {
   const PlainEntry* entry = nullptr;
   int TS = 1, smem = 0, ctasPerSM = 1, numSMs = 1;
   int tileOverride = 0;  // SHWFS_TILESUBAPS; 0 = default
+  // GEMM-DFT form
+  int form = SHWFS_FORM_FP32;
+  bool gemmBuilt = false;
+  GemmGeom gemm{};
+  DevBuf<uint8_t> d_w2, d_kc2;
+  std::vector<float> psfHost, binTHost, binNHost;
+  std::vector<int> binIdxHost;
 
   ~shwfs_handle() {
     for (void* p : registered) cudaHostUnregister(p);
@@ -252,6 +260,9 @@ shwfs_status prepare_bin(shwfs_handle* h) {
       lo[I] = 0;
       hi[I] = -1;
     }
+  h->binTHost = t;
+  h->binNHost = n;
+  h->binIdxHost = idx;
   CK(h->d_binT.upload(t.data(), C));
   CK(h->d_binN.upload(n.data(), C));
   CK(h->d_binII.upload(ii.data(), C));
@@ -295,6 +306,7 @@ shwfs_status set_spot_psf(shwfs_handle* h, const shwfs_array& psf) {
   entry = &it->second;
   if (dim) {
     std::vector<float> hp = to_host<float>(psf);
+    h->psfHost.assign(hp.begin(), hp.begin() + (dim == 2 ? (size_t)P * P : 0));
     const int npsf = dim == 2 ? 1 : h->nsubaps;
     h->psfSums.assign(npsf, 0.f);
     for (int k = 0; k < npsf; k++) {
@@ -534,6 +546,52 @@ WfsArgs make_args(shwfs_handle* h, const float* phs, float* cents, float* bimg, 
   return a;
 }
 
+// GEMM-DFT form: eligibility and device constants.  Configurations outside the
+// GEMM kernel (per-subaperture PSFs, phase+amplitude, optical binning,
+// reference-stream noise, phasesize > 10, nimg > 16) run the FP32 form.
+bool gemm_static_ok(const shwfs_handle* h, GemmGeom* g, GemmSpec* sp) {
+  if (h->psfDim == 4 || h->phaseAmp) return false;
+  sp->p = h->phasesize;
+  sp->N = h->fftsize;
+  sp->padded = h->padded;
+  sp->rs = h->padded > h->fftsize ? (h->padded - h->fftsize) / 2 : 0;
+  sp->ro = h->padded > h->fftsize ? 0 : (h->fftsize - h->padded) / 2;
+  sp->c = h->padded > h->fftsize ? h->fftsize : h->padded;
+  sp->P = h->psfsize;
+  sp->C = h->clipsize;
+  sp->m = h->nimg;
+  sp->preBin = h->preBin;
+  sp->psfDim = h->psfDim;
+  sp->psf = h->psfHost;
+  sp->binT = h->binTHost;
+  sp->binN = h->binNHost;
+  sp->binIdx = h->binIdxHost;
+  return gemm_geometry(*sp, g);
+}
+
+bool gemm_active(const shwfs_handle* h) {
+  return h->form != SHWFS_FORM_FP32 && h->gemmBuilt && h->opticalBinning != 1 &&
+         h->noiseMode == SHWFS_NOISE_COUNTER;
+}
+
+shwfs_status build_gemm(shwfs_handle* h) {
+  h->gemmBuilt = false;
+  if (h->form == SHWFS_FORM_FP32) return SHWFS_OK;
+  GemmSpec sp;
+  GemmGeom g{};
+  if (!gemm_static_ok(h, &g, &sp)) return SHWFS_OK;  // falls back to the FP32 form
+  std::vector<uint8_t> w2, kc2;
+  std::vector<double> kc;
+  gemm_build_w2(sp, g, w2);
+  gemm_kc_matrix(sp, kc);
+  gemm_build_kc(sp, g, kc, kc2);
+  CK(h->d_w2.upload(w2.data(), w2.size()));
+  CK(h->d_kc2.upload(kc2.data(), kc2.size()));
+  h->gemm = g;
+  h->gemmBuilt = true;
+  return SHWFS_OK;
+}
+
 // queue one readout over nframes frames (device pointers)
 shwfs_status enqueue_readout(shwfs_handle* h, const float* phs, float* cents, float* bimg, int nframes,
                              long long phsStride, cudaStream_t st) {
@@ -578,7 +636,13 @@ shwfs_status enqueue_readout(shwfs_handle* h, const float* phs, float* cents, fl
       CK(launch_unlit(a, h->d_unlit.p, (int)h->unlit.size(), st));
     }
   } else {
-    if (nlit) {
+    if (nlit && gemm_active(h)) {
+      WfsArgs a = make_args(h, phs, cents, bimg, nframes, phsStride, kForm | kNoiseCounter | kPost);
+      GemmGeom g = h->gemm;
+      g.w2 = h->d_w2.p;
+      g.kc2 = h->d_kc2.p;
+      CK(launch_gemm(a, g, h->form == SHWFS_FORM_BF16X3 ? 3 : 1, h->numSMs, h->d_status.p, st));
+    } else if (nlit) {
       WfsArgs a = make_args(h, phs, cents, bimg, nframes, phsStride, kForm | kNoiseCounter | kPost);
       CK(h->entry->launch(a, grid, h->smem, st));
     }
@@ -703,10 +767,11 @@ shwfs_status run_impl(shwfs_handle* h, cudaStream_t st, bool sync, float* elapse
       for (int i : h->lit) memcpy(dst + i * mm, h->bimgStage.data() + i * mm, mm * sizeof(float));
       h->scatterPending = false;
     }
-    if (h->noiseMode == SHWFS_NOISE_REFERENCE && readout) {
+    if ((h->noiseMode == SHWFS_NOISE_REFERENCE || gemm_active(h)) && readout) {
       int status = 0;
       CK(cudaMemcpy(&status, h->d_status.p, sizeof(int), cudaMemcpyDeviceToHost));
-      if (status) return fail(SHWFS_ERR_STATE, "reference-stream Poisson sampler hit its iteration limit");
+      if (status & 1) return fail(SHWFS_ERR_STATE, "reference-stream Poisson sampler hit its iteration limit");
+      if (status & 2) return fail(SHWFS_ERR_STATE, "tensor-core pipeline wait timed out (results invalid)");
     }
   }
   if (elapsed) *elapsed = std::chrono::duration<float>(std::chrono::steady_clock::now() - t0).count();
@@ -1043,7 +1108,8 @@ shwfs_status shwfs_update(shwfs_handle* h, int code, const shwfs_value* v) {
       shwfs_array none{};
       if ((s = set_spot_psf(h, v->kind == SHWFS_VAL_ARRAY ? v->arr[0] : none))) return s;
       if ((s = update_totsig(h))) return s;
-      return plan(h);
+      if ((s = plan(h))) return s;
+      return build_gemm(h);
     }
     case SHWFS_NTHREADS:
       if ((s = need(SHWFS_VAL_INT, "int"))) return s;
@@ -1138,6 +1204,12 @@ shwfs_status shwfs_update(shwfs_handle* h, int code, const shwfs_value* v) {
       if (v->kind == SHWFS_VAL_ARRAY)
         return fail(SHWFS_ERR_UNSUPPORTED, "interpolated-phase output is not implemented by this engine yet");
       break;
+    case SHWFS_FORM:
+      if ((s = need(SHWFS_VAL_INT, "int"))) return s;
+      if (v->ival != SHWFS_FORM_FP32 && v->ival != SHWFS_FORM_BF16 && v->ival != SHWFS_FORM_BF16X3)
+        return fail(SHWFS_ERR_INVALID, "unknown compute form %lld", (long long)v->ival);
+      h->form = (int)v->ival;
+      return build_gemm(h);
     case SHWFS_TILESUBAPS:
       if ((s = need(SHWFS_VAL_INT, "int"))) return s;
       if (v->ival < 0 || v->ival > 64) return fail(SHWFS_ERR_INVALID, "tile size must be in [0, 64]");
@@ -1180,6 +1252,8 @@ shwfs_status shwfs_get_info(const shwfs_handle* h, shwfs_info* info) {
   info->noise_mode = h->noiseMode;
   info->cur_integ = h->curInteg;
   info->frames_read = h->framesRead;
+  info->form = h->form;
+  info->form_active = gemm_active(h) ? h->form : SHWFS_FORM_FP32;
   return SHWFS_OK;
 }
 

@@ -155,21 +155,23 @@ __device__ __forceinline__ float loggam_f(float x) {
   return gl;
 }
 
-// Below lambda 10 a single uniform is inverted through the Poisson CDF by
-// sequential search (p_k = p_{k-1} lambda / k); above, Hormann's PTRS
+// Below lambda 30 a single uniform is inverted through the Poisson CDF by
+// sequential search (p_k = p_{k-1} lambda / k): a few FMAs per step, one
+// uniform, little divergence between lanes.  Above, Hormann's PTRS
 // transformed rejection as in the reference (cmod/src/centmodule.c:722-758),
-// which accepts on its first (U, V) pair about 90% of the time.  Both draw
-// from the pixel's counter stream, so one Philox block usually suffices.
+// whose quick-accept region grows with lambda.  Both draw from the pixel's
+// counter stream, so one Philox block usually suffices.
 __device__ __forceinline__ float poisson_counter(CounterStream& st, float lam) {
   if (!(lam > 0.0f)) return 0.0f;
-  if (lam < 10.0f) {
+  if (lam < 30.0f) {
     const float u = st.uniform();
     float p = __expf(-lam);
     float F = p;
     int k = 0;
-    // the tail bound (lambda < 10) keeps the search finite when float
-    // rounding leaves F just below u
-    while (u > F && k < 64) {
+    // bound far in the tail: keeps the search finite when float rounding
+    // leaves F just below u
+    const int kmax = (int)(lam + 10.0f * sqrtf(lam)) + 20;
+    while (u > F && k < kmax) {
       k++;
       p *= __fdividef(lam, (float)k);
       F += p;

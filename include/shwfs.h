@@ -67,7 +67,16 @@ enum {
   SHWFS_NOISEMODE = 100,
   /* extension: subapertures per CTA tile of the fused kernel, ival = 0 picks
    * the default for the geometry */
-  SHWFS_TILESUBAPS = 101
+  SHWFS_TILESUBAPS = 101,
+  /* extension: compute form, ival = SHWFS_FORM_FP32 / _BF16 / _BF16X3 */
+  SHWFS_FORM = 102
+};
+
+/* compute forms */
+enum {
+  SHWFS_FORM_FP32 = 0,   /* fused FP32 kernel, register FFTs (default) */
+  SHWFS_FORM_BF16 = 1,   /* GEMM-DFT on tcgen05 tensor cores, one bf16 pass */
+  SHWFS_FORM_BF16X3 = 2  /* GEMM-DFT, bf16 split products hi*hi + hi*lo + lo*hi */
 };
 
 /* noise generators */
@@ -167,6 +176,10 @@ typedef struct shwfs_info {
   int noise_mode;
   int cur_integ;
   uint64_t frames_read; /* readout frames processed (noise counter) */
+  int form;             /* requested SHWFS_FORM_* */
+  int form_active;      /* form the next readout will use (GEMM forms fall back to
+                           FP32 for 4-D PSFs, phase+amplitude, optical binning,
+                           reference-stream noise or sizes beyond the GEMM kernel) */
 } shwfs_info;
 
 typedef struct shwfs_handle shwfs_handle;
