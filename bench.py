@@ -82,6 +82,15 @@ def make_engine(pup, phs, cents, bimg, noiseless=False):
 
 # ---------------------------------------------------------------- algorithmic work
 
+def tensor_flops_per_subap():
+    """Algorithmic tensor-core flops of one GEMM-DFT pass per lit subap-frame:
+    2 (2c^2)(2p^2) for the cropped DFT plus 2 m^2 c^2 for the convolve+bin map
+    (no padding counted)."""
+    w = WORKLOAD
+    c, p, m = w["N"], w["p"], w["m"]
+    return float(2 * (2 * c * c) * (2 * p * p) + 2 * m * m * c * c)
+
+
 def algorithmic_per_subap():
     """Per lit subap-frame: flops (F_alg) and bytes (B_alg).
 
@@ -321,16 +330,19 @@ def main():
     nlit = info["nlit"]
 
     stream = torch.cuda.Stream()
-    # warm-up
-    with torch.cuda.stream(stream):
-        for k in range(args.warmup):
-            eng.run_batch(batches[k % 2], dc, db, stream=stream)
-    stream.synchronize()
-    barrier(ws)
-    torch.cuda.synchronize()
 
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    with ClockSampler(local) as clk:
+    def time_form(form):
+        """Warm up and time args.steps batched steps of one compute form."""
+        eng.set_form(form)
+        if eng.info()["form_active"] != {"fp32": 0, "bf16": 1, "bf16x3": 2}[form]:
+            return None
+        with torch.cuda.stream(stream):
+            for k in range(args.warmup):
+                eng.run_batch(batches[k % 2], dc, db, stream=stream)
+        stream.synchronize()
+        barrier(ws)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
         t_start = torch.cuda.Event(enable_timing=True)
         t_end = torch.cuda.Event(enable_timing=True)
         with torch.cuda.stream(stream):
@@ -341,15 +353,24 @@ def main():
                 ev[k][1].record(stream)
             t_end.record(stream)
         stream.synchronize()
-    torch.cuda.synchronize()
-    barrier(ws)
-    total_ms = t_start.elapsed_time(t_end)
-    total_ms = reduce_max(total_ms, ws)
-    per_launch_ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
-    ms_per_step = total_ms / args.steps
-    value = ws * nlit * F * args.steps / (total_ms / 1e3)
+        torch.cuda.synchronize()
+        barrier(ws)
+        tot = reduce_max(t_start.elapsed_time(t_end), ws)
+        return {"total_ms": tot, "ms_per_step": tot / args.steps,
+                "per_launch_ms": float(np.mean([a.elapsed_time(b) for a, b in ev])),
+                "value": ws * nlit * F * args.steps / (tot / 1e3)}
 
-    # e2e through the reference-facing call: host phase in, host cents/bimg out
+    with ClockSampler(local) as clk:
+        forms = {f: time_form(f) for f in ("fp32", "bf16x3", "bf16")}
+    head = "bf16x3" if forms.get("bf16x3") else "fp32"
+    eng.set_form(head)
+    total_ms = forms[head]["total_ms"]
+    per_launch_ms = forms[head]["per_launch_ms"]
+    ms_per_step = forms[head]["ms_per_step"]
+    value = forms[head]["value"]
+
+    # e2e through the reference-facing call (headline form): host phase in,
+    # host cents/bimg out
     host_frames = make_frames(screens, 8, 99 + rank)
     lat = []
     for k in range(3):
@@ -368,9 +389,7 @@ def main():
     lat_ms = np.array(lat) * 1e3
 
     F_alg, B_alg = algorithmic_per_subap()
-    bytes_per_launch = B_alg * nlit * F
-    hbm_gbs = bytes_per_launch / (per_launch_ms / 1e3) / 1e9
-    flops_per_launch = F_alg * nlit * F
+    T_alg = tensor_flops_per_subap()
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -379,34 +398,60 @@ def main():
     except Exception:
         peak_src = "fallback"
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    bf16_peak = float(peaks.get("bf16_tflops", 1900.0))
     sm_count = torch.cuda.get_device_properties(0).multi_processor_count
     clocks = clk.summary()
     fp32_peak_tf = sm_count * 128 * 2 * (clocks["sm_max_mhz"] or 2070.0) * 1e6 / 1e12
+    units = nlit * F  # subap-frames per launch
+
+    def rooflines(form, r):
+        t = r["per_launch_ms"] / 1e3
+        out = {"hbm_gbs": B_alg * units / t / 1e9, "hbm_frac": B_alg * units / t / 1e9 / hbm_peak,
+               "fp32_tflops": F_alg * units / t / 1e12, "fp32_frac": F_alg * units / t / 1e12 / fp32_peak_tf}
+        if form != "fp32":
+            tf = T_alg * (3 if form == "bf16x3" else 1) * units / t / 1e12
+            out.update({"tensor_tflops": tf, "tensor_frac": tf / bf16_peak})
+        return out
+
+    form_report = {}
+    for f, r in forms.items():
+        if r:
+            form_report[f] = {"value": r["value"], "ms_per_step": r["ms_per_step"],
+                              "kernel_ms_per_launch": r["per_launch_ms"], **rooflines(f, r)}
     if rank != 0:
         eng.free()
         return
+    rl = rooflines(head, forms[head])
+    if head == "fp32":
+        roof = {"bound": "hbm", "achieved": rl["hbm_gbs"], "peak": hbm_peak, "unit": "GB/s", "frac": rl["hbm_frac"],
+                "traffic": None, "peak_source": peak_src, "algorithmic_bytes_per_subap_frame": B_alg}
+    else:
+        roof = {"bound": "tensor", "achieved": rl["tensor_tflops"], "peak": bf16_peak, "unit": "TFLOP/s",
+                "frac": rl["tensor_frac"], "traffic": None, "peak_source": peak_src + " (bf16 burst)",
+                "algorithmic_flops_per_subap_frame": T_alg * (3 if head == "bf16x3" else 1),
+                "hbm_frac": rl["hbm_frac"]}
+    roof["kernel_ms_per_launch"] = per_launch_ms
+    roof["units_per_launch"] = units
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic: seeded von Karman phase screens (r0 0.157 m @500 nm, L0 25 m, 589 nm)",
+        "dtype": "f32" if head == "fp32" else "bf16x3 (split products, f32 accumulate)",
+        "data": "synthetic: seeded von Karman phase screens (r0 0.157 m @500 nm, L0 25 m, 589 nm)",
         "config": {"workload": w["name"], "nsubx": nsx, "lit_subaps": nlit, "phasesize": w["p"], "fftsize": w["N"],
                    "clipsize": w["C"], "nimg": w["m"], "psf": "2-D Gaussian FWHM 1.5 px (20x20)",
                    "noise": "Poisson + 3 e- read noise, sky 10, floor 6 (counter-based streams)",
-                   "frames_per_step": F, "replicas": ws,
+                   "form": head, "frames_per_step": F, "replicas": ws,
                    "l2": "inputs larger than L2: two rotating %d-frame phase batches of %.0f MB"
-                         % (F, F * W * W * 4 / 1e6),
-                   "tile_subaps": info["tile_subaps"], "smem_bytes": info["smem_bytes"],
-                   "grid_ctas_per_frame": info["grid_ctas"]},
-        "roofline": {"bound": "hbm", "achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": hbm_gbs / hbm_peak, "traffic": None, "peak_source": peak_src,
-                     "algorithmic_bytes_per_subap_frame": B_alg, "kernel_ms_per_launch": per_launch_ms},
-        "fp32_compute": {"achieved_tflops": flops_per_launch / (per_launch_ms / 1e3) / 1e12,
-                         "peak_tflops": fp32_peak_tf, "frac": flops_per_launch / (per_launch_ms / 1e3) / 1e12 / fp32_peak_tf,
-                         "algorithmic_flops_per_subap_frame": F_alg,
-                         "peak_basis": "SMs x 128 FP32 lanes x 2 x max SM clock"},
+                         % (F, F * W * W * 4 / 1e6)},
+        "roofline": roof,
+        "forms": form_report,
+        "fp32_compute": {"achieved_tflops": form_report["fp32"]["fp32_tflops"], "peak_tflops": fp32_peak_tf,
+                         "frac": form_report["fp32"]["fp32_frac"], "algorithmic_flops_per_subap_frame": F_alg,
+                         "peak_basis": "SMs x 128 FP32 lanes x 2 x max SM clock", "form": "fp32"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(W * W * 4),
                 "d2h_bytes_per_step": int(nsub * 2 * 4 + nsub * w["m"] * w["m"] * 4),
-                "path": "centcmod.run -> shwfs_run, host numpy phase/cents/bimg, one synchronous frame per step",
+                "path": "centcmod.run -> shwfs_run (%s form), host numpy phase/cents/bimg, one synchronous frame "
+                        "per step" % head,
                 "frames": args.e2e_frames},
         "latency_ms": {"p50": float(np.percentile(lat_ms, 50)), "p99": float(np.percentile(lat_ms, 99)),
                        "mean": float(lat_ms.mean()), "path": "shwfs_run, host I/O"},
@@ -420,14 +465,18 @@ def main():
         line["cpu_baseline"] = {"value": nl * frames / dt, "unit": UNIT, "cores": 1, "kind": "port",
                                 "sample": "%d noisy frames of the same workload through the numpy/C restatement "
                                           "(%.1f s)" % (frames, dt)}
-        # accuracy of a noiseless frame vs the float64 oracle
+        # accuracy of a noiseless frame of every form vs the float64 oracle
         nph = np.ascontiguousarray(screens[3])
         nc = np.zeros(nsub * 2, np.float32)
         nb = np.zeros((nsx, nsx, w["m"], w["m"]), np.float32)
         e2 = make_engine(pup, nph, nc, nb, noiseless=True)
-        e2.run(0)
-        line["centroid_err_px_vs_fp64"] = accuracy_vs_fp64(nc, nph)
+        errs = {}
+        for f in form_report:
+            e2.set_form(f)
+            e2.run(0)
+            errs[f] = accuracy_vs_fp64(nc, nph)
         e2.free()
+        line["centroid_err_px_vs_fp64"] = errs
     eng.free()
     print(json.dumps(line), flush=True)
 

@@ -37,7 +37,7 @@ namespace shwfs {
 
 namespace {
 
-constexpr int kGemmThreads = 256;
+constexpr int kGemmThreads = 512;
 constexpr int kTileSubaps = 128;
 constexpr uint32_t kTmemCols = 512;
 constexpr int kWaitIter = 1 << 22;
@@ -137,14 +137,28 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   const long long nwork = (long long)a.nlit * a.nframes;
   const long long ntiles = (nwork + kTileSubaps - 1) / kTileSubaps;
 
-  // thread 0: load W2 chunk (oc, kc) into a stage and issue its MMAs
-  auto issue_gemm1 = [&](int oc, uint32_t dcol) {
+  // ---- thread 0: constant streaming and MMA issue ----
+  // The W2 K-chunks of a tile form one sequence j = oc*nkc + kc (global index
+  // gW + j across tiles) through a two-stage ring: chunk j+1 is fetched while
+  // chunk j's MMAs run.  Chunk 0 of the next tile is fetched during the last
+  // chunk of this one (the constants do not depend on the tile).
+  const int nseq = g.noc * g.nkc;
+  auto w2_load = [&](uint32_t gidx, int j) {
+    const uint32_t s = gidx & 1;
+    if (gidx >= 2 && !tc::mbar_wait(&bars.wfree[s], ((gidx >> 1) - 1) & 1, kWaitIter)) ok = false;
+    tc::mbar_expect_tx(&bars.w[s], 2 * wHalf);
+    tc::bulk_g2s(Wst[s], g.w2 + (size_t)j * 2 * wHalf, 2 * wHalf, &bars.w[s]);
+  };
+  auto kc_load = [&](int oc) {
+    tc::mbar_expect_tx(&bars.k, 2 * kHalf);
+    tc::bulk_g2s(KChi, g.kc2 + (size_t)oc * 2 * kHalf, 2 * kHalf, &bars.k);
+  };
+  auto issue_gemm1 = [&](int oc, uint32_t dcol, uint32_t gbase, bool more_tiles) {
     for (int kc = 0; kc < g.nkc; kc++) {
-      const uint32_t s = gW & 1;
-      if (gW >= 2 && !tc::mbar_wait(&bars.wfree[s], ((gW >> 1) - 1) & 1, kWaitIter)) ok = false;
-      tc::mbar_expect_tx(&bars.w[s], 2 * wHalf);
-      tc::bulk_g2s(Wst[s], g.w2 + ((size_t)oc * g.nkc + kc) * 2 * wHalf, 2 * wHalf, &bars.w[s]);
-      if (!tc::mbar_wait(&bars.w[s], (gW >> 1) & 1, kWaitIter)) ok = false;
+      const int j = oc * g.nkc + kc;
+      const uint32_t gidx = gbase + j;
+      const uint32_t s = gidx & 1;
+      if (!tc::mbar_wait(&bars.w[s], (gidx >> 1) & 1, kWaitIter)) ok = false;
       tc::fence_after_sync();
       const int k0 = kc * ksPerChunk;
       const int k1 = min(nks1, k0 + ksPerChunk);
@@ -160,13 +174,21 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         }
       }
       tc::mma_commit(&bars.wfree[s]);
-      gW++;
+      if (j + 1 < nseq)
+        w2_load(gidx + 1, j + 1);
+      else if (more_tiles)
+        w2_load(gidx + 1, 0);
     }
   };
 
+  if (tid == 0 && blockIdx.x < ntiles) {
+    w2_load(0, 0);
+    kc_load(0);
+  }
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const long long w0 = tile * kTileSubaps;
     const int ns = (int)min((long long)kTileSubaps, nwork - w0);
+    const bool more = tile + gridDim.x < ntiles;
     for (int s = tid; s < kTileSubaps; s += blockDim.x) {
       if (s < ns) {
         const long long w = w0 + s;
@@ -176,29 +198,35 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     }
     __syncthreads();
 
-    // ---- E = pup*exp(i(phs - tilt)), split into bf16 hi/lo (row = subap) ----
-    if (tid < kTileSubaps) {
-      const int s = tid;
-      const bool live = s < ns;
-      const int i = live ? s_subap[s] : 0;
-      const int sy = i / a.nsubx, sx = i - sy * a.nsubx;
-      const float* ph = a.phs + (long long)(live ? s_frame[s] : 0) * a.phsFrameStride + (long long)sy * p * a.W + sx * p;
-      const float* pu = a.pup + (long long)i * pp;
-      for (int k = 0; k < g.K1; k++) {
-        float v = 0.f;
-        if (live && k < 2 * pp) {
-          const int pix = k < pp ? k : k - pp;
-          const int r = pix / p, j = pix - r * p;
-          const float t = ph[(long long)r * a.W + j] - s_tilt[pix];
-          float sn, cs;
-          sincosf(t, &sn, &cs);
-          v = pu[pix] * (k < pp ? cs : sn);
-        }
-        const uint16_t hi = bf16_bits(v);
-        const uint32_t off = tc::kmajor_offset(s, k, kLBO, sboE);
-        *reinterpret_cast<uint16_t*>(A1hi + off) = hi;
-        *reinterpret_cast<uint16_t*>(A1lo + off) = bf16_bits(v - bf16_val(hi));
+    // ---- E = pup*exp(i(phs - tilt)), split into bf16 hi/lo (row = subap);
+    // work items (subap, pixel), subap fastest ----
+    for (int w = tid; w < kTileSubaps * pp; w += blockDim.x) {
+      const int s = w & (kTileSubaps - 1), pix = w >> 7;
+      float er = 0.f, ei = 0.f;
+      if (s < ns) {
+        const int i = s_subap[s];
+        const int sy = i / a.nsubx, sx = i - sy * a.nsubx;
+        const int r = pix / p, j = pix - r * p;
+        const float t = a.phs[(long long)s_frame[s] * a.phsFrameStride + (long long)(sy * p + r) * a.W + sx * p + j] -
+                        s_tilt[pix];
+        float sn, cs;
+        sincosf(t, &sn, &cs);
+        const float pu = a.pup[(long long)i * pp + pix];
+        er = pu * cs;
+        ei = pu * sn;
       }
+      const uint16_t hr = bf16_bits(er), hi_ = bf16_bits(ei);
+      const uint32_t offr = tc::kmajor_offset(s, pix, kLBO, sboE), offi = tc::kmajor_offset(s, pp + pix, kLBO, sboE);
+      *reinterpret_cast<uint16_t*>(A1hi + offr) = hr;
+      *reinterpret_cast<uint16_t*>(A1lo + offr) = bf16_bits(er - bf16_val(hr));
+      *reinterpret_cast<uint16_t*>(A1hi + offi) = hi_;
+      *reinterpret_cast<uint16_t*>(A1lo + offi) = bf16_bits(ei - bf16_val(hi_));
+    }
+    for (int w = tid; w < kTileSubaps * (g.K1 - 2 * pp); w += blockDim.x) {
+      const int s = w & (kTileSubaps - 1), k = 2 * pp + (w >> 7);
+      const uint32_t off = tc::kmajor_offset(s, k, kLBO, sboE);
+      *reinterpret_cast<uint16_t*>(A1hi + off) = 0;
+      *reinterpret_cast<uint16_t*>(A1lo + off) = 0;
     }
     tc::fence_async_smem();
     tc::fence_before_sync();
@@ -206,7 +234,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     tc::fence_after_sync();
 
     if (tid == 0) {
-      issue_gemm1(0, tD1[gC & 1]);
+      issue_gemm1(0, tD1[gC & 1], gW, more);
       tc::mma_commit(&bars.d1[gC & 1]);
     }
     for (int oc = 0; oc < g.noc; oc++, gC++) {
@@ -214,46 +242,42 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       // chunk oc+1 runs on the tensor cores while chunk oc is read out; its
       // D1 buffer was last read before the previous iteration's barrier
       if (tid == 0 && oc + 1 < g.noc) {
-        issue_gemm1(oc + 1, tD1[(gC + 1) & 1]);
+        issue_gemm1(oc + 1, tD1[(gC + 1) & 1], gW, more);
         tc::mma_commit(&bars.d1[(gC + 1) & 1]);
       }
       if (!tc::mbar_wait(&bars.d1[buf], (gC >> 1) & 1, kWaitIter)) ok = false;
       // A2 and the Kc stage are free once the previous chunk's GEMM2 completed
-      if (gC > 0 && !tc::mbar_wait(&bars.d2, (gC - 1) & 1, kWaitIter)) ok = false;
+      if (oc > 0) {
+        if (!tc::mbar_wait(&bars.d2, (gC - 1) & 1, kWaitIter)) ok = false;
+        if (tid == 0) kc_load(oc);
+      }
       tc::fence_after_sync();
-      // ---- |F|^2 of 64 outputs; warps w and w+4 split the columns ----
+      // ---- |F|^2 of 64 outputs: warp w reads lanes 32*(w%4), columns
+      // 32*(w/4) .. +31 (16 complex outputs) ----
       {
         const int row = 32 * (warp & 3) + lane;
-        const int half = warp >> 2;  // 0: outputs 0-31, 1: outputs 32-63
-        uint32_t packed_hi[16], packed_lo[16];
+        const int qtr = warp >> 2;
+        uint32_t ph_[8], pl_[8];
 #pragma unroll
-        for (int q = 0; q < 8; q++) {
+        for (int q = 0; q < 4; q++) {
           float v[8];
-          tc::tmem_ld8(tD1[buf] + ((uint32_t)(32 * (warp & 3)) << 16) + half * 64 + q * 8, v);
+          tc::tmem_ld8(tD1[buf] + ((uint32_t)(32 * (warp & 3)) << 16) + qtr * 32 + q * 8, v);
           tc::tmem_ld_wait();
 #pragma unroll
-          for (int e = 0; e < 4; e++) {
-            const float I = v[2 * e] * v[2 * e] + v[2 * e + 1] * v[2 * e + 1];
-            const uint16_t hi = bf16_bits(I);
-            const uint16_t lo = bf16_bits(I - bf16_val(hi));
-            const int o = q * 4 + e;  // 0..31 within this half
-            if (o & 1) {
-              packed_hi[o >> 1] |= (uint32_t)hi << 16;
-              packed_lo[o >> 1] |= (uint32_t)lo << 16;
-            } else {
-              packed_hi[o >> 1] = hi;
-              packed_lo[o >> 1] = lo;
-            }
+          for (int e = 0; e < 4; e += 2) {
+            const float I0 = v[2 * e] * v[2 * e] + v[2 * e + 1] * v[2 * e + 1];
+            const float I1 = v[2 * e + 2] * v[2 * e + 2] + v[2 * e + 3] * v[2 * e + 3];
+            const uint16_t h0 = bf16_bits(I0), h1 = bf16_bits(I1);
+            const uint16_t l0 = bf16_bits(I0 - bf16_val(h0)), l1 = bf16_bits(I1 - bf16_val(h1));
+            ph_[q * 2 + e / 2] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+            pl_[q * 2 + e / 2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
           }
         }
-        // 32 consecutive K values = 4 core-matrix rows of 16 bytes
 #pragma unroll
-        for (int c8 = 0; c8 < 4; c8++) {
-          const uint32_t off = tc::kmajor_offset(row, half * 32 + c8 * 8, kLBO, sbo64);
-          *reinterpret_cast<uint4*>(A2hi + off) =
-              make_uint4(packed_hi[4 * c8], packed_hi[4 * c8 + 1], packed_hi[4 * c8 + 2], packed_hi[4 * c8 + 3]);
-          *reinterpret_cast<uint4*>(A2lo + off) =
-              make_uint4(packed_lo[4 * c8], packed_lo[4 * c8 + 1], packed_lo[4 * c8 + 2], packed_lo[4 * c8 + 3]);
+        for (int c8 = 0; c8 < 2; c8++) {
+          const uint32_t off = tc::kmajor_offset(row, qtr * 16 + c8 * 8, kLBO, sbo64);
+          *reinterpret_cast<uint4*>(A2hi + off) = make_uint4(ph_[4 * c8], ph_[4 * c8 + 1], ph_[4 * c8 + 2], ph_[4 * c8 + 3]);
+          *reinterpret_cast<uint4*>(A2lo + off) = make_uint4(pl_[4 * c8], pl_[4 * c8 + 1], pl_[4 * c8 + 2], pl_[4 * c8 + 3]);
         }
       }
       tc::fence_async_smem();
@@ -261,8 +285,6 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       __syncthreads();
       tc::fence_after_sync();
       if (tid == 0) {
-        tc::mbar_expect_tx(&bars.k, 2 * kHalf);
-        tc::bulk_g2s(KChi, g.kc2 + (size_t)oc * 2 * kHalf, 2 * kHalf, &bars.k);
         if (!tc::mbar_wait(&bars.k, gC & 1, kWaitIter)) ok = false;
         tc::fence_after_sync();
         const uint32_t ahi = tc::smem_addr(A2hi), alo = tc::smem_addr(A2lo);
@@ -279,11 +301,15 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         tc::mma_commit(&bars.d2);
       }
     }
-    // ---- binned image: normalise, sky, noise, threshold -> shared memory ----
+    gW += nseq;
+    // ---- binned image: normalise, sky, noise, threshold -> shared memory;
+    // warp w reads lanes 32*(w%4), pixel columns 32*(w/4) .. +31 ----
     if (!tc::mbar_wait(&bars.d2, (gC - 1) & 1, kWaitIter)) ok = false;
+    if (tid == 0 && more) kc_load(0);  // Kc stage free: prefetch for the next tile
     tc::fence_after_sync();
-    if (tid < kTileSubaps) {
-      const int s = tid;
+    {
+      const int s = 32 * (warp & 3) + lane;
+      const int qtr = warp >> 2;
       const bool live = s < ns;
       const int i = live ? s_subap[s] : 0;
       const float totsig = a.totsig[i];
@@ -294,14 +320,16 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       const bool pois = a.addPoisson == 1 && a.calsource == 0 && pflag;
       const float rn = a.calsource == 0 ? a.readNoise : 0.f;
       const unsigned long long frm = a.frame0 + (live ? s_frame[s] : 0);
-      for (int q0 = 0; q0 < mm; q0 += 8) {
+      const int c1 = min(mm, qtr * 32 + 32);
+      for (int q0 = qtr * 32; q0 < c1; q0 += 8) {
         float v[8];
-        tc::tmem_ld8(tD2 + ((uint32_t)(32 * warp) << 16) + q0, v);
+        tc::tmem_ld8(tD2 + ((uint32_t)(32 * (warp & 3)) << 16) + q0, v);
         tc::tmem_ld_wait();
+        if (!live) continue;
 #pragma unroll
         for (int e = 0; e < 8; e++) {
           const int pix = q0 + e;
-          if (pix >= mm) break;
+          if (pix >= c1) break;
           float x = v[e];
           if (totsig > 0.f) x *= scale;
           if (skyv > 0.f) x += skyv;
@@ -318,8 +346,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     __syncthreads();
     tc::fence_after_sync();
     post_tile(a, ns, s_subap, s_frame, s_cw, [&](int s) { return imgs + s * mm; }, [&](int) { return mm; });
-    tc::fence_async_smem();  // the next tile's E build overwrites the image region
-    __syncthreads();
+    __syncthreads();  // the next tile's E build overwrites the image region
   }
   if (!ok) atomicOr(err, 2);
   tc::fence_before_sync();
