@@ -33,7 +33,8 @@ NOISEMODE = 100
 # every entry point declared in include/shwfs.h
 EXPORTS = ("shwfs_initialise", "shwfs_run", "shwfs_run_slope", "shwfs_update", "shwfs_free",
            "shwfs_last_error", "shwfs_run_async", "shwfs_run_batch", "shwfs_set_io",
-           "shwfs_get_info", "shwfs_version", "shwfs_image_centroids_noalloc")
+           "shwfs_get_info", "shwfs_version", "shwfs_image_centroids_noalloc",
+           "shwfs_batch_create", "shwfs_batch_run", "shwfs_batch_free", "shwfs_autotune")
 
 NOALLOC_MAX_SUBAPS = 65536
 
@@ -115,6 +116,10 @@ def lib() -> ctypes.CDLL:
         L.shwfs_version.restype = ctypes.c_char_p
         L.shwfs_version.argtypes = []
         L.shwfs_image_centroids_noalloc.argtypes = [P(ShwfsImageJob), vp, ctypes.c_char_p, ctypes.c_size_t]
+        L.shwfs_batch_create.argtypes = [P(vp), ctypes.c_int, P(vp)]
+        L.shwfs_batch_run.argtypes = [vp, vp]
+        L.shwfs_batch_free.argtypes = [vp]
+        L.shwfs_autotune.argtypes = [vp, P(ctypes.c_int)]
         for name in EXPORTS:
             if name not in ("shwfs_last_error", "shwfs_version"):
                 getattr(L, name).restype = ctypes.c_int

@@ -306,6 +306,14 @@ class centcmod:
             self.bimg = bimg
         self._keep.extend(keep)
 
+    def autotune(self) -> int:
+        """Time the FP32 kernel over the candidate CTA tile sizes on this
+        handle's own phase input and keep the fastest; returns the tile size
+        (subapertures per CTA).  Results do not depend on the tile size."""
+        best = ctypes.c_int(0)
+        check(_lib.lib().shwfs_autotune(self.centstruct, ctypes.byref(best)), "autotune")
+        return best.value
+
     def info(self) -> dict:
         inf = ShwfsInfo()
         check(_lib.lib().shwfs_get_info(self.centstruct, ctypes.byref(inf)), "get_info")

@@ -152,6 +152,11 @@ struct shwfs_handle {
   DevBuf<uint8_t> d_w2, d_kc2;
   std::vector<float> psfHost, binTHost, binNHost;
   std::vector<int> binIdxHost;
+  // CUDA-graph batches: bumped whenever a launch captured from this handle
+  // could change (update, rebinding, replanning)
+  uint64_t version = 0;
+  const unsigned long long* graphCtr = nullptr;  // set while a batch captures
+  DevBuf<unsigned long long> d_frameCtr;
 
   ~shwfs_handle() {
     for (void* p : registered) cudaHostUnregister(p);
@@ -542,6 +547,7 @@ WfsArgs make_args(shwfs_handle* h, const float* phs, float* cents, float* bimg, 
   a.poisFlag = h->d_poisFlag.p;
   a.seed = h->seed;
   a.frame0 = h->framesRead;
+  a.frameCtr = h->graphCtr;
   a.mode = mode;
   return a;
 }
@@ -593,18 +599,25 @@ shwfs_status build_gemm(shwfs_handle* h) {
 }
 
 // queue one readout over nframes frames (device pointers)
-shwfs_status enqueue_readout(shwfs_handle* h, const float* phs, float* cents, float* bimg, int nframes,
-                             long long phsStride, cudaStream_t st) {
-  const int nlit = (int)h->lit.size();
-  const long long nwork = (long long)nlit * nframes;
-  const long long ntiles = (nwork + h->TS - 1) / h->TS;
-  const int grid = (int)std::max<long long>(1, std::min<long long>(ntiles, (long long)h->numSMs * h->ctasPerSM));
+// device-side state a readout needs that is built lazily (the fit matrix);
+// run before a graph capture so that nothing allocates while capturing
+shwfs_status prepare_readout(shwfs_handle* h) {
   if (h->fitMxParam != h->parabolicFit + h->gaussianFit && (h->parabolicFit || h->gaussianFit > 0)) {
     int fs = h->parabolicFit + h->gaussianFit;
     shwfs_status s = make_fit_mx(h, fs < 0 ? 3 : (fs < 3 ? 3 : fs));
     if (s) return s;
     h->fitMxParam = h->parabolicFit + h->gaussianFit;
   }
+  return SHWFS_OK;
+}
+
+shwfs_status enqueue_readout(shwfs_handle* h, const float* phs, float* cents, float* bimg, int nframes,
+                             long long phsStride, cudaStream_t st) {
+  const int nlit = (int)h->lit.size();
+  const long long nwork = (long long)nlit * nframes;
+  const long long ntiles = (nwork + h->TS - 1) / h->TS;
+  const int grid = (int)std::max<long long>(1, std::min<long long>(ntiles, (long long)h->numSMs * h->ctasPerSM));
+  if (shwfs_status s = prepare_readout(h)) return s;
   if (h->noiseMode == SHWFS_NOISE_REFERENCE) {
     if (nframes != 1) return fail(SHWFS_ERR_UNSUPPORTED, "reference-stream noise runs one frame at a time");
     if (nlit) {
@@ -1027,6 +1040,7 @@ shwfs_status shwfs_run_batch(shwfs_handle* h, int nframes, const float* phs, int
 
 shwfs_status shwfs_set_io(shwfs_handle* h, const shwfs_array* phs, const shwfs_array* cents, const shwfs_array* bimg) {
   if (!h) return fail(SHWFS_ERR_INVALID, "null handle");
+  h->version++;
   shwfs_status s;
   if (phs) {
     if (numel(*phs) != numel(h->phs) || phs->dtype != SHWFS_F32) return fail(SHWFS_ERR_INVALID, "phs shape mismatch");
@@ -1047,6 +1061,7 @@ shwfs_status shwfs_set_io(shwfs_handle* h, const shwfs_array* phs, const shwfs_a
 shwfs_status shwfs_update(shwfs_handle* h, int code, const shwfs_value* v) {
   if (!h || !v) return fail(SHWFS_ERR_INVALID, "null argument");
   g_err.clear();
+  h->version++;
   CK(cudaSetDevice(h->device));
   auto need = [&](int kind, const char* what) -> shwfs_status {
     if (v->kind != kind) return fail(SHWFS_ERR_INVALID, "centmodule: Error extracting %s value", what);
@@ -1254,6 +1269,243 @@ shwfs_status shwfs_get_info(const shwfs_handle* h, shwfs_info* info) {
   info->frames_read = h->framesRead;
   info->form = h->form;
   info->form_active = gemm_active(h) ? h->form : SHWFS_FORM_FP32;
+  return SHWFS_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// batches: one CUDA graph per readout frame of several handles
+// ---------------------------------------------------------------------------
+
+struct shwfs_batch {
+  std::vector<shwfs_handle*> hs;
+  std::vector<uint64_t> versions;   // handle versions the graph was captured at
+  std::vector<uint64_t> ctrFrames;  // frame index each device counter holds
+  int device = 0;
+  cudaStream_t cap = nullptr;  // capture origin and default launch stream
+  std::vector<cudaStream_t> branch;
+  std::vector<cudaEvent_t> ev;  // ev[0] fork, ev[1 + i] join of branch i
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  DevBuf<unsigned long long*> d_ctrs;
+
+  void drop_graph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+  }
+  ~shwfs_batch() {
+    cudaSetDevice(device);
+    if (cap) cudaStreamSynchronize(cap);
+    drop_graph();
+    for (cudaStream_t s : branch) cudaStreamDestroy(s);
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    if (cap) cudaStreamDestroy(cap);
+  }
+};
+
+namespace {
+
+// record every handle's readout on its own branch of one graph, then the
+// counter bump; the handles' launches read their frame index from the
+// device counters, so a replay needs no host-side argument change
+shwfs_status batch_capture(shwfs_batch* b) {
+  b->drop_graph();
+  for (shwfs_handle* h : b->hs)
+    if (shwfs_status s = prepare_readout(h)) return s;
+  CK(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeRelaxed));
+  auto body = [&]() -> shwfs_status {
+    CK(cudaEventRecord(b->ev[0], b->cap));
+    for (size_t i = 0; i < b->hs.size(); i++) {
+      shwfs_handle* h = b->hs[i];
+      CK(cudaStreamWaitEvent(b->branch[i], b->ev[0], 0));
+      h->graphCtr = h->d_frameCtr.p;
+      shwfs_status s = enqueue_readout(h, (const float*)h->phs.data, (float*)h->cents.data, (float*)h->bimg.data, 1,
+                                       0, b->branch[i]);
+      h->graphCtr = nullptr;
+      if (s) return s;
+      CK(cudaEventRecord(b->ev[1 + i], b->branch[i]));
+      CK(cudaStreamWaitEvent(b->cap, b->ev[1 + i], 0));
+    }
+    CK(launch_bump_counters(b->d_ctrs.p, (int)b->hs.size(), b->cap));
+    return SHWFS_OK;
+  };
+  const shwfs_status s = body();
+  const std::string err = g_err;
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(b->cap, &g);
+  if (s) {
+    if (g) cudaGraphDestroy(g);
+    g_err = err;
+    return s;
+  }
+  if (e != cudaSuccess) return fail(SHWFS_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+  b->graph = g;
+  CK(cudaGraphInstantiate(&b->exec, b->graph, 0));
+  for (size_t i = 0; i < b->hs.size(); i++) b->versions[i] = b->hs[i]->version;
+  return SHWFS_OK;
+}
+
+shwfs_status batch_check(const shwfs_handle* h) {
+  if (!h) return fail(SHWFS_ERR_INVALID, "null handle in batch");
+  if (h->noiseMode == SHWFS_NOISE_REFERENCE)
+    return fail(SHWFS_ERR_UNSUPPORTED, "batches need the counter-based noise streams");
+  if (is_none(h->phs) || !h->phs.on_device || !h->cents.on_device || !h->bimg.on_device)
+    return fail(SHWFS_ERR_INVALID, "batched handles need device-resident phs, cents and bimg");
+  return SHWFS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+shwfs_status shwfs_batch_create(shwfs_handle* const* handles, int n, shwfs_batch** out) {
+  if (!handles || !out || n < 1) return fail(SHWFS_ERR_INVALID, "bad batch arguments");
+  *out = nullptr;
+  g_err.clear();
+  for (int i = 0; i < n; i++) {
+    if (shwfs_status s = batch_check(handles[i])) return s;
+    if (handles[i]->device != handles[0]->device) return fail(SHWFS_ERR_INVALID, "batched handles share one device");
+    for (int j = 0; j < i; j++)
+      if (handles[j] == handles[i]) return fail(SHWFS_ERR_INVALID, "handle %d appears twice in the batch", i);
+  }
+  shwfs_batch* b = new shwfs_batch;
+  b->device = handles[0]->device;
+  auto init = [&]() -> shwfs_status {
+    CK(cudaSetDevice(b->device));
+    CK(cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking));
+    std::vector<unsigned long long*> ptrs;
+    for (int i = 0; i < n; i++) {
+      shwfs_handle* h = handles[i];
+      b->hs.push_back(h);
+      if (!h->d_frameCtr.p) CK(h->d_frameCtr.alloc(1));
+      const unsigned long long f0 = h->framesRead;
+      CK(cudaMemcpy(h->d_frameCtr.p, &f0, sizeof(f0), cudaMemcpyHostToDevice));
+      b->ctrFrames.push_back(h->framesRead);
+      b->versions.push_back(h->version);
+      ptrs.push_back(h->d_frameCtr.p);
+      cudaStream_t s = nullptr;
+      CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+      b->branch.push_back(s);
+    }
+    for (int i = 0; i <= n; i++) {
+      cudaEvent_t e = nullptr;
+      CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      b->ev.push_back(e);
+    }
+    CK(b->d_ctrs.upload(ptrs.data(), ptrs.size()));
+    return batch_capture(b);
+  };
+  if (shwfs_status s = init()) {
+    const std::string err = g_err;
+    delete b;
+    g_err = err;
+    return s;
+  }
+  *out = b;
+  return SHWFS_OK;
+}
+
+shwfs_status shwfs_batch_run(shwfs_batch* b, void* stream) {
+  if (!b) return fail(SHWFS_ERR_INVALID, "null batch");
+  CK(cudaSetDevice(b->device));
+  cudaStream_t st = stream ? (cudaStream_t)stream : b->cap;
+  bool stale = false;
+  for (size_t i = 0; i < b->hs.size(); i++) {
+    if (shwfs_status s = batch_check(b->hs[i])) return s;
+    stale |= b->versions[i] != b->hs[i]->version;
+  }
+  if (stale)
+    if (shwfs_status s = batch_capture(b)) return s;
+  // a handle run on its own since the last replay advanced its host frame
+  // index: bring the device counter to it, in stream order
+  for (size_t i = 0; i < b->hs.size(); i++) {
+    shwfs_handle* h = b->hs[i];
+    if (b->ctrFrames[i] != h->framesRead) CK(launch_set_counter(h->d_frameCtr.p, h->framesRead, st));
+  }
+  CK(cudaGraphLaunch(b->exec, st));
+  for (size_t i = 0; i < b->hs.size(); i++) {
+    b->hs[i]->framesRead++;
+    b->ctrFrames[i] = b->hs[i]->framesRead;
+  }
+  if (!stream) {
+    CK(cudaStreamSynchronize(st));
+    for (shwfs_handle* h : b->hs) {
+      if (!gemm_active(h)) continue;
+      int status = 0;
+      CK(cudaMemcpy(&status, h->d_status.p, sizeof(int), cudaMemcpyDeviceToHost));
+      if (status & 2) return fail(SHWFS_ERR_STATE, "tensor-core pipeline wait timed out (results invalid)");
+    }
+  }
+  return SHWFS_OK;
+}
+
+shwfs_status shwfs_batch_free(shwfs_batch* b) {
+  delete b;
+  return SHWFS_OK;
+}
+
+shwfs_status shwfs_autotune(shwfs_handle* h, int* best_tile) {
+  if (!h) return fail(SHWFS_ERR_INVALID, "null handle");
+  g_err.clear();
+  CK(cudaSetDevice(h->device));
+  if (h->lit.empty() || is_none(h->phs) || h->noiseMode == SHWFS_NOISE_REFERENCE || gemm_active(h)) {
+    // nothing to choose: no FP32 phase-input launches on this handle
+    if (best_tile) *best_tile = h->TS;
+    return SHWFS_OK;
+  }
+  if (shwfs_status s = prepare_readout(h)) return s;
+  const int nlit = (int)h->lit.size();
+  const size_t mm = (size_t)h->nimg * h->nimg;
+  // enough frames that every candidate fills the GPU several times over
+  const int nf = (int)std::max<long long>(1, std::min<long long>(64, (16LL * 64 * h->numSMs + nlit - 1) / nlit));
+  DevBuf<float> ph, ce, bi;
+  const float* phs = (const float*)h->phs.data;
+  if (!h->phs.on_device) {
+    CK(ph.upload(phs, (size_t)numel(h->phs)));
+    phs = ph.p;
+  }
+  CK(ce.alloc((size_t)nf * h->nsubaps * 2));
+  CK(bi.alloc((size_t)nf * h->nsubaps * mm));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  const int saved = h->tileOverride;
+  const int cands[] = {0, 4, 6, 8, 10, 12, 14, 16, 20, 24, 32};
+  float bestMs = 1e30f;
+  int bestOverride = saved;
+  shwfs_status s = SHWFS_OK;
+  for (int c : cands) {
+    h->tileOverride = c;
+    if (plan(h) != SHWFS_OK) continue;
+    float ms = 0.f;
+    for (int rep = 0; rep < 2 && !s; rep++) {  // rep 0 warms up
+      if (cudaEventRecord(e0, h->stream) != cudaSuccess) s = fail(SHWFS_ERR_CUDA, "event record failed");
+      for (int k = 0; k < 3 && !s; k++) s = enqueue_readout(h, phs, ce.p, bi.p, nf, 0, h->stream);
+      if (!s && cudaEventRecord(e1, h->stream) != cudaSuccess) s = fail(SHWFS_ERR_CUDA, "event record failed");
+      if (!s && cudaEventSynchronize(e1) != cudaSuccess) s = fail(SHWFS_ERR_CUDA, "autotune launch failed");
+      if (!s) cudaEventElapsedTime(&ms, e0, e1);
+    }
+    if (s) break;
+    if (ms < bestMs) {
+      bestMs = ms;
+      bestOverride = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  h->tileOverride = s ? saved : bestOverride;
+  h->version++;
+  const std::string err = g_err;
+  const shwfs_status sp = plan(h);
+  if (s) {
+    g_err = err;
+    return s;
+  }
+  if (sp) return sp;
+  if (best_tile) *best_tile = h->TS;
   return SHWFS_OK;
 }
 

@@ -68,8 +68,15 @@ struct WfsArgs {
   unsigned char* poisFlag;  // per subap: Poisson applies (reference-stream mode)
   unsigned long long seed;
   unsigned long long frame0;
+  // when set (CUDA-graph replays), the noise frame index is read from this
+  // device counter instead of frame0
+  const unsigned long long* frameCtr;
   int mode;
 };
+
+__device__ __forceinline__ unsigned long long frame_base(const WfsArgs& a) {
+  return a.frameCtr ? *a.frameCtr : a.frame0;
+}
 
 // ---------------------------------------------------------------------------
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as

@@ -303,7 +303,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     }
     gW += nseq;
     // ---- binned image: normalise, sky, noise, threshold -> shared memory;
-    // warp w reads lanes 32*(w%4), pixel columns 32*(w/4) .. +31 ----
+    // warp w reads lanes 32*(w%4), pixel columns 32*(w/4) + 128*j .. +31 ----
     if (!tc::mbar_wait(&bars.d2, (gC - 1) & 1, kWaitIter)) ok = false;
     if (tid == 0 && more) kc_load(0);  // Kc stage free: prefetch for the next tile
     tc::fence_after_sync();
@@ -319,9 +319,10 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       const bool pflag = totsig > 0.f || skyv > 0.f || a.skyArr;
       const bool pois = a.addPoisson == 1 && a.calsource == 0 && pflag;
       const float rn = a.calsource == 0 ? a.readNoise : 0.f;
-      const unsigned long long frm = a.frame0 + (live ? s_frame[s] : 0);
-      const int c1 = min(mm, qtr * 32 + 32);
-      for (int q0 = qtr * 32; q0 < c1; q0 += 8) {
+      const unsigned long long frm = frame_base(a) + (live ? s_frame[s] : 0);
+      for (int cb = qtr * 32; cb < mm; cb += 128) {
+      const int c1 = min(mm, cb + 32);
+      for (int q0 = cb; q0 < c1; q0 += 8) {
         float v[8];
         tc::tmem_ld8(tD2 + ((uint32_t)(32 * (warp & 3)) << 16) + q0, v);
         tc::tmem_ld_wait();
@@ -340,6 +341,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
           x += rn != 0.f ? rn * gnoise + a.readBg : a.readBg;
           imgs[s * mm + pix] = threshold_px(x, a.floorv, a.threshType);
         }
+      }
       }
     }
     tc::fence_before_sync();

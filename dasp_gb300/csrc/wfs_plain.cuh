@@ -707,7 +707,7 @@ __global__ void __launch_bounds__(kThreads) wfs_plain_kernel(const WfsArgs a) {
         const int s = w / mm, pix = w - (w / mm) * mm;
         if (pix >= nexp) continue;
         const int i = s_subap[s];
-        const unsigned long long fr = a.frame0 + s_frame[s];
+        const unsigned long long fr = frame_base(a) + s_frame[s];
         float v = IMG(s)[pix];
         // one stream per pixel: the read-noise normal takes the first two
         // uniforms, the Poisson sampler continues from the third
@@ -737,6 +737,10 @@ __global__ void __launch_bounds__(kThreads) wfs_plain_kernel(const WfsArgs a) {
 
 // launcher of the unlit-subaperture kernel (wfs_unlit.cu)
 cudaError_t launch_unlit(const WfsArgs& a, const int* unlit, int nunlit, cudaStream_t stream);
+// increment n device counters (graph replays of a batch)
+cudaError_t launch_bump_counters(unsigned long long* const* ctrs, int n, cudaStream_t stream);
+// store v in one device counter, in stream order
+cudaError_t launch_set_counter(unsigned long long* ctr, unsigned long long v, cudaStream_t stream);
 // image-input (runSlope) kernel over the lit subapertures (wfs_image.cu)
 cudaError_t launch_image(const WfsArgs& a, const float* img, int dims, int npxlx, const int* loc, int numSMs,
                          cudaStream_t stream);

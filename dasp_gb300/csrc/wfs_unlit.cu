@@ -22,7 +22,7 @@ __global__ void wfs_unlit_kernel(const WfsArgs a, const int* unlit, int nunlit) 
       float v = a.readBg;
       const float rn = a.calsource == 0 ? a.readNoise : 0.f;
       if (rn != 0.f) {
-        CounterStream st(a.seed, a.frame0 + f, i, pix, 1);
+        CounterStream st(a.seed, frame_base(a) + f, i, pix, 1);
         v = rn * normal_counter(st) + a.readBg;
       }
       a.bimg[(long long)f * a.bimgFrameStride + (long long)i * mm + pix] = threshold_px(v, a.floorv, a.threshType);
@@ -48,6 +48,24 @@ cudaError_t launch_publish(const float* src, float* dst, const int* list, int n,
   if (total == 0) return cudaSuccess;
   const int blocks = (int)((total + 255) / 256 < 2048 ? (total + 255) / 256 : 2048);
   publish_subaps_kernel<<<blocks, 256, 0, stream>>>(src, dst, list, n, mm);
+  return cudaGetLastError();
+}
+
+// advance the device frame counters of a graph's handles (one per handle)
+__global__ void bump_counters_kernel(unsigned long long* const* ctrs, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) ctrs[i][0] += 1ull;
+}
+
+cudaError_t launch_bump_counters(unsigned long long* const* ctrs, int n, cudaStream_t stream) {
+  bump_counters_kernel<<<(n + 127) / 128, 128, 0, stream>>>(ctrs, n);
+  return cudaGetLastError();
+}
+
+__global__ void set_counter_kernel(unsigned long long* ctr, unsigned long long v) { *ctr = v; }
+
+cudaError_t launch_set_counter(unsigned long long* ctr, unsigned long long v, cudaStream_t stream) {
+  set_counter_kernel<<<1, 1, 0, stream>>>(ctr, v);
   return cudaGetLastError();
 }
 

@@ -229,6 +229,25 @@ shwfs_status shwfs_get_info(const shwfs_handle* h, shwfs_info* info);
 /* Library version string. */
 const char* shwfs_version(void);
 
+/* ---- many wavefront sensors per launch (no reference counterpart; the
+ * reference serves several WFSs by resource sharing through one module
+ * object, science/wfscent.py:41-52,585-598) ----
+ * A batch captures one readout frame of every handle into a CUDA graph: each
+ * handle's persistent kernel(s) on its own graph branch, branches running
+ * concurrently, so WFSs of different subaperture counts, FFT sizes and spot
+ * PSFs go to the GPU with one graph launch.  Every handle must have
+ * device-resident phs/cents/bimg.  The graph is re-captured when a handle is
+ * updated; noise frame counters advance on the device between replays. */
+typedef struct shwfs_batch shwfs_batch;
+shwfs_status shwfs_batch_create(shwfs_handle* const* handles, int n, shwfs_batch** out);
+shwfs_status shwfs_batch_run(shwfs_batch* b, void* stream);
+shwfs_status shwfs_batch_free(shwfs_batch* b);
+
+/* Time the fused FP32 kernel over the candidate tile sizes on scratch
+ * buffers and keep the fastest for this handle (results are unchanged: the
+ * tile size only changes how subapertures are grouped per CTA). */
+shwfs_status shwfs_autotune(shwfs_handle* h, int* best_tile);
+
 /* ---- allocation-free image centroiding (no counterpart in the reference) ----
  *
  * For callers that cannot allocate GPU memory: a real-time control thread

@@ -1,0 +1,141 @@
+"""Many WFSs per launch (CUDA-graph batches) and the tile autotuner.
+
+A batched readout frame must give bit-identical images and centroids to the
+same handle configuration run on its own (``run_batch`` with one frame): the
+graph replays the same kernels, and each handle's noise frame index advances
+on the device exactly as its host counter does."""
+import numpy as np
+import pytest
+
+from tests.wfs_cases import Case
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+NOISY = dict(sig=2e3, skybrightness=5.0, readnoise=2.0, addPoisson=1, noiseFloor=1.0)
+GEOMS = [dict(nsubx=8, p=8, N=16, C=16, m=8), dict(nsubx=12, p=10, N=20, C=20, m=10, psf="gauss"),
+         dict(nsubx=6, p=8, N=24, C=24, m=12)]
+
+
+class DevEngine:
+    """An engine whose phase and outputs live in CUDA tensors."""
+
+    def __init__(self, case, form="fp32"):
+        self.c = case
+        self.eng = case.engine()
+        self.phs = torch.from_numpy(case.phs.copy()).cuda()
+        self.cents = torch.zeros(case.nsubaps * 2, device="cuda")
+        self.bimg = torch.zeros(case.nsubaps, case.m, case.m, device="cuda")
+        self.eng.set_io(self.phs, self.cents, self.bimg)
+        if form != "fp32":
+            self.eng.set_form(form)
+        torch.cuda.synchronize()  # the engine's streams do not wait on torch's
+
+    def run_alone(self):
+        self.eng.run_batch(self.phs[None], self.cents[None], self.bimg[None])
+
+    def outputs(self):
+        torch.cuda.synchronize()
+        return self.cents.cpu().numpy().copy(), self.bimg.cpu().numpy().copy()
+
+
+def _pairs(forms=None):
+    forms = forms or ["fp32"] * len(GEOMS)
+    a = [DevEngine(Case(**g, **NOISY), f) for g, f in zip(GEOMS, forms)]
+    b = [DevEngine(Case(**g, **NOISY), f) for g, f in zip(GEOMS, forms)]
+    return a, b
+
+
+def _same(x, y):
+    for (c0, b0), (c1, b1) in zip(x, y):
+        np.testing.assert_array_equal(c0, c1)
+        np.testing.assert_array_equal(b0, b1)
+
+
+def _new_phase(pairs, seed):
+    for k, (x, y) in enumerate(pairs):
+        ph = torch.from_numpy(np.ascontiguousarray(x.c.new_phase(seed + k), np.float32)).cuda()
+        x.phs.copy_(ph)
+        y.phs.copy_(ph)
+    torch.cuda.synchronize()
+
+
+def test_batch_equals_individual_runs():
+    from dasp_gb300.batch import WfsBatch
+    a, b = _pairs()
+    batch = WfsBatch([x.eng for x in a])
+    for f in range(3):
+        _new_phase(list(zip(a, b)), 50 + 10 * f)
+        batch.run()
+        for y in b:
+            y.run_alone()
+        _same([x.outputs() for x in a], [y.outputs() for y in b])
+        assert all(x.eng.info()["frames_read"] == f + 1 for x in a)
+    # noise really changes between frames
+    c0, _ = a[0].outputs()
+    batch.run()
+    c1, _ = a[0].outputs()
+    assert not np.array_equal(c0, c1)
+    batch.free()
+
+
+def test_batch_recaptures_after_update_and_solo_runs():
+    from dasp_gb300.batch import WfsBatch
+    from dasp_gb300.centcmod import SIG
+    a, b = _pairs()
+    batch = WfsBatch([x.eng for x in a])
+    batch.run()
+    for y in b:
+        y.run_alone()
+    # an update changes a captured argument: the batch re-captures
+    a[1].eng.update(SIG, 3.5e3)
+    b[1].eng.update(SIG, 3.5e3)
+    # a handle run on its own advances its frame index outside the graph
+    a[2].run_alone()
+    b[2].run_alone()
+    torch.cuda.synchronize()
+    for _ in range(2):
+        batch.run(torch.cuda.current_stream())
+        for y in b:
+            y.run_alone()
+    _same([x.outputs() for x in a], [y.outputs() for y in b])
+    batch.free()
+
+
+def test_batch_with_tensor_core_form():
+    from dasp_gb300.batch import WfsBatch
+    a, b = _pairs(["bf16x3", "fp32", "bf16x3"])
+    assert a[0].eng.info()["form_active"] == 2
+    batch = WfsBatch([x.eng for x in a])
+    for f in range(2):
+        _new_phase(list(zip(a, b)), 80 + 10 * f)
+        batch.run()
+        for y in b:
+            y.run_alone()
+    _same([x.outputs() for x in a], [y.outputs() for y in b])
+    batch.free()
+
+
+def test_batch_rejects_host_io_and_duplicates():
+    from dasp_gb300.batch import WfsBatch
+    c = Case(nsubx=8, **NOISY)
+    host = c.engine()
+    with pytest.raises(ValueError):
+        WfsBatch([host])
+    d = DevEngine(Case(nsubx=8, **NOISY))
+    with pytest.raises(ValueError):
+        WfsBatch([d.eng, d.eng])
+    host.free()
+
+
+def test_autotune_keeps_results():
+    base = DevEngine(Case(nsubx=16, p=10, N=20, C=20, m=10, psf="gauss", **NOISY))
+    tuned = DevEngine(Case(nsubx=16, p=10, N=20, C=20, m=10, psf="gauss", **NOISY))
+    ts = tuned.eng.autotune()
+    assert ts == tuned.eng.info()["tile_subaps"] and 1 <= ts <= 64
+    assert tuned.eng.info()["frames_read"] == 0
+    for _ in range(2):
+        base.run_alone()
+        tuned.run_alone()
+    _same([base.outputs()], [tuned.outputs()])
