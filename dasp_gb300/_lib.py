@@ -34,7 +34,8 @@ NOISEMODE = 100
 EXPORTS = ("shwfs_initialise", "shwfs_run", "shwfs_run_slope", "shwfs_update", "shwfs_free",
            "shwfs_last_error", "shwfs_run_async", "shwfs_run_batch", "shwfs_set_io",
            "shwfs_get_info", "shwfs_version", "shwfs_image_centroids_noalloc",
-           "shwfs_batch_create", "shwfs_batch_run", "shwfs_batch_free", "shwfs_autotune")
+           "shwfs_batch_create", "shwfs_batch_run", "shwfs_batch_free", "shwfs_autotune",
+           "shwfs_sample_noise", "shwfs_set_split_event")
 
 NOALLOC_MAX_SUBAPS = 65536
 
@@ -120,6 +121,8 @@ def lib() -> ctypes.CDLL:
         L.shwfs_batch_run.argtypes = [vp, vp]
         L.shwfs_batch_free.argtypes = [vp]
         L.shwfs_autotune.argtypes = [vp, P(ctypes.c_int)]
+        L.shwfs_set_split_event.argtypes = [vp, vp]
+        L.shwfs_sample_noise.argtypes = [ctypes.c_int, vp, ctypes.c_int64, ctypes.c_uint64, ctypes.c_uint64, vp, vp]
         for name in EXPORTS:
             if name not in ("shwfs_last_error", "shwfs_version"):
                 getattr(L, name).restype = ctypes.c_int

@@ -48,7 +48,7 @@ OUTPUTPHASEARR = 22
 
 TILESUBAPS = 101  # extension: subapertures per CTA tile (0 = default)
 FORM = 102  # extension: compute form (FORMS below)
-FORMS = {"fp32": 0, "bf16": 1, "bf16x3": 2}
+FORMS = {"fp32": 0, "bf16": 1, "bf16x3": 2, "fp16": 3, "tf32": 4}
 
 _INT_CODES = {CALSOURCE, ADDPOISSON, NCEN, NTHREADS, OPTICALBINNING, CORRELATIONCENTROIDING, INTEGSTEPS,
               NOISEMODE, TILESUBAPS, FORM}
@@ -259,10 +259,12 @@ class centcmod:
         self.update(NOISEMODE, code)
 
     def set_form(self, form):
-        """Compute form: ``"fp32"`` (fused FP32 kernel, default), ``"bf16"`` or
-        ``"bf16x3"`` (GEMM-DFT on the tensor cores, one pass or split
-        products).  Configurations the GEMM kernel does not cover keep running
-        the FP32 form; ``info()["form_active"]`` tells which one runs."""
+        """Compute form: ``"fp32"`` (fused FP32 kernel, default), or GEMM-DFT
+        on the tensor cores: ``"bf16"`` (one pass), ``"bf16x3"`` (split
+        products), ``"fp16"`` (one pass, |F|^2 scaled per subaperture) or
+        ``"tf32"`` (one pass).  Configurations the GEMM kernel does not cover
+        keep running the FP32 form; ``info()["form_active"]`` tells which one
+        runs."""
         self.update(FORM, FORMS[form])
 
     def run_batch(self, phs_frames, cents_frames, bimg_frames, stream=None):
@@ -305,6 +307,13 @@ class centcmod:
         if bimg is not None:
             self.bimg = bimg
         self._keep.extend(keep)
+
+    def set_split_event(self, event):
+        """Timing aid: the engine records ``event`` (a created torch.cuda.Event
+        or raw cudaEvent_t handle; None switches it off) between the
+        tensor-core image-formation kernel and the noise/centroid kernel."""
+        ev = None if event is None else getattr(event, "cuda_event", event)
+        check(_lib.lib().shwfs_set_split_event(self.centstruct, ev), "set_split_event")
 
     def autotune(self) -> int:
         """Time the FP32 kernel over the candidate CTA tile sizes on this

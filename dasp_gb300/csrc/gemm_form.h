@@ -9,6 +9,11 @@
 
 namespace shwfs {
 
+// operand formats of the tensor-core passes
+enum : int { kFmtBF16 = 0, kFmtFP16 = 1, kFmtTF32 = 2 };
+constexpr int kGemmMaxNW = 8;  // W2 ring stages
+constexpr int kGemmMaxNK = 2;  // Kc ring stages
+
 // geometry of one handle, as the GEMM form needs it
 struct GemmSpec {
   int p, N, c, ro, rs, padded, P, C, m, preBin, psfDim;
@@ -19,22 +24,54 @@ struct GemmSpec {
 
 // launch geometry and device constants
 struct GemmGeom {
-  int K1;    // 2 p^2 rounded up to 16 (GEMM1 K)
-  int KC;    // GEMM1 K columns per streamed chunk (multiple of 16)
-  int nkc;   // GEMM1 K chunks
-  int noc;   // output chunks of 64 complex outputs (GEMM1 N = 128 columns each)
-  int N2;    // GEMM2 N: nimg^2 rounded up to 16
-  const uint8_t* w2;   // [noc][nkc] x {hi, lo} x [128 x KC] bf16, tensor-core smem order
-  const uint8_t* kc2;  // [noc] x {hi, lo} x [N2 x 64] bf16, tensor-core smem order
+  int fmt;     // kFmt*
+  int passes;  // 1, or 3 split-product passes (bf16 only)
+  int K1;      // GEMM1 K in elements: [Re E | Im E], each p^2 rounded up to 8, total rounded up to 16
+  int KCB;     // GEMM1 K bytes per row of one streamed W2 chunk (multiple of 32)
+  int nkc;     // W2 chunks per output chunk
+  int noc;     // output chunks of 64 complex outputs (GEMM1 N = 128 columns each)
+  int N2;      // GEMM2 N: nimg^2 rounded up to 16
+  int NW, NK;  // ring stages for W2 and Kc chunks
+  const uint8_t* w2;   // [noc][nkc] x {hi[, lo]} x [128 x KCB bytes], tensor-core smem order
+  const uint8_t* kc2;  // [noc] x {hi[, lo]} x [N2 x 64 elements], tensor-core smem order
 };
 
-// fills K1/KC/nkc/noc/N2; false if the geometry does not fit the kernel
-bool gemm_geometry(const GemmSpec& sp, GemmGeom* g);
-int gemm_smem_bytes(const GemmGeom& g, int m);
+// dynamic shared-memory layout (byte offsets)
+struct GemmSmem {
+  uint32_t a1, a2, w, k, total;
+  uint32_t a1Half, a2Half, wHalf, wStage, kHalf, kStage;
+};
+
+__host__ __device__ inline GemmSmem gemm_smem_layout(const GemmGeom& g) {
+  GemmSmem L;
+  const uint32_t esz = g.fmt == kFmtTF32 ? 4u : 2u, hl = g.passes == 3 ? 2u : 1u;
+  L.a1Half = 128u * (uint32_t)g.K1 * esz;
+  L.a2Half = 128u * 64u * esz;
+  L.wHalf = 128u * (uint32_t)g.KCB;
+  L.wStage = L.wHalf * hl;
+  L.kHalf = (uint32_t)g.N2 * 64u * esz;
+  L.kStage = L.kHalf * hl;
+  L.a1 = 0;
+  L.a2 = (L.a1 + L.a1Half * hl + 1023u) & ~1023u;
+  L.w = (L.a2 + L.a2Half * hl + 1023u) & ~1023u;
+  L.k = (L.w + (uint32_t)g.NW * L.wStage + 1023u) & ~1023u;
+  L.total = L.k + (uint32_t)g.NK * L.kStage;
+  return L;
+}
+
+// fills the geometry for one operand format; false if it does not fit the kernel
+bool gemm_geometry(const GemmSpec& sp, int fmt, int passes, GemmGeom* g);
+int gemm_smem_bytes(const GemmGeom& g);
 void gemm_build_w2(const GemmSpec& sp, const GemmGeom& g, std::vector<uint8_t>& out);
 // dense [m^2][c^2] map from the cropped power spectrum to the binned image
 void gemm_kc_matrix(const GemmSpec& sp, std::vector<double>& kc);
 void gemm_build_kc(const GemmSpec& sp, const GemmGeom& g, const std::vector<double>& kc, std::vector<uint8_t>& out);
-cudaError_t launch_gemm(const WfsArgs& a, const GemmGeom& g, int passes, int numSMs, int* err, cudaStream_t stream);
+// image formation of the lit subaperture-frames into bimg (pre-noise);
+// iscale: per-subaperture |F|^2 scale of the fp16 format (else null)
+cudaError_t launch_gemm(const WfsArgs& a, const GemmGeom& g, const float* iscale, int numSMs, int* err,
+                        cudaStream_t stream);
+// noise, threshold and the post stages on the pre-noise images in bimg
+// (wfs_post.cu)
+cudaError_t launch_post(const WfsArgs& a, int numSMs, cudaStream_t stream);
 
 }  // namespace shwfs

@@ -150,6 +150,8 @@ struct shwfs_handle {
   bool gemmBuilt = false;
   GemmGeom gemm{};
   DevBuf<uint8_t> d_w2, d_kc2;
+  DevBuf<float> d_iscale;  // fp16 form: 1 / (sum of the subaperture's pupil)^2
+  cudaEvent_t splitEvent = nullptr;  // recorded between image formation and post stages
   std::vector<float> psfHost, binTHost, binNHost;
   std::vector<int> binIdxHost;
   // CUDA-graph batches: bumped whenever a launch captured from this handle
@@ -572,7 +574,8 @@ bool gemm_static_ok(const shwfs_handle* h, GemmGeom* g, GemmSpec* sp) {
   sp->binT = h->binTHost;
   sp->binN = h->binNHost;
   sp->binIdx = h->binIdxHost;
-  return gemm_geometry(*sp, g);
+  const int fmt = h->form == SHWFS_FORM_FP16 ? kFmtFP16 : (h->form == SHWFS_FORM_TF32 ? kFmtTF32 : kFmtBF16);
+  return gemm_geometry(*sp, fmt, h->form == SHWFS_FORM_BF16X3 ? 3 : 1, g);
 }
 
 bool gemm_active(const shwfs_handle* h) {
@@ -593,6 +596,16 @@ shwfs_status build_gemm(shwfs_handle* h) {
   gemm_build_kc(sp, g, kc, kc2);
   CK(h->d_w2.upload(w2.data(), w2.size()));
   CK(h->d_kc2.upload(kc2.data(), kc2.size()));
+  if (g.fmt == kFmtFP16) {
+    const int pp = h->phasesize * h->phasesize;
+    std::vector<float> isc((size_t)h->nsubaps, 1.f);
+    for (int i = 0; i < h->nsubaps; i++) {
+      double s = 0;
+      for (int k = 0; k < pp; k++) s += h->pup[(size_t)i * pp + k];
+      if (s > 0) isc[i] = (float)(1.0 / (s * s));
+    }
+    CK(h->d_iscale.upload(isc.data(), isc.size()));
+  }
   h->gemm = g;
   h->gemmBuilt = true;
   return SHWFS_OK;
@@ -650,11 +663,15 @@ shwfs_status enqueue_readout(shwfs_handle* h, const float* phs, float* cents, fl
     }
   } else {
     if (nlit && gemm_active(h)) {
-      WfsArgs a = make_args(h, phs, cents, bimg, nframes, phsStride, kForm | kNoiseCounter | kPost);
+      // tensor-core image formation into bimg, then noise + post stages
+      WfsArgs a = make_args(h, phs, cents, bimg, nframes, phsStride, kForm);
       GemmGeom g = h->gemm;
       g.w2 = h->d_w2.p;
       g.kc2 = h->d_kc2.p;
-      CK(launch_gemm(a, g, h->form == SHWFS_FORM_BF16X3 ? 3 : 1, h->numSMs, h->d_status.p, st));
+      CK(launch_gemm(a, g, g.fmt == kFmtFP16 ? h->d_iscale.p : nullptr, h->numSMs, h->d_status.p, st));
+      if (h->splitEvent) CK(cudaEventRecord(h->splitEvent, st));
+      a.mode = kNoiseCounter | kPost;
+      CK(launch_post(a, h->numSMs, st));
     } else if (nlit) {
       WfsArgs a = make_args(h, phs, cents, bimg, nframes, phsStride, kForm | kNoiseCounter | kPost);
       CK(h->entry->launch(a, grid, h->smem, st));
@@ -1221,7 +1238,7 @@ shwfs_status shwfs_update(shwfs_handle* h, int code, const shwfs_value* v) {
       break;
     case SHWFS_FORM:
       if ((s = need(SHWFS_VAL_INT, "int"))) return s;
-      if (v->ival != SHWFS_FORM_FP32 && v->ival != SHWFS_FORM_BF16 && v->ival != SHWFS_FORM_BF16X3)
+      if (v->ival < SHWFS_FORM_FP32 || v->ival > SHWFS_FORM_TF32)
         return fail(SHWFS_ERR_INVALID, "unknown compute form %lld", (long long)v->ival);
       h->form = (int)v->ival;
       return build_gemm(h);
@@ -1442,8 +1459,25 @@ shwfs_status shwfs_batch_run(shwfs_batch* b, void* stream) {
   return SHWFS_OK;
 }
 
+shwfs_status shwfs_sample_noise(int kind, const float* lam, int64_t n, uint64_t seed, uint64_t frame, float* out,
+                                void* stream) {
+  if (n < 0 || n > (1LL << 32) || !out || (kind == 0 && !lam) || (kind != 0 && kind != 1))
+    return fail(SHWFS_ERR_INVALID, "bad noise-sampling arguments");
+  cudaStream_t st = (cudaStream_t)stream;
+  CK(launch_sample_noise(lam, n, seed, frame, kind, out, st));
+  if (!stream) CK(cudaStreamSynchronize(st));
+  return SHWFS_OK;
+}
+
 shwfs_status shwfs_batch_free(shwfs_batch* b) {
   delete b;
+  return SHWFS_OK;
+}
+
+shwfs_status shwfs_set_split_event(shwfs_handle* h, void* event) {
+  if (!h) return fail(SHWFS_ERR_INVALID, "null handle");
+  h->splitEvent = (cudaEvent_t)event;
+  h->version++;
   return SHWFS_OK;
 }
 

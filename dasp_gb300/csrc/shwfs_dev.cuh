@@ -162,29 +162,63 @@ __device__ __forceinline__ float loggam_f(float x) {
   return gl;
 }
 
-// Below lambda 30 a single uniform is inverted through the Poisson CDF by
-// sequential search (p_k = p_{k-1} lambda / k): a few FMAs per step, one
-// uniform, little divergence between lanes.  Above, Hormann's PTRS
-// transformed rejection as in the reference (cmod/src/centmodule.c:722-758),
-// whose quick-accept region grows with lambda.  Both draw from the pixel's
-// counter stream, so one Philox block usually suffices.
+// Poisson deviate by inversion of one uniform u along the support ordered
+// from the mode outwards.  The visited values always form an interval around
+// the mode m = floor(lam); each step extends it by the more probable of its
+// two neighbours (a fixed order that depends on lam only, so the inversion is
+// exact up to float rounding).  The expected number of steps is about
+// 1.5 sqrt(lam) (4.4 at lam 9.7), against lam + 1 for the search from 0.
+// P(m) = exp(m log1p((lam - m)/m) - (lam - m) + c(m)), c(m) = m ln m - m - ln m!
+// from Stirling's series for m >= 4 (truncation below 4e-8) and its exact
+// values for m = 1..3; m = 0 gives P(0) = exp(-lam).
+constexpr float kModalMaxLam = 64.0f;
+__device__ __forceinline__ float poisson_modal(float u, float lam) {
+  const float fm = floorf(lam);
+  float lp = -lam;
+  if (fm > 0.0f) {
+    const float d = lam - fm;  // exact
+    float c;
+    if (fm >= 4.0f) {
+      const float r = 1.0f / fm, r2 = r * r;
+      c = -0.5f * logf(6.28318530717958648f * fm) -
+          r * (1.0f / 12.0f - r2 * (1.0f / 360.0f - r2 * (1.0f / 1260.0f)));
+    } else {
+      c = fm == 1.0f ? -1.0f : (fm == 2.0f ? -1.30685281944005469f : -1.49592260322372630f);
+    }
+    lp = fm * log1pf(d / fm) - d + c;
+  }
+  const float pm = expf(lp);
+  float F = pm;
+  if (u <= F) return fm;
+  const float ilam = 1.0f / lam;
+  float kup = fm + 1.0f, kdn = fm - 1.0f;
+  float pup = pm * __fdividef(lam, kup);
+  float pdn = pm * fm * ilam;  // 0 when m = 0
+  // bound far in the tail: keeps the search finite when float rounding
+  // leaves F just below u
+  const int kmax = (int)(10.0f * sqrtf(lam)) + 20;
+  for (int it = 0; it < kmax; it++) {
+    const bool up = pup >= pdn;
+    F += up ? pup : pdn;
+    if (u <= F) return up ? kup : kdn;
+    if (up) {
+      kup += 1.0f;
+      pup *= __fdividef(lam, kup);
+    } else {
+      pdn *= kdn * ilam;
+      kdn -= 1.0f;
+    }
+  }
+  return fm;
+}
+
+// Below lambda 64 the modal inversion above (one uniform); above, Hormann's
+// PTRS transformed rejection as in the reference (cmod/src/centmodule.c:
+// 722-758), whose quick-accept region grows with lambda.  Both draw from the
+// pixel's counter stream, so one Philox block usually suffices.
 __device__ __forceinline__ float poisson_counter(CounterStream& st, float lam) {
   if (!(lam > 0.0f)) return 0.0f;
-  if (lam < 30.0f) {
-    const float u = st.uniform();
-    float p = __expf(-lam);
-    float F = p;
-    int k = 0;
-    // bound far in the tail: keeps the search finite when float rounding
-    // leaves F just below u
-    const int kmax = (int)(lam + 10.0f * sqrtf(lam)) + 20;
-    while (u > F && k < kmax) {
-      k++;
-      p *= __fdividef(lam, (float)k);
-      F += p;
-    }
-    return (float)k;
-  }
+  if (lam < kModalMaxLam) return poisson_modal(st.uniform(), lam);
   const float slam = sqrtf(lam), loglam = __logf(lam);
   const float b = 0.931f + 2.53f * slam;
   const float a = -0.059f + 0.02483f * b;

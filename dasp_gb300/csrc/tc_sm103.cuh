@@ -38,6 +38,29 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
+// Wait for the phase with the given parity to complete, for at most
+// max_cycles SM clock cycles.  A wait that runs out sets *abort; any wait
+// that sees *abort set returns false at once, so that after one failure the
+// whole CTA drains within a few polls instead of timing out wait by wait.
+__device__ __forceinline__ bool mbar_wait_abortable(uint64_t* bar, uint32_t parity, volatile int* abort,
+                                                    long long max_cycles) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const long long t0 = clock64();
+  for (uint32_t i = 1;; i++) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 63u) == 0) {
+      if (*abort) return false;
+      if (clock64() - t0 > max_cycles) {
+        *abort = 1;
+        return false;
+      }
+    }
+  }
+}
+// plain arrival (release) of this thread on bar
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
 // Wait for the phase with the given parity to complete; false after
 // max_iter polls (each try_wait already suspends for a while).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int max_iter) {
@@ -101,7 +124,34 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
+// instruction descriptor with an f32 accumulator, A and B of one type, both
+// K-major: fmt 0 = bf16 and 1 = f16 (kind::f16, type codes 1 and 0),
+// 2 = tf32 (kind::tf32, type code 2); the kFmt* values of gemm_form.h
+__host__ __device__ constexpr uint32_t idesc_f32acc(int fmt, int M, int N) {
+  const uint32_t t = fmt == 0 ? 1u : (fmt == 1 ? 0u : 2u);
+  return (1u << 4) | (t << 7) | (t << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
 // ---- MMA: D[tmem] (+)= A[smem] * B[smem]^T, issued by one thread ----
+template <int FMT>
+__device__ __forceinline__ void mma(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                    uint32_t accumulate) {
+  if constexpr (FMT == 2) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.u32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+  } else {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.u32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+  }
+}
 __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
                                          uint32_t accumulate) {
   asm volatile(

@@ -1,28 +1,44 @@
-// GEMM-DFT ("precision") form of the WFS step on the tcgen05 tensor cores.
+// GEMM-DFT ("precision") form of the WFS image formation on the tcgen05
+// tensor cores.
 //
 // For a tile of 128 subapertures (one per TMEM lane / MMA row):
 //
-//   GEMM1  F[s, (o,re|im)] = E[s, k] . W2[(o,re|im), k]          bf16 -> f32 (TMEM)
-//          E = pup*exp(i(phs - tilt)) as [Re E | Im E] over the p x p pixels
-//          (k < 2p^2), W2 = real embedding of the 2-D DFT restricted to the
-//          c x c outputs that survive the central crop (addPowerSpecCentral,
+//   GEMM1  F[s, (o,re|im)] = E[s, k] . W2[(o,re|im), k]                 -> f32 (TMEM)
+//          E = pup*exp(i(phs - tilt)) as [Re E | Im E] over the p x p pixels,
+//          W2 = real embedding of the 2-D DFT restricted to the c x c outputs
+//          that survive the central crop (addPowerSpecCentral,
 //          cmod/src/centmodule.c:430-471), 64 complex outputs per chunk
-//   |F|^2  per thread (its own subaperture), split into bf16 hi/lo
-//   GEMM2  B[s, q] += I[s, o] . Kc[q, o]                          bf16 -> f32 (TMEM)
+//   |F|^2  per thread (its own subaperture row)
+//   GEMM2  B[s, q] += I[s, o] . Kc[q, o]                                   -> f32 (TMEM)
 //          Kc = the whole linear chain 180-degree placement -> [prebin] ->
 //          spot-PSF circular convolution -> clip -> binImage, as one matrix
 //          (cmod/src/centmodule.c:504, 1816-1827)
 //
-// then normalisation, sky, noise, threshold and the shared post stages
-// (post_tile) exactly as the FP32 kernel.  Precision: one bf16 pass, or three
-// split-product passes (a.b ~ ah.bh + ah.bl + al.bh) with f32 accumulation.
+// then normalisation and sky (cmod/src/centmodule.c:1829-1872); the binned
+// pre-noise image goes to bimg, and wfs_post_kernel (wfs_post.cu) adds the
+// noise and computes the centroids.
 //
-// Constants (W2, Kc, hi and lo) are laid out on the host in the tensor-core
-// shared-memory order (K-major 8x8 core matrices, no swizzle) and streamed
-// into shared memory with bulk asynchronous copies; MMAs are issued by one
-// thread and tracked with mbarriers.  Every wait is bounded: a wait that runs
-// out records an error for the host instead of hanging.
+// Operand formats: bf16 (one pass, or three split-product passes
+// a.b ~ ah.bh + ah.bl + al.bh), fp16 (one pass; |F|^2 scaled per
+// subaperture by 1/(sum pup)^2 so that it stays far from the fp16 range
+// limit) and tf32 (one pass, kind::tf32).  Accumulation is always f32.
+//
+// Warp roles (576 threads):
+//   warps 0-15  consumers: thread t owns MMA row r = t & 127 (its subaperture)
+//               and column quarter q = t >> 7; they build E, read D1 and
+//               write |F|^2, read D2 and store the image
+//   warp 16     GEMM1 producer: streams W2 chunks through an NW-stage ring
+//               with bulk asynchronous copies and issues the GEMM1 MMAs
+//   warp 17     GEMM2 producer: streams Kc chunks (NK-stage ring) and
+//               issues the GEMM2 MMAs
+// All hand-offs are mbarriers (no block-wide barrier inside the tile loop);
+// every wait is bounded and a wait that runs out records an error for the
+// host instead of hanging.
+//
+// Constants (W2, Kc) are laid out on the host in the tensor-core
+// shared-memory order (K-major 8-row x 16-byte core matrices, no swizzle).
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <stdint.h>
 #include <string.h>
 
@@ -37,318 +53,390 @@ namespace shwfs {
 
 namespace {
 
-constexpr int kGemmThreads = 512;
+constexpr int kConsumers = 512;
+constexpr int kGemmThreads = kConsumers + 64;
 constexpr int kTileSubaps = 128;
 constexpr uint32_t kTmemCols = 512;
-constexpr int kWaitIter = 1 << 22;
+constexpr long long kWaitCycles = 4000000000LL;  // about 2 s at the maximum SM clock
 constexpr uint32_t kLBO = 128;  // bytes between core matrices along K
 
-__device__ __forceinline__ uint16_t bf16_bits(float x) {
-  return __bfloat16_as_ushort(__float2bfloat16_rn(x));
+// ---- element encodings (device) ----
+template <int FMT>
+__device__ __forceinline__ uint32_t enc(float x) {
+  if constexpr (FMT == kFmtBF16) {
+    return __bfloat16_as_ushort(__float2bfloat16_rn(x));
+  } else if constexpr (FMT == kFmtFP16) {
+    return __half_as_ushort(__float2half_rn(x));
+  } else {  // tf32: round to nearest even on the top 19 bits, kept as f32 bits
+    const uint32_t u = __float_as_uint(x);
+    return (u + 0xfffu + ((u >> 13) & 1u)) & 0xffffe000u;
+  }
 }
-__device__ __forceinline__ float bf16_val(uint16_t b) { return __bfloat162float(__ushort_as_bfloat16(b)); }
+template <int FMT>
+__device__ __forceinline__ float dec(uint32_t b) {
+  if constexpr (FMT == kFmtBF16) {
+    return __bfloat162float(__ushort_as_bfloat16((unsigned short)b));
+  } else if constexpr (FMT == kFmtFP16) {
+    return __half2float(__ushort_as_half((unsigned short)b));
+  } else {
+    return __uint_as_float(b);
+  }
+}
 
-struct GemmSmem {
-  uint32_t a1, w0, w1, a2, kc, img;  // byte offsets in dynamic smem
-  uint32_t total;
-};
+// 8 consecutive K elements of one row (16 bytes for 16-bit formats, 32 for
+// tf32) at byte offset `off` of a K-major tile: hi (and lo) parts
+template <int FMT, bool SPLIT>
+__device__ __forceinline__ void store8(uint8_t* hi, uint8_t* lo, uint32_t off, const float (&x)[8]) {
+  if constexpr (FMT == kFmtTF32) {
+    uint32_t h[8];
+#pragma unroll
+    for (int e = 0; e < 8; e++) h[e] = enc<FMT>(x[e]);
+    // elements 0-3 and 4-7 are in consecutive core matrices along K
+    *reinterpret_cast<uint4*>(hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4*>(hi + off + kLBO) = make_uint4(h[4], h[5], h[6], h[7]);
+  } else {
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      const uint32_t h0 = enc<FMT>(x[2 * e]), h1 = enc<FMT>(x[2 * e + 1]);
+      h[e] = h0 | (h1 << 16);
+      if constexpr (SPLIT) {
+        const uint32_t l0 = enc<FMT>(x[2 * e] - dec<FMT>(h0)), l1 = enc<FMT>(x[2 * e + 1] - dec<FMT>(h1));
+        l[e] = l0 | (l1 << 16);
+      }
+    }
+    *reinterpret_cast<uint4*>(hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
+    if constexpr (SPLIT) *reinterpret_cast<uint4*>(lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
+  }
+}
 
-__host__ __device__ inline GemmSmem gemm_smem_layout(const GemmGeom& g, int m) {
-  GemmSmem L;
-  const uint32_t a1 = (uint32_t)kTileSubaps * g.K1 * 2 * 2;            // E hi + lo
-  const uint32_t img = (uint32_t)kTileSubaps * m * m * 4;              // post-stage images
-  const uint32_t r0 = a1 > img ? a1 : img;
-  const uint32_t wst = (uint32_t)128 * g.KC * 2 * 2;                   // one W2 stage, hi + lo
-  const uint32_t a2 = (uint32_t)kTileSubaps * 64 * 2 * 2;              // |F|^2 chunk hi + lo
-  const uint32_t kc = (uint32_t)g.N2 * 64 * 2 * 2;                     // Kc chunk hi + lo
-  L.a1 = 0;
-  L.img = 0;
-  L.w0 = (r0 + 1023) & ~1023u;
-  L.w1 = L.w0 + wst;
-  L.a2 = L.w1 + wst;
-  L.kc = L.a2 + a2;
-  L.total = L.kc + kc;
-  return L;
+// byte offset of K element k of row `row` in a K-major no-swizzle tile whose
+// row groups are sbo bytes apart (esz = bytes per element)
+__host__ __device__ __forceinline__ uint32_t kmaj(int row, int k, int esz, uint32_t sbo) {
+  const uint32_t kb = (uint32_t)(k * esz);
+  return (uint32_t)(row >> 3) * sbo + (kb >> 4) * kLBO + (uint32_t)(row & 7) * 16u + (kb & 15u);
+}
+
+// phase -> [0, 2pi) reduction in float (Cody-Waite, 2pi = C1 + C2 with C1 =
+// 201/32 exact in 8 bits), then the fast sine/cosine on |t| <= pi
+__device__ __forceinline__ void sincos_reduced(float t, float* s, float* c) {
+  const float k = rintf(t * 0.15915494309189535f);
+  float r = fmaf(-k, 6.28125f, t);
+  r = fmaf(-k, 1.9353071795864769e-3f, r);
+  __sincosf(r, s, c);
 }
 
 struct Bars {
-  uint64_t w[2], wfree[2], d1[2], k, d2;
+  uint64_t wfull[kGemmMaxNW], wfree[kGemmMaxNW];
+  uint64_t kfull[kGemmMaxNK], kfree[kGemmMaxNK];
+  uint64_t efull, efree;
+  uint64_t d1full[2], d1free[2];
+  uint64_t a2full, a2free;
+  uint64_t d2full, d2free;
 };
 
-template <int PASSES>
+template <int FMT, int PASSES>
 __global__ void __launch_bounds__(kGemmThreads, 1)
-    wfs_gemm_kernel(const WfsArgs a, const GemmGeom g, int* err) {
+    wfs_gemm_kernel(const WfsArgs a, const GemmGeom g, const float* __restrict__ iscale, int* err) {
+  constexpr bool SPLIT = PASSES == 3;
+  constexpr int ESZ = FMT == kFmtTF32 ? 4 : 2;
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ Bars bars;
   __shared__ uint32_t s_tmem;
-  __shared__ int s_subap[kTileSubaps];
-  __shared__ int s_frame[kTileSubaps];
   __shared__ float s_tilt[256];
-  __shared__ float s_cw[256];
+  __shared__ int s_abort;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int p = a.p, pp = p * p, m = a.m, mm = m * m;
-  const GemmSmem L = gemm_smem_layout(g, m);
+  const int p = a.p, pp = p * p, ppr = (pp + 7) & ~7, mm = a.m * a.m;
+  const GemmSmem L = gemm_smem_layout(g);
   uint8_t* A1hi = smem + L.a1;
-  uint8_t* A1lo = A1hi + (size_t)kTileSubaps * g.K1 * 2;
-  uint8_t* Wst[2] = {smem + L.w0, smem + L.w1};
+  uint8_t* A1lo = A1hi + L.a1Half;
   uint8_t* A2hi = smem + L.a2;
-  uint8_t* A2lo = A2hi + kTileSubaps * 64 * 2;
-  uint8_t* KChi = smem + L.kc;
-  float* imgs = reinterpret_cast<float*>(smem + L.img);
-  const uint32_t sboE = (uint32_t)(g.K1 / 8) * 128;
-  const uint32_t sboW = (uint32_t)(g.KC / 8) * 128;
-  const uint32_t sbo64 = 8 * 128;
-  const uint32_t wHalf = (uint32_t)128 * g.KC * 2;   // bytes of the hi half of a W2 stage
-  const uint32_t kHalf = (uint32_t)g.N2 * 64 * 2;    // bytes of the hi half of a Kc chunk
+  uint8_t* A2lo = A2hi + L.a2Half;
+  const uint32_t sboE = (uint32_t)(g.K1 * ESZ / 16) * 128;
+  const uint32_t sboW = (uint32_t)(g.KCB / 16) * 128;
+  const uint32_t sbo2 = (uint32_t)(64 * ESZ / 16) * 128;
+  const int nseq = g.noc * g.nkc;
+  const int K1B = g.K1 * ESZ;
 
   for (int k = tid; k < pp; k += blockDim.x) s_tilt[k] = a.tilt[k];
-  if (a.centWeightDim == 2)
-    for (int k = tid; k < mm; k += blockDim.x) s_cw[k] = a.centWeight[k];
+  if (tid == 0) s_abort = 0;
   if (warp == 0) {
     tc::tmem_alloc<kTmemCols>(&s_tmem);
     tc::tmem_relinquish();
   }
   if (tid == 0) {
-    for (int i = 0; i < 2; i++) {
-      tc::mbar_init(&bars.w[i], 1);
+    for (int i = 0; i < g.NW; i++) {
+      tc::mbar_init(&bars.wfull[i], 1);
       tc::mbar_init(&bars.wfree[i], 1);
-      tc::mbar_init(&bars.d1[i], 1);
     }
-    tc::mbar_init(&bars.k, 1);
-    tc::mbar_init(&bars.d2, 1);
+    for (int i = 0; i < g.NK; i++) {
+      tc::mbar_init(&bars.kfull[i], 1);
+      tc::mbar_init(&bars.kfree[i], 1);
+    }
+    tc::mbar_init(&bars.efull, kConsumers / 32);
+    tc::mbar_init(&bars.efree, 1);
+    for (int i = 0; i < 2; i++) {
+      tc::mbar_init(&bars.d1full[i], 1);
+      tc::mbar_init(&bars.d1free[i], kConsumers / 32);
+    }
+    tc::mbar_init(&bars.a2full, kConsumers / 32);
+    tc::mbar_init(&bars.a2free, 1);
+    tc::mbar_init(&bars.d2full, 1);
+    tc::mbar_init(&bars.d2free, kConsumers / 32);
     tc::fence_mbar_init();
   }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = s_tmem;
-  const uint32_t tD1[2] = {tmem, tmem + 128};
-  const uint32_t tD2 = tmem + 256;
-  constexpr uint32_t idesc1 = tc::idesc_bf16_f32(128, 128);
-  const uint32_t idesc2 = tc::idesc_bf16_f32(128, g.N2);
-  const int nks1 = g.K1 / 16;          // k-steps of GEMM1
-  const int ksPerChunk = g.KC / 16;
   bool ok = true;
-
-  // global counters (continue across tiles) for barrier parities
-  uint32_t gW = 0;   // W2 chunk loads issued (thread 0)
-  uint32_t gC = 0;   // output chunks processed (all threads)
+  auto wait = [&](uint64_t* bar, uint32_t parity) {
+    if (!tc::mbar_wait_abortable(bar, parity, &s_abort, kWaitCycles)) ok = false;
+  };
 
   const long long nwork = (long long)a.nlit * a.nframes;
   const long long ntiles = (nwork + kTileSubaps - 1) / kTileSubaps;
+  const int myTiles = blockIdx.x < ntiles ? (int)((ntiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
 
-  // ---- thread 0: constant streaming and MMA issue ----
-  // The W2 K-chunks of a tile form one sequence j = oc*nkc + kc (global index
-  // gW + j across tiles) through a two-stage ring: chunk j+1 is fetched while
-  // chunk j's MMAs run.  Chunk 0 of the next tile is fetched during the last
-  // chunk of this one (the constants do not depend on the tile).
-  const int nseq = g.noc * g.nkc;
-  auto w2_load = [&](uint32_t gidx, int j) {
-    const uint32_t s = gidx & 1;
-    if (gidx >= 2 && !tc::mbar_wait(&bars.wfree[s], ((gidx >> 1) - 1) & 1, kWaitIter)) ok = false;
-    tc::mbar_expect_tx(&bars.w[s], 2 * wHalf);
-    tc::bulk_g2s(Wst[s], g.w2 + (size_t)j * 2 * wHalf, 2 * wHalf, &bars.w[s]);
-  };
-  auto kc_load = [&](int oc) {
-    tc::mbar_expect_tx(&bars.k, 2 * kHalf);
-    tc::bulk_g2s(KChi, g.kc2 + (size_t)oc * 2 * kHalf, 2 * kHalf, &bars.k);
-  };
-  auto issue_gemm1 = [&](int oc, uint32_t dcol, uint32_t gbase, bool more_tiles) {
-    for (int kc = 0; kc < g.nkc; kc++) {
-      const int j = oc * g.nkc + kc;
-      const uint32_t gidx = gbase + j;
-      const uint32_t s = gidx & 1;
-      if (!tc::mbar_wait(&bars.w[s], (gidx >> 1) & 1, kWaitIter)) ok = false;
-      tc::fence_after_sync();
-      const int k0 = kc * ksPerChunk;
-      const int k1 = min(nks1, k0 + ksPerChunk);
-      const uint32_t whi = tc::smem_addr(Wst[s]), wlo = whi + wHalf;
-      const uint32_t ehi = tc::smem_addr(A1hi), elo = tc::smem_addr(A1lo);
-      for (int ks = k0; ks < k1; ks++) {
-        const uint32_t eoff = (uint32_t)ks * 2 * kLBO, woff = (uint32_t)(ks - k0) * 2 * kLBO;
-        const uint32_t acc0 = (kc > 0 || ks > k0) ? 1u : 0u;
-        tc::mma_bf16(dcol, tc::smem_desc(ehi + eoff, kLBO, sboE), tc::smem_desc(whi + woff, kLBO, sboW), idesc1, acc0);
-        if (PASSES == 3) {
-          tc::mma_bf16(dcol, tc::smem_desc(ehi + eoff, kLBO, sboE), tc::smem_desc(wlo + woff, kLBO, sboW), idesc1, 1u);
-          tc::mma_bf16(dcol, tc::smem_desc(elo + eoff, kLBO, sboE), tc::smem_desc(whi + woff, kLBO, sboW), idesc1, 1u);
+  if (warp == kConsumers / 32) {
+    // ================= GEMM1 producer =================
+    if (lane == 0 && myTiles > 0) {
+      const long long totalJ = (long long)myTiles * nseq;
+      constexpr uint32_t idesc1 = tc::idesc_f32acc(FMT, 128, 128);
+      auto wload = [&](long long j) {  // global chunk j -> its ring stage
+        const int s = (int)(j % g.NW);
+        tc::mbar_expect_tx(&bars.wfull[s], L.wStage);
+        tc::bulk_g2s(smem + L.w + (size_t)s * L.wStage, g.w2 + (size_t)(j % nseq) * L.wStage, L.wStage,
+                     &bars.wfull[s]);
+      };
+      for (long long j = 0; j < g.NW && j < totalJ; j++) wload(j);
+      long long gJ = 0;
+      uint32_t gC = 0;
+      for (int lt = 0; lt < myTiles; lt++) {
+        wait(&bars.efull, lt & 1);
+        tc::fence_after_sync();
+        for (int oc = 0; oc < g.noc; oc++, gC++) {
+          const uint32_t buf = gC & 1;
+          if (gC >= 2) wait(&bars.d1free[buf], ((gC >> 1) - 1) & 1);
+          tc::fence_after_sync();
+          const uint32_t dcol = tmem + buf * 128;
+          for (int kc = 0; kc < g.nkc; kc++, gJ++) {
+            const int s = (int)(gJ % g.NW);
+            wait(&bars.wfull[s], (uint32_t)((gJ / g.NW) & 1));
+            tc::fence_after_sync();
+            const uint32_t whi = tc::smem_addr(smem + L.w + (size_t)s * L.wStage), wlo = whi + L.wHalf;
+            const uint32_t ehi = tc::smem_addr(A1hi), elo = tc::smem_addr(A1lo);
+            const int ks0 = kc * g.KCB / 32, ks1 = min(K1B, (kc + 1) * g.KCB) / 32;
+            for (int ks = ks0; ks < ks1; ks++) {
+              const uint32_t eoff = (uint32_t)ks * 2 * kLBO, woff = (uint32_t)(ks - ks0) * 2 * kLBO;
+              const uint32_t acc0 = ks > 0 ? 1u : 0u;
+              tc::mma<FMT>(dcol, tc::smem_desc(ehi + eoff, kLBO, sboE), tc::smem_desc(whi + woff, kLBO, sboW), idesc1,
+                           acc0);
+              if constexpr (SPLIT) {
+                tc::mma<FMT>(dcol, tc::smem_desc(ehi + eoff, kLBO, sboE), tc::smem_desc(wlo + woff, kLBO, sboW),
+                             idesc1, 1u);
+                tc::mma<FMT>(dcol, tc::smem_desc(elo + eoff, kLBO, sboE), tc::smem_desc(whi + woff, kLBO, sboW),
+                             idesc1, 1u);
+              }
+            }
+            tc::mma_commit(&bars.wfree[s]);
+            // refill the stage of the previous chunk (its MMAs were issued a
+            // chunk ago), keeping this chunk's MMAs queued meanwhile
+            if (gJ >= 1 && gJ - 1 + g.NW < totalJ) {
+              const int sp = (int)((gJ - 1) % g.NW);
+              wait(&bars.wfree[sp], (uint32_t)(((gJ - 1) / g.NW) & 1));
+              wload(gJ - 1 + g.NW);
+            }
+          }
+          tc::mma_commit(&bars.d1full[buf]);
+        }
+        tc::mma_commit(&bars.efree);
+      }
+    }
+    __syncwarp();
+  } else if (warp == kConsumers / 32 + 1) {
+    // ================= GEMM2 producer =================
+    if (lane == 0 && myTiles > 0) {
+      const long long totalK = (long long)myTiles * g.noc;
+      const uint32_t idesc2 = tc::idesc_f32acc(FMT, 128, g.N2);
+      const uint32_t sboK = sbo2;
+      auto kload = [&](long long j) {
+        const int s = (int)(j % g.NK);
+        tc::mbar_expect_tx(&bars.kfull[s], L.kStage);
+        tc::bulk_g2s(smem + L.k + (size_t)s * L.kStage, g.kc2 + (size_t)(j % g.noc) * L.kStage, L.kStage,
+                     &bars.kfull[s]);
+      };
+      for (long long j = 0; j < g.NK && j < totalK; j++) kload(j);
+      long long gK = 0;
+      const uint32_t dcol = tmem + 256;
+      for (int lt = 0; lt < myTiles; lt++) {
+        for (int oc = 0; oc < g.noc; oc++, gK++) {
+          if (oc == 0 && lt >= 1) wait(&bars.d2free, (lt - 1) & 1);
+          wait(&bars.a2full, (uint32_t)(gK & 1));
+          const int s = (int)(gK % g.NK);
+          wait(&bars.kfull[s], (uint32_t)((gK / g.NK) & 1));
+          tc::fence_after_sync();
+          const uint32_t ahi = tc::smem_addr(A2hi), alo = tc::smem_addr(A2lo);
+          const uint32_t khi = tc::smem_addr(smem + L.k + (size_t)s * L.kStage), klo = khi + L.kHalf;
+          for (int ks = 0; ks < 2 * ESZ; ks++) {
+            const uint32_t off = (uint32_t)ks * 2 * kLBO;
+            const uint32_t acc0 = (oc > 0 || ks > 0) ? 1u : 0u;
+            tc::mma<FMT>(dcol, tc::smem_desc(ahi + off, kLBO, sbo2), tc::smem_desc(khi + off, kLBO, sboK), idesc2,
+                         acc0);
+            if constexpr (SPLIT) {
+              tc::mma<FMT>(dcol, tc::smem_desc(ahi + off, kLBO, sbo2), tc::smem_desc(klo + off, kLBO, sboK), idesc2,
+                           1u);
+              tc::mma<FMT>(dcol, tc::smem_desc(alo + off, kLBO, sbo2), tc::smem_desc(khi + off, kLBO, sboK), idesc2,
+                           1u);
+            }
+          }
+          tc::mma_commit(&bars.a2free);
+          tc::mma_commit(&bars.kfree[s]);
+          if (oc == g.noc - 1) tc::mma_commit(&bars.d2full);
+          if (gK + g.NK < totalK) {
+            wait(&bars.kfree[s], (uint32_t)((gK / g.NK) & 1));
+            kload(gK + g.NK);
+          }
         }
       }
-      tc::mma_commit(&bars.wfree[s]);
-      if (j + 1 < nseq)
-        w2_load(gidx + 1, j + 1);
-      else if (more_tiles)
-        w2_load(gidx + 1, 0);
     }
-  };
-
-  if (tid == 0 && blockIdx.x < ntiles) {
-    w2_load(0, 0);
-    kc_load(0);
-  }
-  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const long long w0 = tile * kTileSubaps;
-    const int ns = (int)min((long long)kTileSubaps, nwork - w0);
-    const bool more = tile + gridDim.x < ntiles;
-    for (int s = tid; s < kTileSubaps; s += blockDim.x) {
-      if (s < ns) {
-        const long long w = w0 + s;
-        s_frame[s] = (int)(w / a.nlit);
-        s_subap[s] = a.lit[w % a.nlit];
-      }
-    }
-    __syncthreads();
-
-    // ---- E = pup*exp(i(phs - tilt)), split into bf16 hi/lo (row = subap);
-    // work items (subap, pixel), subap fastest ----
-    for (int w = tid; w < kTileSubaps * pp; w += blockDim.x) {
-      const int s = w & (kTileSubaps - 1), pix = w >> 7;
-      float er = 0.f, ei = 0.f;
-      if (s < ns) {
-        const int i = s_subap[s];
-        const int sy = i / a.nsubx, sx = i - sy * a.nsubx;
-        const int r = pix / p, j = pix - r * p;
-        const float t = a.phs[(long long)s_frame[s] * a.phsFrameStride + (long long)(sy * p + r) * a.W + sx * p + j] -
-                        s_tilt[pix];
-        float sn, cs;
-        sincosf(t, &sn, &cs);
-        const float pu = a.pup[(long long)i * pp + pix];
-        er = pu * cs;
-        ei = pu * sn;
-      }
-      const uint16_t hr = bf16_bits(er), hi_ = bf16_bits(ei);
-      const uint32_t offr = tc::kmajor_offset(s, pix, kLBO, sboE), offi = tc::kmajor_offset(s, pp + pix, kLBO, sboE);
-      *reinterpret_cast<uint16_t*>(A1hi + offr) = hr;
-      *reinterpret_cast<uint16_t*>(A1lo + offr) = bf16_bits(er - bf16_val(hr));
-      *reinterpret_cast<uint16_t*>(A1hi + offi) = hi_;
-      *reinterpret_cast<uint16_t*>(A1lo + offi) = bf16_bits(ei - bf16_val(hi_));
-    }
-    for (int w = tid; w < kTileSubaps * (g.K1 - 2 * pp); w += blockDim.x) {
-      const int s = w & (kTileSubaps - 1), k = 2 * pp + (w >> 7);
-      const uint32_t off = tc::kmajor_offset(s, k, kLBO, sboE);
-      *reinterpret_cast<uint16_t*>(A1hi + off) = 0;
-      *reinterpret_cast<uint16_t*>(A1lo + off) = 0;
-    }
-    tc::fence_async_smem();
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-
-    if (tid == 0) {
-      issue_gemm1(0, tD1[gC & 1], gW, more);
-      tc::mma_commit(&bars.d1[gC & 1]);
-    }
-    for (int oc = 0; oc < g.noc; oc++, gC++) {
-      const uint32_t buf = gC & 1;
-      // chunk oc+1 runs on the tensor cores while chunk oc is read out; its
-      // D1 buffer was last read before the previous iteration's barrier
-      if (tid == 0 && oc + 1 < g.noc) {
-        issue_gemm1(oc + 1, tD1[(gC + 1) & 1], gW, more);
-        tc::mma_commit(&bars.d1[(gC + 1) & 1]);
-      }
-      if (!tc::mbar_wait(&bars.d1[buf], (gC >> 1) & 1, kWaitIter)) ok = false;
-      // A2 and the Kc stage are free once the previous chunk's GEMM2 completed
-      if (oc > 0) {
-        if (!tc::mbar_wait(&bars.d2, (gC - 1) & 1, kWaitIter)) ok = false;
-        if (tid == 0) kc_load(oc);
-      }
-      tc::fence_after_sync();
-      // ---- |F|^2 of 64 outputs: warp w reads lanes 32*(w%4), columns
-      // 32*(w/4) .. +31 (16 complex outputs) ----
-      {
-        const int row = 32 * (warp & 3) + lane;
-        const int qtr = warp >> 2;
-        uint32_t ph_[8], pl_[8];
+    __syncwarp();
+  } else {
+    // ================= consumers =================
+    const int r = tid & 127, q = tid >> 7;
+    const uint32_t lanebase = (uint32_t)(32 * (warp & 3)) << 16;
+    uint32_t gC = 0, gA = 0;
+    // the previous tile's row (its D2 is read after this tile's E is built)
+    bool pLive = false;
+    int pSub = 0, pFrm = 0;
+    for (int lt = 0; lt <= myTiles; lt++) {
+      const long long tile = blockIdx.x + (long long)lt * gridDim.x;
+      bool live = false;
+      int sub = 0, frm = 0;
+      if (lt < myTiles) {
+        const long long w = tile * kTileSubaps + r;
+        live = w < nwork;
+        if (live) {
+          frm = (int)(w / a.nlit);
+          sub = a.lit[w % a.nlit];
+        }
+        // ---- E = pup*exp(i(phs - tilt)) for this row: groups of 8 pixels,
+        // Re at K = pix, Im at K = ppr + pix ----
+        if (lt >= 1) wait(&bars.efree, (lt - 1) & 1);
+        const int sy = sub / a.nsubx, sx = sub - sy * a.nsubx;
+        const float* ph = a.phs + (long long)frm * a.phsFrameStride + (long long)sy * p * a.W + sx * p;
+        const float* pu = a.pup + (long long)sub * pp;
+        for (int g8 = q; g8 * 8 < ppr; g8 += 4) {
+          float er[8], ei[8];
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
+          for (int e = 0; e < 8; e++) {
+            const int pix = g8 * 8 + e;
+            er[e] = 0.f;
+            ei[e] = 0.f;
+            if (live && pix < pp) {
+              const int ii = pix / p, jj = pix - ii * p;
+              const float t = ph[(long long)ii * a.W + jj] - s_tilt[pix];
+              float sn, cs;
+              if constexpr (SPLIT) {
+                sincosf(t, &sn, &cs);
+              } else {
+                sincos_reduced(t, &sn, &cs);
+              }
+              const float w0 = pu[pix];
+              er[e] = w0 * cs;
+              ei[e] = w0 * sn;
+            }
+          }
+          store8<FMT, SPLIT>(A1hi, A1lo, kmaj(r, g8 * 8, ESZ, sboE), er);
+          store8<FMT, SPLIT>(A1hi, A1lo, kmaj(r, ppr + g8 * 8, ESZ, sboE), ei);
+        }
+        // zero K padding beyond 2*ppr (none when 2*ppr is a multiple of 16)
+        for (int k = 2 * ppr + q; k < g.K1; k += 4) {
+          const uint32_t off = kmaj(r, k, ESZ, sboE);
+          if constexpr (ESZ == 4) {
+            *reinterpret_cast<uint32_t*>(A1hi + off) = 0u;
+          } else {
+            *reinterpret_cast<uint16_t*>(A1hi + off) = 0;
+            if constexpr (SPLIT) *reinterpret_cast<uint16_t*>(A1lo + off) = 0;
+          }
+        }
+        tc::fence_async_smem();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&bars.efull);
+      }
+      // ---- previous tile: binned image from D2, normalise, sky -> bimg ----
+      if (lt >= 1) {
+        wait(&bars.d2full, (lt - 1) & 1);
+        tc::fence_after_sync();
+        const int i = pSub;
+        const float totsig = a.totsig[i];
+        const float fr = a.frac[i];
+        float scale = totsig > 0.f ? (a.sigArr ? a.sigArr[i] / totsig : a.sig * fr / totsig) : 1.f;
+        if (iscale) scale = scale / iscale[i];  // undo the fp16 range scaling
+        const float skyv = a.sky * fr;
+        float* out = a.bimg + (long long)pFrm * a.bimgFrameStride + (long long)i * mm;
+        const float* skyA = a.skyArr ? a.skyArr + (long long)i * mm : nullptr;
+        for (int cb = q * 32; cb < mm; cb += 128) {
+          const int c1 = min(mm, cb + 32);
+          for (int q0 = cb; q0 < c1; q0 += 8) {
+            float v[8];
+            tc::tmem_ld8(tmem + 256 + lanebase + q0, v);
+            tc::tmem_ld_wait();
+            if (!pLive) continue;
+#pragma unroll
+            for (int e = 0; e < 8; e++) {
+              const int pix = q0 + e;
+              if (pix < c1) {
+                float x = v[e];
+                if (totsig > 0.f || iscale) x *= scale;
+                if (skyv > 0.f) x += skyv;
+                if (skyA) x += skyA[pix];
+                out[pix] = x;
+              }
+            }
+          }
+        }
+        tc::fence_before_sync();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&bars.d2free);
+      }
+      if (lt == myTiles) break;
+      pLive = live;
+      pSub = sub;
+      pFrm = frm;
+      const float isc = (iscale && live) ? iscale[sub] : 1.f;
+      // ---- output chunks: |F|^2 of 64 complex outputs; this thread reads
+      // columns 32q .. 32q+31 (16 outputs) of its row ----
+      for (int oc = 0; oc < g.noc; oc++, gC++, gA++) {
+        const uint32_t buf = gC & 1;
+        wait(&bars.d1full[buf], (gC >> 1) & 1);
+        tc::fence_after_sync();
+        float I[16];
+#pragma unroll
+        for (int h = 0; h < 4; h++) {
           float v[8];
-          tc::tmem_ld8(tD1[buf] + ((uint32_t)(32 * (warp & 3)) << 16) + qtr * 32 + q * 8, v);
+          tc::tmem_ld8(tmem + buf * 128 + lanebase + q * 32 + h * 8, v);
           tc::tmem_ld_wait();
 #pragma unroll
-          for (int e = 0; e < 4; e += 2) {
-            const float I0 = v[2 * e] * v[2 * e] + v[2 * e + 1] * v[2 * e + 1];
-            const float I1 = v[2 * e + 2] * v[2 * e + 2] + v[2 * e + 3] * v[2 * e + 3];
-            const uint16_t h0 = bf16_bits(I0), h1 = bf16_bits(I1);
-            const uint16_t l0 = bf16_bits(I0 - bf16_val(h0)), l1 = bf16_bits(I1 - bf16_val(h1));
-            ph_[q * 2 + e / 2] = (uint32_t)h0 | ((uint32_t)h1 << 16);
-            pl_[q * 2 + e / 2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
-          }
+          for (int e = 0; e < 4; e++) I[h * 4 + e] = (v[2 * e] * v[2 * e] + v[2 * e + 1] * v[2 * e + 1]) * isc;
         }
+        tc::fence_before_sync();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&bars.d1free[buf]);
+        // A2 is free once the previous chunk's GEMM2 has completed
+        if (gA >= 1) wait(&bars.a2free, (gA - 1) & 1);
 #pragma unroll
-        for (int c8 = 0; c8 < 2; c8++) {
-          const uint32_t off = tc::kmajor_offset(row, qtr * 16 + c8 * 8, kLBO, sbo64);
-          *reinterpret_cast<uint4*>(A2hi + off) = make_uint4(ph_[4 * c8], ph_[4 * c8 + 1], ph_[4 * c8 + 2], ph_[4 * c8 + 3]);
-          *reinterpret_cast<uint4*>(A2lo + off) = make_uint4(pl_[4 * c8], pl_[4 * c8 + 1], pl_[4 * c8 + 2], pl_[4 * c8 + 3]);
+        for (int h = 0; h < 2; h++) {
+          float x8[8];
+#pragma unroll
+          for (int e = 0; e < 8; e++) x8[e] = I[h * 8 + e];
+          store8<FMT, SPLIT>(A2hi, A2lo, kmaj(r, q * 16 + h * 8, ESZ, sbo2), x8);
         }
-      }
-      tc::fence_async_smem();
-      tc::fence_before_sync();
-      __syncthreads();
-      tc::fence_after_sync();
-      if (tid == 0) {
-        if (!tc::mbar_wait(&bars.k, gC & 1, kWaitIter)) ok = false;
-        tc::fence_after_sync();
-        const uint32_t ahi = tc::smem_addr(A2hi), alo = tc::smem_addr(A2lo);
-        const uint32_t khi = tc::smem_addr(KChi), klo = khi + kHalf;
-        for (int ks = 0; ks < 4; ks++) {
-          const uint32_t off = (uint32_t)ks * 2 * kLBO;
-          const uint32_t acc0 = (oc > 0 || ks > 0) ? 1u : 0u;
-          tc::mma_bf16(tD2, tc::smem_desc(ahi + off, kLBO, sbo64), tc::smem_desc(khi + off, kLBO, sbo64), idesc2, acc0);
-          if (PASSES == 3) {
-            tc::mma_bf16(tD2, tc::smem_desc(ahi + off, kLBO, sbo64), tc::smem_desc(klo + off, kLBO, sbo64), idesc2, 1u);
-            tc::mma_bf16(tD2, tc::smem_desc(alo + off, kLBO, sbo64), tc::smem_desc(khi + off, kLBO, sbo64), idesc2, 1u);
-          }
-        }
-        tc::mma_commit(&bars.d2);
+        tc::fence_async_smem();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&bars.a2full);
       }
     }
-    gW += nseq;
-    // ---- binned image: normalise, sky, noise, threshold -> shared memory;
-    // warp w reads lanes 32*(w%4), pixel columns 32*(w/4) + 128*j .. +31 ----
-    if (!tc::mbar_wait(&bars.d2, (gC - 1) & 1, kWaitIter)) ok = false;
-    if (tid == 0 && more) kc_load(0);  // Kc stage free: prefetch for the next tile
-    tc::fence_after_sync();
-    {
-      const int s = 32 * (warp & 3) + lane;
-      const int qtr = warp >> 2;
-      const bool live = s < ns;
-      const int i = live ? s_subap[s] : 0;
-      const float totsig = a.totsig[i];
-      const float fr = a.frac[i];
-      const float scale = totsig > 0.f ? (a.sigArr ? a.sigArr[i] / totsig : a.sig * fr / totsig) : 1.f;
-      const float skyv = a.sky * fr;
-      const bool pflag = totsig > 0.f || skyv > 0.f || a.skyArr;
-      const bool pois = a.addPoisson == 1 && a.calsource == 0 && pflag;
-      const float rn = a.calsource == 0 ? a.readNoise : 0.f;
-      const unsigned long long frm = frame_base(a) + (live ? s_frame[s] : 0);
-      for (int cb = qtr * 32; cb < mm; cb += 128) {
-      const int c1 = min(mm, cb + 32);
-      for (int q0 = cb; q0 < c1; q0 += 8) {
-        float v[8];
-        tc::tmem_ld8(tD2 + ((uint32_t)(32 * (warp & 3)) << 16) + q0, v);
-        tc::tmem_ld_wait();
-        if (!live) continue;
-#pragma unroll
-        for (int e = 0; e < 8; e++) {
-          const int pix = q0 + e;
-          if (pix >= c1) break;
-          float x = v[e];
-          if (totsig > 0.f) x *= scale;
-          if (skyv > 0.f) x += skyv;
-          if (a.skyArr) x += a.skyArr[(long long)i * mm + pix];
-          CounterStream st(a.seed, frm, i, pix, 0);
-          const float gnoise = rn != 0.f ? normal_counter(st) : 0.f;
-          if (pois) x = poisson_counter(st, x);
-          x += rn != 0.f ? rn * gnoise + a.readBg : a.readBg;
-          imgs[s * mm + pix] = threshold_px(x, a.floorv, a.threshType);
-        }
-      }
-      }
-    }
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    post_tile(a, ns, s_subap, s_frame, s_cw, [&](int s) { return imgs + s * mm; }, [&](int) { return mm; });
-    __syncthreads();  // the next tile's E build overwrites the image region
   }
   if (!ok) atomicOr(err, 2);
   tc::fence_before_sync();
@@ -371,66 +459,129 @@ float host_bf16_val(uint16_t b) {
   memcpy(&f, &u, 4);
   return f;
 }
-void put_split(uint8_t* hi, uint8_t* lo, uint32_t off, double v) {
-  const float f = (float)v;
-  const uint16_t h = host_bf16(f);
-  const uint16_t l = host_bf16(f - host_bf16_val(h));
-  memcpy(hi + off, &h, 2);
-  memcpy(lo + off, &l, 2);
+// IEEE binary16, round to nearest even (finite inputs of magnitude < 65520)
+uint16_t host_f16(float f) {
+  uint32_t x;
+  memcpy(&x, &f, 4);
+  const uint32_t sign = (x >> 16) & 0x8000u, ax = x & 0x7fffffffu;
+  if (ax >= 0x477ff000u) return (uint16_t)(sign | 0x7c00u);  // overflow -> inf
+  if (ax < 0x38800000u) {                                    // below 2^-14: subnormal, unit 2^-24
+    float v;
+    memcpy(&v, &ax, 4);
+    return (uint16_t)(sign | (uint32_t)std::nearbyint(v * 16777216.0f));
+  }
+  uint32_t h = ((((ax >> 23) - 127 + 15) & 0x1fu) << 10) | ((ax & 0x7fffffu) >> 13);
+  const uint32_t rem = ax & 0x1fffu;
+  if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) h++;
+  return (uint16_t)(sign | h);
 }
-uint32_t host_kmajor(int row, int k, uint32_t sbo) {
-  return (uint32_t)(row >> 3) * sbo + (uint32_t)(k >> 3) * kLBO + (uint32_t)(row & 7) * 16u + (uint32_t)(k & 7) * 2u;
+uint32_t host_tf32(float f) {
+  uint32_t u;
+  memcpy(&u, &f, 4);
+  return (u + 0xfffu + ((u >> 13) & 1u)) & 0xffffe000u;
+}
+// one constant in the operand format; with split, hi and lo parts
+void put_val(int fmt, bool split, uint8_t* hi, uint8_t* lo, uint32_t off, double v) {
+  const float f = (float)v;
+  if (fmt == kFmtTF32) {
+    const uint32_t b = host_tf32(f);
+    memcpy(hi + off, &b, 4);
+  } else if (fmt == kFmtFP16) {
+    const uint16_t b = host_f16(f);
+    memcpy(hi + off, &b, 2);
+  } else {
+    const uint16_t h = host_bf16(f);
+    memcpy(hi + off, &h, 2);
+    if (split) {
+      const uint16_t l = host_bf16(f - host_bf16_val(h));
+      memcpy(lo + off, &l, 2);
+    }
+  }
+}
+
+template <int FMT, int PASSES>
+cudaError_t launch_one(const WfsArgs& a, const GemmGeom& g, const float* iscale, int numSMs, int* err,
+                       cudaStream_t stream) {
+  const int smem = (int)gemm_smem_layout(g).total;
+  const long long nwork = (long long)a.nlit * a.nframes;
+  const long long ntiles = (nwork + kTileSubaps - 1) / kTileSubaps;
+  const int grid = (int)(ntiles < numSMs ? (ntiles > 0 ? ntiles : 1) : numSMs);
+  cudaError_t e = cudaFuncSetAttribute(wfs_gemm_kernel<FMT, PASSES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       smem);
+  if (e != cudaSuccess) return e;
+  wfs_gemm_kernel<FMT, PASSES><<<grid, kGemmThreads, smem, stream>>>(a, g, iscale, err);
+  return cudaGetLastError();
 }
 
 }  // namespace
 
-bool gemm_geometry(const GemmSpec& sp, GemmGeom* g) {
-  const int K1 = ((2 * sp.p * sp.p + 15) / 16) * 16;
+bool gemm_geometry(const GemmSpec& sp, int fmt, int passes, GemmGeom* g) {
+  if (fmt != kFmtBF16 && fmt != kFmtFP16 && fmt != kFmtTF32) return false;
+  if (passes != 1 && !(passes == 3 && fmt == kFmtBF16)) return false;
+  const int esz = fmt == kFmtTF32 ? 4 : 2;
+  const int pp = sp.p * sp.p, ppr = (pp + 7) & ~7;
+  const int K1 = ((2 * ppr + 15) / 16) * 16;
   const int mm = sp.m * sp.m;
   const int N2 = ((mm + 15) / 16) * 16;
-  if (K1 > 208 || N2 > 256 || mm > 256 || sp.p * sp.p > 256) return false;
+  if (N2 > 256 || pp > 256) return false;
+  g->fmt = fmt;
+  g->passes = passes;
   g->K1 = K1;
   g->N2 = N2;
   g->noc = (sp.c * sp.c + 63) / 64;
-  int KC = 64;
-  for (; KC >= 16; KC -= 16) {
+  g->KCB = 64;  // bytes of K per row in one streamed W2 chunk (two k-steps)
+  g->nkc = (K1 * esz + g->KCB - 1) / g->KCB;
+  // dynamic limit: 227 KB minus the kernel's static shared memory (< 2 KB)
+  const uint32_t limit = 227 * 1024 - 4096;
+  for (int nk = 2; nk >= 1; nk--) {
     GemmGeom t = *g;
-    t.KC = KC;
-    // dynamic limit 227 KB minus the kernel's ~3.2 KB of static shared memory
-    if (gemm_smem_layout(t, sp.m).total <= 227 * 1024 - 4096) break;
+    t.NK = nk;
+    t.NW = 0;
+    const GemmSmem base = gemm_smem_layout(t);
+    if (base.total > limit) continue;
+    const uint32_t wst = gemm_smem_layout(t).wStage;
+    int nw = (int)((limit - base.total) / wst);
+    if (nw > kGemmMaxNW) nw = kGemmMaxNW;
+    // prefer two Kc stages only when the W2 ring keeps at least 4 stages
+    if (nw < (nk == 2 ? 4 : 2)) continue;
+    g->NK = nk;
+    g->NW = nw;
+    return true;
   }
-  if (KC < 16) return false;
-  g->KC = KC;
-  g->nkc = (K1 + KC - 1) / KC;
-  return true;
+  return false;
 }
 
-int gemm_smem_bytes(const GemmGeom& g, int m) { return (int)gemm_smem_layout(g, m).total; }
+int gemm_smem_bytes(const GemmGeom& g) { return (int)gemm_smem_layout(g).total; }
 
 void gemm_build_w2(const GemmSpec& sp, const GemmGeom& g, std::vector<uint8_t>& out) {
-  const int p = sp.p, pp = p * p, c = sp.c, N = sp.N;
-  const size_t half = (size_t)128 * g.KC * 2;
-  out.assign((size_t)g.noc * g.nkc * 2 * half, 0);
-  const uint32_t sbo = (uint32_t)(g.KC / 8) * 128;
+  const int p = sp.p, pp = p * p, ppr = (pp + 7) & ~7, c = sp.c, N = sp.N;
+  const int esz = g.fmt == kFmtTF32 ? 4 : 2;
+  const bool split = g.passes == 3;
+  const GemmSmem L = gemm_smem_layout(g);
+  out.assign((size_t)g.noc * g.nkc * L.wStage, 0);
+  const uint32_t sbo = (uint32_t)(g.KCB / 16) * 128;
+  const int kce = g.KCB / esz;  // elements per chunk row
   for (int oc = 0; oc < g.noc; oc++)
     for (int ol = 0; ol < 64; ol++) {
       const int o = oc * 64 + ol;
       if (o >= c * c) continue;
       const int ku = sp.ro + o / c, kv = sp.ro + o % c;
-      for (int k = 0; k < 2 * pp; k++) {
-        const int pix = k < pp ? k : k - pp;
+      for (int k = 0; k < 2 * ppr; k++) {
+        const bool re = k < ppr;
+        const int pix = re ? k : k - ppr;
+        if (pix >= pp) continue;
         const int i = pix / p, j = pix % p;
         const long long e = ((long long)ku * i + (long long)kv * j) % N;
         const double th = -2.0 * M_PI * (double)e / N;
         const double cr = cos(th), si = sin(th);
         // row 2ol: Re F = sum Re W Re E - Im W Im E ; row 2ol+1: Im F = Im W Re E + Re W Im E
-        const double vre = k < pp ? cr : -si;
-        const double vim = k < pp ? si : cr;
-        const int kc = k / g.KC, kk = k % g.KC;
-        uint8_t* hi = out.data() + ((size_t)oc * g.nkc + kc) * 2 * half;
-        uint8_t* lo = hi + half;
-        put_split(hi, lo, host_kmajor(2 * ol, kk, sbo), vre);
-        put_split(hi, lo, host_kmajor(2 * ol + 1, kk, sbo), vim);
+        const double vre = re ? cr : -si;
+        const double vim = re ? si : cr;
+        const int kc = k / kce, kk = k % kce;
+        uint8_t* hi = out.data() + ((size_t)oc * g.nkc + kc) * L.wStage;
+        uint8_t* lo = hi + L.wHalf;
+        put_val(g.fmt, split, hi, lo, kmaj(2 * ol, kk, esz, sbo), vre);
+        put_val(g.fmt, split, hi, lo, kmaj(2 * ol + 1, kk, esz, sbo), vim);
       }
     }
 }
@@ -519,36 +670,33 @@ void gemm_kc_matrix(const GemmSpec& sp, std::vector<double>& kc) {
 void gemm_build_kc(const GemmSpec& sp, const GemmGeom& g, const std::vector<double>& kc, std::vector<uint8_t>& out) {
   // kc: [m*m][c*c] dense, row-major
   const int mm = sp.m * sp.m, cc = sp.c * sp.c;
-  const size_t half = (size_t)g.N2 * 64 * 2;
-  out.assign((size_t)g.noc * 2 * half, 0);
+  const int esz = g.fmt == kFmtTF32 ? 4 : 2;
+  const bool split = g.passes == 3;
+  const GemmSmem L = gemm_smem_layout(g);
+  const uint32_t sbo = (uint32_t)(64 * esz / 16) * 128;
+  out.assign((size_t)g.noc * L.kStage, 0);
   for (int oc = 0; oc < g.noc; oc++) {
-    uint8_t* hi = out.data() + (size_t)oc * 2 * half;
-    uint8_t* lo = hi + half;
+    uint8_t* hi = out.data() + (size_t)oc * L.kStage;
+    uint8_t* lo = hi + L.kHalf;
     for (int q = 0; q < mm; q++)
       for (int ol = 0; ol < 64; ol++) {
         const int o = oc * 64 + ol;
         if (o >= cc) continue;
-        put_split(hi, lo, host_kmajor(q, ol, 8 * 128), kc[(size_t)q * cc + o]);
+        put_val(g.fmt, split, hi, lo, kmaj(q, ol, esz, sbo), kc[(size_t)q * cc + o]);
       }
   }
 }
 
-cudaError_t launch_gemm(const WfsArgs& a, const GemmGeom& g, int passes, int numSMs, int* err, cudaStream_t stream) {
-  const int smem = gemm_smem_bytes(g, a.m);
-  const long long nwork = (long long)a.nlit * a.nframes;
-  const long long ntiles = (nwork + kTileSubaps - 1) / kTileSubaps;
-  const int grid = (int)(ntiles < numSMs ? (ntiles > 0 ? ntiles : 1) : numSMs);
-  cudaError_t e;
-  if (passes == 3) {
-    e = cudaFuncSetAttribute(wfs_gemm_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    wfs_gemm_kernel<3><<<grid, kGemmThreads, smem, stream>>>(a, g, err);
-  } else {
-    e = cudaFuncSetAttribute(wfs_gemm_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    wfs_gemm_kernel<1><<<grid, kGemmThreads, smem, stream>>>(a, g, err);
+cudaError_t launch_gemm(const WfsArgs& a, const GemmGeom& g, const float* iscale, int numSMs, int* err,
+                        cudaStream_t stream) {
+  if (g.NW < 2 || g.NW > kGemmMaxNW || g.NK < 1 || g.NK > kGemmMaxNK) return cudaErrorInvalidValue;
+  if (g.fmt == kFmtBF16) {
+    return g.passes == 3 ? launch_one<kFmtBF16, 3>(a, g, nullptr, numSMs, err, stream)
+                         : launch_one<kFmtBF16, 1>(a, g, nullptr, numSMs, err, stream);
   }
-  return cudaGetLastError();
+  if (g.fmt == kFmtFP16) return launch_one<kFmtFP16, 1>(a, g, iscale, numSMs, err, stream);
+  if (g.fmt == kFmtTF32) return launch_one<kFmtTF32, 1>(a, g, nullptr, numSMs, err, stream);
+  return cudaErrorInvalidValue;
 }
 
 }  // namespace shwfs

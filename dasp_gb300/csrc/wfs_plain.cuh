@@ -739,6 +739,9 @@ __global__ void __launch_bounds__(kThreads) wfs_plain_kernel(const WfsArgs a) {
 cudaError_t launch_unlit(const WfsArgs& a, const int* unlit, int nunlit, cudaStream_t stream);
 // increment n device counters (graph replays of a batch)
 cudaError_t launch_bump_counters(unsigned long long* const* ctrs, int n, cudaStream_t stream);
+// counter-based noise draws for testing the samplers (kind 0 Poisson, 1 normal)
+cudaError_t launch_sample_noise(const float* lam, long long n, unsigned long long seed, unsigned long long frame,
+                                int kind, float* out, cudaStream_t stream);
 // store v in one device counter, in stream order
 cudaError_t launch_set_counter(unsigned long long* ctr, unsigned long long v, cudaStream_t stream);
 // image-input (runSlope) kernel over the lit subapertures (wfs_image.cu)

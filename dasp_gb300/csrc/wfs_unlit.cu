@@ -69,6 +69,25 @@ cudaError_t launch_set_counter(unsigned long long* ctr, unsigned long long v, cu
   return cudaGetLastError();
 }
 
+// n draws of the counter-based noise (kind 0 Poisson of mean lam[i], kind 1
+// standard normal), element i from the stream of (seed, frame, i), as the
+// pipeline draws one pixel's noise
+__global__ void sample_noise_kernel(const float* __restrict__ lam, long long n, unsigned long long seed,
+                                    unsigned long long frame, int kind, float* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    CounterStream st(seed, frame, (int)(i >> 16), (int)(i & 0xffff), 2);
+    out[i] = kind == 0 ? poisson_counter(st, lam[i]) : normal_counter(st);
+  }
+}
+
+cudaError_t launch_sample_noise(const float* lam, long long n, unsigned long long seed, unsigned long long frame,
+                                int kind, float* out, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  const long long blocks = (n + 255) / 256 < 152 * 16 ? (n + 255) / 256 : 152 * 16;
+  sample_noise_kernel<<<(int)blocks, 256, 0, stream>>>(lam, n, seed, frame, kind, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_unlit(const WfsArgs& a, const int* unlit, int nunlit, cudaStream_t stream) {
   const long long total = (long long)nunlit * a.nframes * (a.imageOnly ? a.m * a.m : 1);
   if (total == 0) return cudaSuccess;

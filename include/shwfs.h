@@ -68,7 +68,7 @@ enum {
   /* extension: subapertures per CTA tile of the fused kernel, ival = 0 picks
    * the default for the geometry */
   SHWFS_TILESUBAPS = 101,
-  /* extension: compute form, ival = SHWFS_FORM_FP32 / _BF16 / _BF16X3 */
+  /* extension: compute form, ival = SHWFS_FORM_* */
   SHWFS_FORM = 102
 };
 
@@ -76,7 +76,9 @@ enum {
 enum {
   SHWFS_FORM_FP32 = 0,   /* fused FP32 kernel, register FFTs (default) */
   SHWFS_FORM_BF16 = 1,   /* GEMM-DFT on tcgen05 tensor cores, one bf16 pass */
-  SHWFS_FORM_BF16X3 = 2  /* GEMM-DFT, bf16 split products hi*hi + hi*lo + lo*hi */
+  SHWFS_FORM_BF16X3 = 2, /* GEMM-DFT, bf16 split products hi*hi + hi*lo + lo*hi */
+  SHWFS_FORM_FP16 = 3,   /* GEMM-DFT, one fp16 pass, |F|^2 scaled per subaperture */
+  SHWFS_FORM_TF32 = 4    /* GEMM-DFT, one tf32 pass (kind::tf32) */
 };
 
 /* noise generators */
@@ -247,6 +249,22 @@ shwfs_status shwfs_batch_free(shwfs_batch* b);
  * buffers and keep the fastest for this handle (results are unchanged: the
  * tile size only changes how subapertures are grouped per CTA). */
 shwfs_status shwfs_autotune(shwfs_handle* h, int* best_tile);
+
+/* Timing aid (no reference counterpart): with a non-NULL CUDA event, every
+ * readout of a tensor-core form records it on the launch stream between the
+ * image-formation kernel and the noise/centroid kernel, so that a caller can
+ * time the two separately.  NULL switches it off.  The event must outlive its
+ * use by the handle. */
+shwfs_status shwfs_set_split_event(shwfs_handle* h, void* event);
+
+/* Draws of the engine's counter-based noise for testing its samplers (no
+ * reference counterpart; the reference draws through rk_poisson/gsl,
+ * cmod/src/centmodule.c:722-784).  kind 0: out[i] ~ Poisson(lam[i]);
+ * kind 1: out[i] ~ N(0, 1) (lam unused).  Element i uses the stream of
+ * (seed, frame, i).  lam and out are device pointers; with stream NULL the
+ * call waits for the result. */
+shwfs_status shwfs_sample_noise(int kind, const float* lam, int64_t n, uint64_t seed, uint64_t frame, float* out,
+                                void* stream);
 
 /* ---- allocation-free image centroiding (no counterpart in the reference) ----
  *

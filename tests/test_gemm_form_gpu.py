@@ -31,12 +31,13 @@ def _run(c, form, mode="f64", frames=1):
     return info, max(errs_c), max(errs_b)
 
 
-@pytest.mark.parametrize("form,ctol,btol", [("bf16x3", 1e-4, 1e-3), ("bf16", 5e-3, 2e-2)])
+@pytest.mark.parametrize("form,ctol,btol", [("bf16x3", 1e-4, 1e-3), ("bf16", 5e-3, 2e-2), ("fp16", 1e-3, 5e-3),
+                                             ("tf32", 1e-3, 5e-3)])
 def test_elt_74x74_psf(form, ctol, btol):
     c = Case(nsubx=74, p=10, N=20, C=20, m=10, obs=0.28, Dtel=39.0, r0=0.157, L0=25.0, wavelength=589.0,
              psf="gauss", sig=500.0, skybrightness=10.0, noiseFloor=6.0)
     info, ec, eb = _run(c, form, frames=2)
-    assert info["form_active"] == {"bf16": 1, "bf16x3": 2}[form]
+    assert info["form_active"] == {"bf16": 1, "bf16x3": 2, "fp16": 3, "tf32": 4}[form]
     assert ec <= ctol, "centroid error %g px" % ec
     assert eb <= btol, "image error %g of peak" % eb
 
@@ -49,6 +50,16 @@ def test_geometries_bf16x3(kw):
     info, ec, eb = _run(c, "bf16x3")
     assert info["form_active"] == 2
     assert ec <= 1e-4 and eb <= 1e-3, (ec, eb)
+
+
+@pytest.mark.parametrize("form,code", [("fp16", 3), ("tf32", 4)])
+@pytest.mark.parametrize("kw", [dict(N=16, C=16, m=8, p=8), dict(N=20, C=16, m=8, p=10, psf="gauss"),
+                                dict(N=24, C=24, m=12, p=10), dict(N=22, C=22, m=11, p=11)])
+def test_geometries_one_pass_formats(kw, form, code):
+    c = Case(nsubx=12, sig=2e3, **kw)
+    info, ec, eb = _run(c, form)
+    assert info["form_active"] == code
+    assert ec <= 1e-3 and eb <= 5e-3, (ec, eb)
 
 
 def test_psf_padding_and_prebin_bf16x3():
