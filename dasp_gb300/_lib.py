@@ -35,9 +35,26 @@ EXPORTS = ("shwfs_initialise", "shwfs_run", "shwfs_run_slope", "shwfs_update", "
            "shwfs_last_error", "shwfs_run_async", "shwfs_run_batch", "shwfs_set_io",
            "shwfs_get_info", "shwfs_version", "shwfs_image_centroids_noalloc",
            "shwfs_batch_create", "shwfs_batch_run", "shwfs_batch_free", "shwfs_autotune",
-           "shwfs_sample_noise", "shwfs_set_split_event")
+           "shwfs_sample_noise", "shwfs_set_split_event", "shwfs_server_create", "shwfs_server_add_system",
+           "shwfs_server_remove_system", "shwfs_server_submit", "shwfs_server_poll", "shwfs_server_get_stats",
+           "shwfs_server_clock", "shwfs_server_destroy")
 
 NOALLOC_MAX_SUBAPS = 65536
+
+
+class ShwfsServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_int64), ("max_inflight", ctypes.c_int), ("device", ctypes.c_int)]
+
+
+class ShwfsCompletion(ctypes.Structure):
+    _fields_ = [("request", ctypes.c_uint64), ("system", ctypes.c_int), ("status", ctypes.c_int),
+                ("readout", ctypes.c_int), ("latency_s", ctypes.c_double), ("done_s", ctypes.c_double)]
+
+
+class ShwfsServerStats(ctypes.Structure):
+    _fields_ = [("systems", ctypes.c_int), ("admitted", ctypes.c_int), ("pending", ctypes.c_int),
+                ("used_bytes", ctypes.c_int64), ("budget_bytes", ctypes.c_int64), ("inflight", ctypes.c_int),
+                ("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64)]
 
 
 class ShwfsImageJob(ctypes.Structure):
@@ -122,9 +139,19 @@ def lib() -> ctypes.CDLL:
         L.shwfs_batch_free.argtypes = [vp]
         L.shwfs_autotune.argtypes = [vp, P(ctypes.c_int)]
         L.shwfs_set_split_event.argtypes = [vp, vp]
+        L.shwfs_server_create.argtypes = [P(ShwfsServerConfig), P(vp)]
+        L.shwfs_server_add_system.argtypes = [vp, P(ShwfsInit), ctypes.c_int, P(ctypes.c_int)]
+        L.shwfs_server_remove_system.argtypes = [vp, ctypes.c_int]
+        L.shwfs_server_submit.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int, vp, ctypes.c_double,
+                                          P(ctypes.c_uint64)]
+        L.shwfs_server_poll.argtypes = [vp, P(ShwfsCompletion), ctypes.c_int, P(ctypes.c_int)]
+        L.shwfs_server_get_stats.argtypes = [vp, P(ShwfsServerStats)]
+        L.shwfs_server_clock.argtypes = [vp]
+        L.shwfs_server_destroy.argtypes = [vp]
+        L.shwfs_server_clock.restype = ctypes.c_double
         L.shwfs_sample_noise.argtypes = [ctypes.c_int, vp, ctypes.c_int64, ctypes.c_uint64, ctypes.c_uint64, vp, vp]
         for name in EXPORTS:
-            if name not in ("shwfs_last_error", "shwfs_version"):
+            if name not in ("shwfs_last_error", "shwfs_version", "shwfs_server_clock"):
                 getattr(L, name).restype = ctypes.c_int
         _lib = L
     return _lib

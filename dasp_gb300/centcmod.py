@@ -182,10 +182,14 @@ class centcmod:
         ini.gaussianReplaceVal = float(self.gaussianReplaceVal)
         ini.inputImage = as_array(inputImage, "f", "inputImage", keep)
         ini.subapLocation = as_array(subapLocation, "i", "subapLocation", keep)
+        self._ini = ini
+        self._keep = keep  # borrowed arrays stay referenced while the handle lives
+        self._create(ini)
+
+    def _create(self, ini):
         handle = ctypes.c_void_p()
         check(_lib.lib().shwfs_initialise(ctypes.byref(ini), ctypes.byref(handle)), "initialise")
         self.centstruct = handle
-        self._keep = keep  # borrowed arrays stay referenced while the handle lives
 
     # -- util/centcmod.py:119-145 --
     def run(self, calsource):

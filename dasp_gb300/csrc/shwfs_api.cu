@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "../../include/shwfs.h"
+#include "engine_internal.h"
 #include "gemm_form.h"
 #include "refnoise.h"
 #include "wfs_launch.cuh"
@@ -1544,3 +1545,40 @@ shwfs_status shwfs_autotune(shwfs_handle* h, int* best_tile) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// hooks for the native runtime (engine_internal.h)
+// ---------------------------------------------------------------------------
+namespace shwfs {
+
+shwfs_status engine_frame(shwfs_handle* h, const float* phs_dev, cudaStream_t st, int* readout) {
+  *readout = readout_frame(h);
+  if (*readout) {
+    if (!h->cents.on_device || !h->bimg.on_device)
+      return fail(SHWFS_ERR_STATE, "engine_frame needs device-resident cents and bimg");
+    if (shwfs_status s = enqueue_readout(h, phs_dev, (float*)h->cents.data, (float*)h->bimg.data, 1, 0, st))
+      return s;
+    h->framesRead++;
+  }
+  h->curInteg++;
+  if (h->curInteg >= h->nintegrations + h->nlatency) h->curInteg = 0;
+  return SHWFS_OK;
+}
+
+int64_t engine_device_bytes(const shwfs_handle* h) {
+  int64_t b = 0;
+  auto add = [&](const auto& buf) { b += (int64_t)buf.n * (int64_t)sizeof(*buf.p); };
+  add(h->d_pup); add(h->d_tilt); add(h->d_frac); add(h->d_totsig); add(h->d_sigArr); add(h->d_skyArr);
+  add(h->d_cw); add(h->d_ref); add(h->d_calData); add(h->d_calSteps); add(h->d_calCoeff); add(h->d_fitMx);
+  add(h->d_binT); add(h->d_binN); add(h->d_psf); add(h->d_lit); add(h->d_unlit); add(h->d_binII);
+  add(h->d_binLo); add(h->d_binHi); add(h->d_ubArr); add(h->d_calBounds); add(h->d_subflag);
+  add(h->d_subapStart); add(h->d_status); add(h->d_psfSpec); add(h->d_phs); add(h->d_cents); add(h->d_bimg);
+  add(h->d_image); add(h->d_subapLoc); add(h->d_poisFlag); add(h->d_rng); add(h->d_w2); add(h->d_kc2);
+  add(h->d_iscale); add(h->d_frameCtr);
+  return b;
+}
+
+const int* engine_status_ptr(const shwfs_handle* h) { return h->d_status.p; }
+int engine_nsubaps(const shwfs_handle* h) { return h->nsubaps; }
+
+}  // namespace shwfs

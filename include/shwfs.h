@@ -312,6 +312,60 @@ typedef struct shwfs_image_job {
 } shwfs_image_job;
 shwfs_status shwfs_image_centroids_noalloc(const shwfs_image_job* job, void* stream, char* err, size_t errlen);
 
+/* ---- serving loop (no reference counterpart; the reference runs each WFS
+ * of a simulation in its own process step, science/wfscent.py:585-683) ----
+ * A server owns a dispatcher thread that serves WFS-frame requests of many
+ * simulated AO systems on one GPU with continuous batching: a request is
+ * launched as soon as its release time has passed, its system has no frame
+ * in flight and a device slot is free, each system on its own CUDA stream so
+ * that frames of different systems overlap on the device.  Systems are
+ * admitted against a fixed HBM budget: a system whose device state does not
+ * fit waits until removed systems free enough memory.  A system's state
+ * (pupil, PSF spectra, tables, integration state, output buffers) stays on
+ * the device while it is admitted.  The engine of a system is created from
+ * its shwfs_init when admitted; the arrays the init points to must stay
+ * valid until then (phs, cents and bimg there only give shapes: the server
+ * allocates the system's own device buffers).  All calls are thread-safe. */
+typedef struct shwfs_server shwfs_server;
+typedef struct shwfs_server_config {
+  int64_t hbm_budget_bytes; /* device memory the admitted systems may hold */
+  int max_inflight;         /* frames on the device at once (all systems) */
+  int device;               /* CUDA device ordinal */
+} shwfs_server_config;
+typedef struct shwfs_completion {
+  uint64_t request;  /* id returned by shwfs_server_submit */
+  int system;
+  int status;        /* SHWFS_OK, or the failure of this frame */
+  int readout;       /* 1: a readout frame (centroids written), 0: integrating */
+  double latency_s;  /* from the release time to completion seen by the server */
+  double done_s;     /* completion time on the server clock */
+} shwfs_completion;
+typedef struct shwfs_server_stats {
+  int systems, admitted, pending;
+  int64_t used_bytes, budget_bytes;
+  int inflight;
+  uint64_t submitted, completed;
+} shwfs_server_stats;
+
+shwfs_status shwfs_server_create(const shwfs_server_config* cfg, shwfs_server** out);
+/* form: SHWFS_FORM_*; *system receives the system id */
+shwfs_status shwfs_server_add_system(shwfs_server* s, const shwfs_init* init, int form, int* system);
+shwfs_status shwfs_server_remove_system(shwfs_server* s, int system);
+/* One WFS frame of `system` from the W x W float32 phase at `phs` (device
+ * pointer when phs_on_device, else host); released at release_s on the
+ * server clock (seconds since creation; <= 0: now).  With out_cents non-NULL
+ * the frame's centroids (nsubaps*2 floats, host memory) are written there
+ * before the completion is reported.  The phase must stay valid until the
+ * request completes. */
+shwfs_status shwfs_server_submit(shwfs_server* s, int system, const float* phs, int phs_on_device, float* out_cents,
+                                 double release_s, uint64_t* request);
+/* up to max completions since the last poll; *n receives the count */
+shwfs_status shwfs_server_poll(shwfs_server* s, shwfs_completion* out, int max, int* n);
+shwfs_status shwfs_server_get_stats(shwfs_server* s, shwfs_server_stats* st);
+/* seconds since the server was created */
+double shwfs_server_clock(shwfs_server* s);
+shwfs_status shwfs_server_destroy(shwfs_server* s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -53,8 +53,8 @@ def test_geometries_bf16x3(kw):
 
 
 @pytest.mark.parametrize("form,code", [("fp16", 3), ("tf32", 4)])
-@pytest.mark.parametrize("kw", [dict(N=16, C=16, m=8, p=8), dict(N=20, C=16, m=8, p=10, psf="gauss"),
-                                dict(N=24, C=24, m=12, p=10), dict(N=22, C=22, m=11, p=11)])
+@pytest.mark.parametrize("kw", [dict(N=16, C=16, m=8, p=8), dict(N=20, C=16, m=8, p=10, psf="gauss", psfsize=20),
+                                dict(N=24, C=24, m=12, p=10), dict(N=24, C=24, m=12, p=12)])
 def test_geometries_one_pass_formats(kw, form, code):
     c = Case(nsubx=12, sig=2e3, **kw)
     info, ec, eb = _run(c, form)
