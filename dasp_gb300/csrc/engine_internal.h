@@ -19,5 +19,7 @@ int64_t engine_device_bytes(const shwfs_handle* h);
 // limit, bit 2: tensor-core wait timed out)
 const int* engine_status_ptr(const shwfs_handle* h);
 int engine_nsubaps(const shwfs_handle* h);
+// set the calling thread's shwfs_last_error() message; returns st
+shwfs_status engine_fail(shwfs_status st, const char* msg);
 
 }  // namespace shwfs

@@ -1580,5 +1580,6 @@ int64_t engine_device_bytes(const shwfs_handle* h) {
 
 const int* engine_status_ptr(const shwfs_handle* h) { return h->d_status.p; }
 int engine_nsubaps(const shwfs_handle* h) { return h->nsubaps; }
+shwfs_status engine_fail(shwfs_status st, const char* msg) { return fail(st, "%s", msg); }
 
 }  // namespace shwfs

@@ -309,7 +309,8 @@ struct shwfs_server {
 extern "C" {
 
 shwfs_status shwfs_server_create(const shwfs_server_config* cfg, shwfs_server** out) {
-  if (!cfg || !out || cfg->hbm_budget_bytes <= 0 || cfg->max_inflight < 1) return SHWFS_ERR_INVALID;
+  if (!cfg || !out || cfg->hbm_budget_bytes <= 0 || cfg->max_inflight < 1)
+    return shwfs::engine_fail(SHWFS_ERR_INVALID, "server needs a positive HBM budget and max_inflight >= 1");
   shwfs_server* s = new shwfs_server;
   s->cfg = *cfg;
   s->t0 = Clock::now();
@@ -319,14 +320,17 @@ shwfs_status shwfs_server_create(const shwfs_server_config* cfg, shwfs_server** 
 }
 
 shwfs_status shwfs_server_add_system(shwfs_server* s, const shwfs_init* init, int form, int* system) {
-  if (!s || !init || !system || form < SHWFS_FORM_FP32 || form > SHWFS_FORM_TF32) return SHWFS_ERR_INVALID;
-  if (!init->phs.data || !init->cents.data || !init->bimg.data) return SHWFS_ERR_INVALID;
+  if (!s || !init || !system || form < SHWFS_FORM_FP32 || form > SHWFS_FORM_TF32)
+    return shwfs::engine_fail(SHWFS_ERR_INVALID, "bad add_system arguments");
+  if (!init->phs.data || !init->cents.data || !init->bimg.data)
+    return shwfs::engine_fail(SHWFS_ERR_INVALID, "phs, cents and bimg must give the system's shapes");
   auto sys = std::make_unique<System>();
   sys->init = *init;
   sys->form = form;
   sys->estimate = estimate_bytes(*init, form);
   std::lock_guard<std::mutex> lk(s->mu);
-  if (sys->estimate > s->cfg.hbm_budget_bytes) return SHWFS_ERR_NOMEM;
+  if (sys->estimate > s->cfg.hbm_budget_bytes)
+    return shwfs::engine_fail(SHWFS_ERR_NOMEM, "system needs more device memory than the whole HBM budget");
   sys->id = (int)s->systems.size();
   *system = sys->id;
   s->systems.push_back(std::move(sys));
@@ -350,12 +354,13 @@ shwfs_status shwfs_server_remove_system(shwfs_server* s, int system) {
 
 shwfs_status shwfs_server_submit(shwfs_server* s, int system, const float* phs, int phs_on_device, float* out_cents,
                                  double release_s, uint64_t* request) {
-  if (!s || !phs) return SHWFS_ERR_INVALID;
+  if (!s || !phs) return shwfs::engine_fail(SHWFS_ERR_INVALID, "null server or phase");
   std::lock_guard<std::mutex> lk(s->mu);
-  if (system < 0 || system >= (int)s->systems.size()) return SHWFS_ERR_INVALID;
+  if (system < 0 || system >= (int)s->systems.size()) return shwfs::engine_fail(SHWFS_ERR_INVALID, "no such system");
   System& sys = *s->systems[system];
-  if (sys.removing) return SHWFS_ERR_STATE;
-  if (sys.failed) return SHWFS_ERR_STATE;
+  if (sys.removing) return shwfs::engine_fail(SHWFS_ERR_STATE, "system is being removed");
+  if (sys.failed)
+    return shwfs::engine_fail(SHWFS_ERR_STATE, ("system could not be started: " + sys.error).c_str());
   Request r{};
   r.id = s->nextReq++;
   r.phs = phs;

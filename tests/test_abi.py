@@ -15,7 +15,7 @@ HEADER = os.path.join(ROOT, "include", "shwfs.h")
 
 def declared_functions():
     src = open(HEADER).read()
-    return sorted(set(re.findall(r"^\s*(?:shwfs_status|const char\*)\s+(shwfs_\w+)\s*\(", src, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:shwfs_status|const char\*|double)\s+(shwfs_\w+)\s*\(", src, re.M)))
 
 
 def test_header_declares_reference_entry_points():
