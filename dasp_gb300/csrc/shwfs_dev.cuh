@@ -177,26 +177,27 @@ __device__ __forceinline__ float poisson_modal(float u, float lam) {
   float lp = -lam;
   if (fm > 0.0f) {
     const float d = lam - fm;  // exact
+    const float r = __fdividef(1.0f, fm);
     float c;
     if (fm >= 4.0f) {
-      const float r = 1.0f / fm, r2 = r * r;
-      c = -0.5f * logf(6.28318530717958648f * fm) -
+      const float r2 = r * r;
+      c = -0.5f * __logf(6.28318530717958648f * fm) -
           r * (1.0f / 12.0f - r2 * (1.0f / 360.0f - r2 * (1.0f / 1260.0f)));
     } else {
       c = fm == 1.0f ? -1.0f : (fm == 2.0f ? -1.30685281944005469f : -1.49592260322372630f);
     }
-    lp = fm * log1pf(d / fm) - d + c;
+    lp = fm * log1pf(d * r) - d + c;
   }
-  const float pm = expf(lp);
+  const float pm = __expf(lp);
   float F = pm;
   if (u <= F) return fm;
-  const float ilam = 1.0f / lam;
+  const float ilam = __fdividef(1.0f, lam);
   float kup = fm + 1.0f, kdn = fm - 1.0f;
   float pup = pm * __fdividef(lam, kup);
   float pdn = pm * fm * ilam;  // 0 when m = 0
-  // bound far in the tail: keeps the search finite when float rounding
-  // leaves F just below u
-  const int kmax = (int)(10.0f * sqrtf(lam)) + 20;
+  // bound far in the tail (at least 10 sqrt(lam) + 20 for lam < 64): keeps
+  // the search finite when float rounding leaves F just below u
+  const int kmax = 2 * (int)lam + 40;
   for (int it = 0; it < kmax; it++) {
     const bool up = pup >= pdn;
     F += up ? pup : pdn;
@@ -240,8 +241,18 @@ __device__ __forceinline__ float poisson_counter(CounterStream& st, float lam) {
 // one standard normal deviate (Box-Muller, cosine branch)
 __device__ __forceinline__ float normal_counter(CounterStream& st) {
   const float u1 = st.uniform(), u2 = st.uniform();
-  const float r = sqrtf(-2.0f * __logf(u1));
+  const float q = -2.0f * __logf(u1);  // > 0: u1 < 1
+  const float r = q * rsqrtf(q);
   return r * __cosf(6.28318530717958648f * u2 - 3.14159265358979324f) * -1.0f;
+}
+
+// floor(w / d) for 0 <= w < 2^22 and d >= 1 with the float reciprocal
+// inv_d ~ 1/d, corrected to the exact quotient
+__device__ __forceinline__ int div_small(int w, int d, float inv_d) {
+  int q = (int)((float)w * inv_d);
+  if (q * d > w) q--;
+  else if ((q + 1) * d <= w) q++;
+  return q;
 }
 
 // readCCD threshold (cmod/src/centmodule.c:785-817)

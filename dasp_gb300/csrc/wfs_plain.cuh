@@ -250,8 +250,9 @@ __device__ __forceinline__ void post_tile(const WfsArgs& a, int ns, const int* s
     }
 
     // ---- 8: pixel power, bimg write ----
+    const float inv_mm = 1.0f / (float)mm;
     for (int w = tid; w < ns * mm; w += blockDim.x) {
-      const int s = w / mm, pix = w - (w / mm) * mm;
+      const int s = div_small(w, mm, inv_mm), pix = w - s * mm;
       float v = img_of(s)[pix];
       if (pix < nexp_of(s)) {
         if (a.pxlPower == 2.f)

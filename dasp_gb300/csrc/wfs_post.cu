@@ -25,6 +25,7 @@ __global__ void __launch_bounds__(kPostThreads, 4) wfs_post_kernel(const WfsArgs
   extern __shared__ float smem_post[];
   __shared__ int s_subap[kPostMaxTS];
   __shared__ int s_frame[kPostMaxTS];
+  __shared__ unsigned char s_pflag[kPostMaxTS];
   const int tid = threadIdx.x;
   const int mm = a.m * a.m;
   const bool cw2d = a.centWeightDim == 2;
@@ -46,21 +47,23 @@ __global__ void __launch_bounds__(kPostThreads, 4) wfs_post_kernel(const WfsArgs
     __syncthreads();  // previous tile fully consumed
     for (int s = tid; s < ns; s += blockDim.x) {
       const long long w = w0 + s;
+      const int i = a.lit[w % a.nlit];
       s_frame[s] = (int)(w / a.nlit);
-      s_subap[s] = a.lit[w % a.nlit];
+      s_subap[s] = i;
+      s_pflag[s] = a.totsig[i] > 0.f || a.sky * a.frac[i] > 0.f || a.skyArr;
     }
     __syncthreads();
+    const float inv_mm = 1.0f / (float)mm;
     for (int w = tid; w < ns * mm; w += blockDim.x) {
-      const int s = w / mm, pix = w - s * mm;
+      const int s = div_small(w, mm, inv_mm), pix = w - s * mm;
       const int i = s_subap[s];
       float v = a.bimg[(long long)s_frame[s] * a.bimgFrameStride + (long long)i * mm + pix];
       if (noise) {
         // one stream per pixel: the read-noise normal takes the first two
         // uniforms, the Poisson sampler continues from the third
-        const bool pflag = a.totsig[i] > 0.f || a.sky * a.frac[i] > 0.f || a.skyArr;
         CounterStream st(a.seed, fbase + s_frame[s], i, pix, 0);
         const float g = rn != 0.f ? normal_counter(st) : 0.f;
-        if (pois && pflag) v = poisson_counter(st, v);
+        if (pois && s_pflag[s]) v = poisson_counter(st, v);
         if (rn != 0.f)
           v += rn * g + a.readBg;
         else

@@ -54,7 +54,7 @@ def test_geometries_bf16x3(kw):
 
 @pytest.mark.parametrize("form,code", [("fp16", 3), ("tf32", 4)])
 @pytest.mark.parametrize("kw", [dict(N=16, C=16, m=8, p=8), dict(N=20, C=16, m=8, p=10, psf="gauss", psfsize=20),
-                                dict(N=24, C=24, m=12, p=10), dict(N=24, C=24, m=12, p=12)])
+                                dict(N=24, C=24, m=12, p=10), dict(N=24, C=24, m=12, p=11)])
 def test_geometries_one_pass_formats(kw, form, code):
     c = Case(nsubx=12, sig=2e3, **kw)
     info, ec, eb = _run(c, form)
