@@ -200,17 +200,28 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
 
   if (warp == kConsumers / 32) {
     // ================= GEMM1 producer =================
+    // Ring bookkeeping without divisions: chunk gJ sits in stage cs with
+    // phase bit cph; the previous chunk's stage/phase are ps/pph; lseq is the
+    // W2 chunk (mod nseq) of the next load.
     if (lane == 0 && myTiles > 0) {
-      const long long totalJ = (long long)myTiles * nseq;
+      const int totalJ = myTiles * nseq;
       constexpr uint32_t idesc1 = tc::idesc_f32acc(FMT, 128, 128);
-      auto wload = [&](long long j) {  // global chunk j -> its ring stage
-        const int s = (int)(j % g.NW);
+      const uint32_t wbase = tc::smem_addr(smem + L.w);
+      int nextLoad = 0, lseq = 0;
+      auto wload = [&](int s) {  // chunk lseq -> stage s
         tc::mbar_expect_tx(&bars.wfull[s], L.wStage);
-        tc::bulk_g2s(smem + L.w + (size_t)s * L.wStage, g.w2 + (size_t)(j % nseq) * L.wStage, L.wStage,
-                     &bars.wfull[s]);
+        tc::bulk_g2s(smem + L.w + (size_t)s * L.wStage, g.w2 + (size_t)lseq * L.wStage, L.wStage, &bars.wfull[s]);
+        nextLoad++;
+        if (++lseq == nseq) lseq = 0;
       };
-      for (long long j = 0; j < g.NW && j < totalJ; j++) wload(j);
-      long long gJ = 0;
+      for (int s0 = 0; s0 < g.NW && nextLoad < totalJ; s0++) wload(s0);
+      // descriptors: the 14-bit start-address field (bits 0-13, in 16-byte
+      // units) advances by 16 per k-step of 256 bytes; all addresses < 256 KB
+      const uint64_t dEh = tc::smem_desc(tc::smem_addr(A1hi), kLBO, sboE);
+      const uint64_t dEl = tc::smem_desc(tc::smem_addr(A1lo), kLBO, sboE);
+      int cs = 0, ps = 0;
+      uint32_t cph = 0, pph = 0;
+      bool first = true;
       uint32_t gC = 0;
       for (int lt = 0; lt < myTiles; lt++) {
         wait(&bars.efull, lt & 1);
@@ -220,32 +231,34 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
           if (gC >= 2) wait(&bars.d1free[buf], ((gC >> 1) - 1) & 1);
           tc::fence_after_sync();
           const uint32_t dcol = tmem + buf * 128;
-          for (int kc = 0; kc < g.nkc; kc++, gJ++) {
-            const int s = (int)(gJ % g.NW);
-            wait(&bars.wfull[s], (uint32_t)((gJ / g.NW) & 1));
+          int ks = 0;
+          for (int kc = 0; kc < g.nkc; kc++) {
+            wait(&bars.wfull[cs], cph);
             tc::fence_after_sync();
-            const uint32_t whi = tc::smem_addr(smem + L.w + (size_t)s * L.wStage), wlo = whi + L.wHalf;
-            const uint32_t ehi = tc::smem_addr(A1hi), elo = tc::smem_addr(A1lo);
-            const int ks0 = kc * g.KCB / 32, ks1 = min(K1B, (kc + 1) * g.KCB) / 32;
-            for (int ks = ks0; ks < ks1; ks++) {
-              const uint32_t eoff = (uint32_t)ks * 2 * kLBO, woff = (uint32_t)(ks - ks0) * 2 * kLBO;
-              const uint32_t acc0 = ks > 0 ? 1u : 0u;
-              tc::mma<FMT>(dcol, tc::smem_desc(ehi + eoff, kLBO, sboE), tc::smem_desc(whi + woff, kLBO, sboW), idesc1,
-                           acc0);
+            const uint64_t dWh = tc::smem_desc(wbase + (uint32_t)cs * L.wStage, kLBO, sboW);
+            const uint64_t dWl = dWh + (L.wHalf >> 4);
+            const int ks1 = min(K1B, (kc + 1) * g.KCB) >> 5;
+            for (uint64_t wo = 0; ks < ks1; ks++, wo += 16) {
+              const uint64_t eo = (uint64_t)ks * 16;
+              tc::mma<FMT>(dcol, dEh + eo, dWh + wo, idesc1, ks > 0 ? 1u : 0u);
               if constexpr (SPLIT) {
-                tc::mma<FMT>(dcol, tc::smem_desc(ehi + eoff, kLBO, sboE), tc::smem_desc(wlo + woff, kLBO, sboW),
-                             idesc1, 1u);
-                tc::mma<FMT>(dcol, tc::smem_desc(elo + eoff, kLBO, sboE), tc::smem_desc(whi + woff, kLBO, sboW),
-                             idesc1, 1u);
+                tc::mma<FMT>(dcol, dEh + eo, dWl + wo, idesc1, 1u);
+                tc::mma<FMT>(dcol, dEl + eo, dWh + wo, idesc1, 1u);
               }
             }
-            tc::mma_commit(&bars.wfree[s]);
+            tc::mma_commit(&bars.wfree[cs]);
             // refill the stage of the previous chunk (its MMAs were issued a
-            // chunk ago), keeping this chunk's MMAs queued meanwhile
-            if (gJ >= 1 && gJ - 1 + g.NW < totalJ) {
-              const int sp = (int)((gJ - 1) % g.NW);
-              wait(&bars.wfree[sp], (uint32_t)(((gJ - 1) / g.NW) & 1));
-              wload(gJ - 1 + g.NW);
+            // chunk ago) while this chunk's MMAs stay queued
+            if (!first && nextLoad < totalJ) {
+              wait(&bars.wfree[ps], pph);
+              wload(ps);
+            }
+            first = false;
+            ps = cs;
+            pph = cph;
+            if (++cs == g.NW) {
+              cs = 0;
+              cph ^= 1u;
             }
           }
           tc::mma_commit(&bars.d1full[buf]);
@@ -257,45 +270,50 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   } else if (warp == kConsumers / 32 + 1) {
     // ================= GEMM2 producer =================
     if (lane == 0 && myTiles > 0) {
-      const long long totalK = (long long)myTiles * g.noc;
+      const int totalK = myTiles * g.noc;
       const uint32_t idesc2 = tc::idesc_f32acc(FMT, 128, g.N2);
-      const uint32_t sboK = sbo2;
-      auto kload = [&](long long j) {
-        const int s = (int)(j % g.NK);
+      const uint32_t kbase = tc::smem_addr(smem + L.k);
+      int nextK = 0, kseq = 0;
+      auto kload = [&](int s) {  // chunk kseq -> stage s
         tc::mbar_expect_tx(&bars.kfull[s], L.kStage);
-        tc::bulk_g2s(smem + L.k + (size_t)s * L.kStage, g.kc2 + (size_t)(j % g.noc) * L.kStage, L.kStage,
-                     &bars.kfull[s]);
+        tc::bulk_g2s(smem + L.k + (size_t)s * L.kStage, g.kc2 + (size_t)kseq * L.kStage, L.kStage, &bars.kfull[s]);
+        nextK++;
+        if (++kseq == g.noc) kseq = 0;
       };
-      for (long long j = 0; j < g.NK && j < totalK; j++) kload(j);
-      long long gK = 0;
+      for (int s0 = 0; s0 < g.NK && nextK < totalK; s0++) kload(s0);
+      const uint64_t dAh = tc::smem_desc(tc::smem_addr(A2hi), kLBO, sbo2);
+      const uint64_t dAl = tc::smem_desc(tc::smem_addr(A2lo), kLBO, sbo2);
       const uint32_t dcol = tmem + 256;
+      int ksg = 0;
+      uint32_t kph = 0, aph = 0;
       for (int lt = 0; lt < myTiles; lt++) {
-        for (int oc = 0; oc < g.noc; oc++, gK++) {
+        for (int oc = 0; oc < g.noc; oc++) {
           if (oc == 0 && lt >= 1) wait(&bars.d2free, (lt - 1) & 1);
-          wait(&bars.a2full, (uint32_t)(gK & 1));
-          const int s = (int)(gK % g.NK);
-          wait(&bars.kfull[s], (uint32_t)((gK / g.NK) & 1));
+          wait(&bars.a2full, aph);
+          wait(&bars.kfull[ksg], kph);
           tc::fence_after_sync();
-          const uint32_t ahi = tc::smem_addr(A2hi), alo = tc::smem_addr(A2lo);
-          const uint32_t khi = tc::smem_addr(smem + L.k + (size_t)s * L.kStage), klo = khi + L.kHalf;
+          const uint64_t dKh = tc::smem_desc(kbase + (uint32_t)ksg * L.kStage, kLBO, sbo2);
+          const uint64_t dKl = dKh + (L.kHalf >> 4);
           for (int ks = 0; ks < 2 * ESZ; ks++) {
-            const uint32_t off = (uint32_t)ks * 2 * kLBO;
+            const uint64_t o = (uint64_t)ks * 16;
             const uint32_t acc0 = (oc > 0 || ks > 0) ? 1u : 0u;
-            tc::mma<FMT>(dcol, tc::smem_desc(ahi + off, kLBO, sbo2), tc::smem_desc(khi + off, kLBO, sboK), idesc2,
-                         acc0);
+            tc::mma<FMT>(dcol, dAh + o, dKh + o, idesc2, acc0);
             if constexpr (SPLIT) {
-              tc::mma<FMT>(dcol, tc::smem_desc(ahi + off, kLBO, sbo2), tc::smem_desc(klo + off, kLBO, sboK), idesc2,
-                           1u);
-              tc::mma<FMT>(dcol, tc::smem_desc(alo + off, kLBO, sbo2), tc::smem_desc(khi + off, kLBO, sboK), idesc2,
-                           1u);
+              tc::mma<FMT>(dcol, dAh + o, dKl + o, idesc2, 1u);
+              tc::mma<FMT>(dcol, dAl + o, dKh + o, idesc2, 1u);
             }
           }
           tc::mma_commit(&bars.a2free);
-          tc::mma_commit(&bars.kfree[s]);
+          tc::mma_commit(&bars.kfree[ksg]);
           if (oc == g.noc - 1) tc::mma_commit(&bars.d2full);
-          if (gK + g.NK < totalK) {
-            wait(&bars.kfree[s], (uint32_t)((gK / g.NK) & 1));
-            kload(gK + g.NK);
+          if (nextK < totalK) {
+            wait(&bars.kfree[ksg], kph);
+            kload(ksg);
+          }
+          aph ^= 1u;
+          if (++ksg == g.NK) {
+            ksg = 0;
+            kph ^= 1u;
           }
         }
       }
@@ -304,6 +322,9 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   } else {
     // ================= consumers =================
     const int r = tid & 127, q = tid >> 7;
+    const bool vecPup = (pp & 3) == 0 && ((uintptr_t)a.pup & 15) == 0;
+    const bool vecPhs = (p & 1) == 0 && (a.W & 1) == 0 && (a.phsFrameStride & 1) == 0 && ((uintptr_t)a.phs & 7) == 0;
+    const bool vecOut = (mm & 3) == 0 && (a.bimgFrameStride & 3) == 0 && ((uintptr_t)a.bimg & 15) == 0;
     const uint32_t lanebase = (uint32_t)(32 * (warp & 3)) << 16;
     uint32_t gC = 0, gA = 0;
     // the previous tile's row (its D2 is read after this tile's E is built)
@@ -327,24 +348,55 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         const float* ph = a.phs + (long long)frm * a.phsFrameStride + (long long)sy * p * a.W + sx * p;
         const float* pu = a.pup + (long long)sub * pp;
         for (int g8 = q; g8 * 8 < ppr; g8 += 4) {
-          float er[8], ei[8];
+          float er[8], ei[8], phv[8], puv[8];
+          const int pix0 = g8 * 8;
+          // vector loads where the layout allows: each lane reads its own
+          // subaperture's row, so wide loads cut the memory transactions
+          if (live && vecPup && pix0 + 8 <= pp) {
+            const float4 u0 = *reinterpret_cast<const float4*>(pu + pix0);
+            const float4 u1 = *reinterpret_cast<const float4*>(pu + pix0 + 4);
+            puv[0] = u0.x; puv[1] = u0.y; puv[2] = u0.z; puv[3] = u0.w;
+            puv[4] = u1.x; puv[5] = u1.y; puv[6] = u1.z; puv[7] = u1.w;
+          } else {
+#pragma unroll
+            for (int e = 0; e < 8; e++) puv[e] = (live && pix0 + e < pp) ? pu[pix0 + e] : 0.f;
+          }
+          if (live && vecPhs) {
+#pragma unroll
+            for (int e = 0; e < 8; e += 2) {
+              const int pix = pix0 + e;
+              if (pix < pp) {
+                const int ii = pix / p, jj = pix - ii * p;  // jj even: the pair stays in the row
+                const float2 v2 = *reinterpret_cast<const float2*>(ph + (long long)ii * a.W + jj);
+                phv[e] = v2.x;
+                phv[e + 1] = v2.y;
+              } else {
+                phv[e] = phv[e + 1] = 0.f;
+              }
+            }
+          } else {
+#pragma unroll
+            for (int e = 0; e < 8; e++) {
+              const int pix = pix0 + e;
+              const int ii = pix / p, jj = pix - ii * p;
+              phv[e] = (live && pix < pp) ? ph[(long long)ii * a.W + jj] : 0.f;
+            }
+          }
 #pragma unroll
           for (int e = 0; e < 8; e++) {
-            const int pix = g8 * 8 + e;
+            const int pix = pix0 + e;
             er[e] = 0.f;
             ei[e] = 0.f;
             if (live && pix < pp) {
-              const int ii = pix / p, jj = pix - ii * p;
-              const float t = ph[(long long)ii * a.W + jj] - s_tilt[pix];
+              const float t = phv[e] - s_tilt[pix];
               float sn, cs;
               if constexpr (SPLIT) {
                 sincosf(t, &sn, &cs);
               } else {
                 sincos_reduced(t, &sn, &cs);
               }
-              const float w0 = pu[pix];
-              er[e] = w0 * cs;
-              ei[e] = w0 * sn;
+              er[e] = puv[e] * cs;
+              ei[e] = puv[e] * sn;
             }
           }
           store8<FMT, SPLIT>(A1hi, A1lo, kmaj(r, g8 * 8, ESZ, sboE), er);
@@ -377,23 +429,27 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         float* out = a.bimg + (long long)pFrm * a.bimgFrameStride + (long long)i * mm;
         const float* skyA = a.skyArr ? a.skyArr + (long long)i * mm : nullptr;
         for (int cb = q * 32; cb < mm; cb += 128) {
-          const int c1 = min(mm, cb + 32);
-          for (int q0 = cb; q0 < c1; q0 += 8) {
-            float v[8];
-            tc::tmem_ld8(tmem + 256 + lanebase + q0, v);
-            tc::tmem_ld_wait();
-            if (!pLive) continue;
+          uint32_t v[32];
+          tc::tmem_ld32(tmem + 256 + lanebase + cb, v);
+          tc::tmem_ld_wait();
+          if (!pLive) continue;
+          const int n = min(32, mm - cb);
+          float x[32];
 #pragma unroll
-            for (int e = 0; e < 8; e++) {
-              const int pix = q0 + e;
-              if (pix < c1) {
-                float x = v[e];
-                if (totsig > 0.f || iscale) x *= scale;
-                if (skyv > 0.f) x += skyv;
-                if (skyA) x += skyA[pix];
-                out[pix] = x;
-              }
-            }
+          for (int e = 0; e < 32; e++) {
+            x[e] = __uint_as_float(v[e]);
+            if (totsig > 0.f || iscale) x[e] *= scale;
+            if (skyv > 0.f) x[e] += skyv;
+            if (skyA && e < n) x[e] += skyA[cb + e];
+          }
+          if (vecOut) {  // n is a multiple of 4 here
+#pragma unroll
+            for (int e = 0; e < 32; e += 4)
+              if (e < n) *reinterpret_cast<float4*>(out + cb + e) = make_float4(x[e], x[e + 1], x[e + 2], x[e + 3]);
+          } else {
+#pragma unroll
+            for (int e = 0; e < 32; e++)
+              if (e < n) out[cb + e] = x[e];
           }
         }
         tc::fence_before_sync();
@@ -412,13 +468,15 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         wait(&bars.d1full[buf], (gC >> 1) & 1);
         tc::fence_after_sync();
         float I[16];
-#pragma unroll
-        for (int h = 0; h < 4; h++) {
-          float v[8];
-          tc::tmem_ld8(tmem + buf * 128 + lanebase + q * 32 + h * 8, v);
+        {
+          uint32_t v[32];
+          tc::tmem_ld32(tmem + buf * 128 + lanebase + q * 32, v);
           tc::tmem_ld_wait();
 #pragma unroll
-          for (int e = 0; e < 4; e++) I[h * 4 + e] = (v[2 * e] * v[2 * e] + v[2 * e + 1] * v[2 * e + 1]) * isc;
+          for (int e = 0; e < 16; e++) {
+            const float re = __uint_as_float(v[2 * e]), im = __uint_as_float(v[2 * e + 1]);
+            I[e] = (re * re + im * im) * isc;
+          }
         }
         tc::fence_before_sync();
         __syncwarp();

@@ -40,6 +40,10 @@ __global__ void __launch_bounds__(kPostThreads, 4) wfs_post_kernel(const WfsArgs
   const bool pois = a.addPoisson == 1 && a.calsource == 0;
   const float rn = a.calsource == 0 ? a.readNoise : 0.f;
   const unsigned long long fbase = frame_base(a);
+  // the common configuration (window CoG, no brightest-pixel selection, no
+  // fit) takes a lean path; everything else runs post_tile
+  const bool simple = !(a.calsource == 0 && (a.useBrightest != 0 || a.useBrightestArr)) && a.opticalBinning != 1 &&
+                      a.fitSize == 0 && a.gaussianFit <= 0 && a.cob == 0;
 
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const long long w0 = tile * TS;
@@ -57,7 +61,8 @@ __global__ void __launch_bounds__(kPostThreads, 4) wfs_post_kernel(const WfsArgs
     for (int w = tid; w < ns * mm; w += blockDim.x) {
       const int s = div_small(w, mm, inv_mm), pix = w - s * mm;
       const int i = s_subap[s];
-      float v = a.bimg[(long long)s_frame[s] * a.bimgFrameStride + (long long)i * mm + pix];
+      float* gp = a.bimg + (long long)s_frame[s] * a.bimgFrameStride + (long long)i * mm + pix;
+      float v = *gp;
       if (noise) {
         // one stream per pixel: the read-noise normal takes the first two
         // uniforms, the Poisson sampler continues from the third
@@ -70,10 +75,56 @@ __global__ void __launch_bounds__(kPostThreads, 4) wfs_post_kernel(const WfsArgs
           v += a.readBg;
         v = threshold_px(v, a.floorv, a.threshType);
       }
+      if (simple) {
+        // pixel power and the bimg write of post_tile's stage 8, here
+        if (a.pxlPower == 2.f)
+          v = v * v;
+        else if (a.pxlPower != 1.f && a.pxlPower != 0.f)
+          v = powf(v, a.pxlPower);
+        *gp = v;
+      }
       imgs[s * mm + pix] = v;
     }
     __syncthreads();
-    post_tile(a, ns, s_subap, s_frame, s_cw, [&](int s) { return imgs + s * mm; }, [&](int) { return mm; });
+    if (!simple) {
+      post_tile(a, ns, s_subap, s_frame, s_cw, [&](int s) { return imgs + s * mm; }, [&](int) { return mm; });
+      continue;
+    }
+    if (a.imageOnly != 0) continue;
+    // centred-window CoG (post_tile's stage 9, same summation order): one
+    // warp per subaperture, lanes over the window pixels
+    const int warp = tid >> 5, lane = tid & 31, nwarps = blockDim.x >> 5;
+    const int m = a.m, ncen = a.ncen, sx0 = (m - ncen) / 2, nwin = ncen * ncen;
+    const float inv_nc = 1.0f / (float)ncen;
+    for (int s = warp; s < ns; s += nwarps) {
+      const float* img = imgs + s * mm;
+      const int i = s_subap[s];
+      const float* wt = cw2d ? s_cw : (a.centWeightDim == 4 ? a.centWeight + (long long)i * mm : nullptr);
+      float sum = 0.f, sxv = 0.f, syv = 0.f;
+      for (int k = lane; k < nwin; k += 32) {
+        const int rr = div_small(k, ncen, inv_nc);
+        const int r = sx0 + rr, c = sx0 + (k - rr * ncen);
+        float t = img[r * m + c];
+        if (wt) t *= wt[r * m + c];
+        sum += t;
+        sxv += t * c;
+        syv += t * r;
+      }
+#pragma unroll
+      for (int o = 16; o; o >>= 1) {
+        sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        sxv += __shfl_xor_sync(0xffffffffu, sxv, o);
+        syv += __shfl_xor_sync(0xffffffffu, syv, o);
+      }
+      if (lane == 0) {
+        float cx = 0.f, cy = 0.f;
+        if (sum > 0.f) {
+          cx = sxv / sum - 0.5f * (float)(m - 1);
+          cy = syv / sum - 0.5f * (float)(m - 1);
+        }
+        calibrate_and_store(a, i, s_frame[s], cx, cy);
+      }
+    }
   }
 }
 
