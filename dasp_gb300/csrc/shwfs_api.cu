@@ -1462,7 +1462,7 @@ shwfs_status shwfs_batch_run(shwfs_batch* b, void* stream) {
 
 shwfs_status shwfs_sample_noise(int kind, const float* lam, int64_t n, uint64_t seed, uint64_t frame, float* out,
                                 void* stream) {
-  if (n < 0 || n > (1LL << 32) || !out || (kind == 0 && !lam) || (kind != 0 && kind != 1))
+  if (n < 0 || n > (1LL << 32) || !out || (kind != 1 && !lam) || kind < 0 || kind > 2)
     return fail(SHWFS_ERR_INVALID, "bad noise-sampling arguments");
   cudaStream_t st = (cudaStream_t)stream;
   CK(launch_sample_noise(lam, n, seed, frame, kind, out, st));

@@ -213,6 +213,50 @@ __device__ __forceinline__ float poisson_modal(float u, float lam) {
   return fm;
 }
 
+// Tables for Poisson(lam) with lam < 64 as the sum of two independent parts,
+// Poisson(L) + Poisson(d), L = floor(lam), d = lam - L in [0, 1):
+//   Poisson(L): inversion of one uniform through the CDF of Poisson(L),
+//     tabulated for L = 1..63 (computed in double, rounded to float; each
+//     table runs until the CDF is 1 in float), starting from a 64-entry
+//     guide table (first k whose CDF reaches j/64);
+//   Poisson(d): inversion of a second uniform by sequential search from 0
+//     (at most a few steps for d < 1).
+// The sum of independent Poisson variables is Poisson, so the draw is exact
+// up to float rounding of the tabulated CDF.  ~22 KB, staged into shared
+// memory by the kernels that use it.
+constexpr int kPoisTabL = 64;      // L = 0..63
+constexpr int kPoisGuide = 64;
+constexpr int kPoisCdfMax = 4480;  // >= sum of the table lengths
+struct PoisTab {
+  float cdf[kPoisCdfMax];
+  uint16_t off[kPoisTabL];
+  uint16_t len[kPoisTabL];
+  uint8_t guide[kPoisTabL][kPoisGuide];
+};
+
+__device__ __forceinline__ float poisson_tab(const PoisTab& T, float u3, float u4, float lam) {
+  const int L = (int)lam;
+  const float d = lam - (float)L;  // exact
+  int k = 0;
+  if (L > 0) {
+    const float* C = T.cdf + T.off[L];
+    const int n = T.len[L];
+    k = T.guide[L][(int)(u3 * (float)kPoisGuide)];
+    while (k < n - 1 && u3 > C[k]) k++;
+  }
+  if (d > 0.0f) {
+    float p = __expf(-d), F = p;
+    int k2 = 0;
+    while (u4 > F && k2 < 40) {
+      k2++;
+      p *= __fdividef(d, (float)k2);
+      F += p;
+    }
+    k += k2;
+  }
+  return (float)k;
+}
+
 // Below lambda 64 the modal inversion above (one uniform); above, Hormann's
 // PTRS transformed rejection as in the reference (cmod/src/centmodule.c:
 // 722-758), whose quick-accept region grows with lambda.  Both draw from the
@@ -236,6 +280,21 @@ __device__ __forceinline__ float poisson_counter(CounterStream& st, float lam) {
       return kf;
   }
   return floorf(lam + 0.5f);  // unreachable in practice: bounded loop
+}
+
+// device address of the tables on the current device, built on first use
+// (pois_table.cu)
+cudaError_t pois_table_device(const PoisTab** out);
+
+// As poisson_counter, with the tabulated sampler below lambda 64 (two
+// uniforms from the pixel's stream)
+__device__ __forceinline__ float poisson_counter_tab(CounterStream& st, float lam, const PoisTab& T) {
+  if (!(lam > 0.0f)) return 0.0f;
+  if (lam < kModalMaxLam) {
+    const float u3 = st.uniform(), u4 = st.uniform();
+    return poisson_tab(T, u3, u4, lam);
+  }
+  return poisson_counter(st, lam);
 }
 
 // one standard normal deviate (Box-Muller, cosine branch)

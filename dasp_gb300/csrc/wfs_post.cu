@@ -21,16 +21,23 @@ namespace {
 constexpr int kPostThreads = 256;
 constexpr int kPostMaxTS = 64;
 
-__global__ void __launch_bounds__(kPostThreads, 4) wfs_post_kernel(const WfsArgs a) {
-  extern __shared__ float smem_post[];
+__global__ void __launch_bounds__(kPostThreads, 4) wfs_post_kernel(const WfsArgs a, const PoisTab* __restrict__ tab) {
+  extern __shared__ __align__(16) float smem_post[];
   __shared__ int s_subap[kPostMaxTS];
   __shared__ int s_frame[kPostMaxTS];
   __shared__ unsigned char s_pflag[kPostMaxTS];
   const int tid = threadIdx.x;
   const int mm = a.m * a.m;
   const bool cw2d = a.centWeightDim == 2;
-  float* s_cw = smem_post;
-  float* imgs = smem_post + (cw2d ? mm : 0);
+  const bool useTab = tab != nullptr;
+  PoisTab* s_tab = reinterpret_cast<PoisTab*>(smem_post);
+  float* s_cw = smem_post + (useTab ? sizeof(PoisTab) / sizeof(float) : 0);
+  float* imgs = s_cw + (cw2d ? mm : 0);
+  if (useTab) {
+    const int4* src = reinterpret_cast<const int4*>(tab);
+    int4* dst = reinterpret_cast<int4*>(s_tab);
+    for (int k = tid; k < (int)(sizeof(PoisTab) / sizeof(int4)); k += blockDim.x) dst[k] = src[k];
+  }
   if (cw2d)
     for (int k = tid; k < mm; k += blockDim.x) s_cw[k] = a.centWeight[k];
   const int TS = a.TS;
@@ -68,7 +75,7 @@ __global__ void __launch_bounds__(kPostThreads, 4) wfs_post_kernel(const WfsArgs
         // uniforms, the Poisson sampler continues from the third
         CounterStream st(a.seed, fbase + s_frame[s], i, pix, 0);
         const float g = rn != 0.f ? normal_counter(st) : 0.f;
-        if (pois && s_pflag[s]) v = poisson_counter(st, v);
+        if (pois && s_pflag[s]) v = poisson_counter_tab(st, v, *s_tab);
         if (rn != 0.f)
           v += rn * g + a.readBg;
         else
@@ -136,7 +143,14 @@ cudaError_t launch_post(const WfsArgs& a0, int numSMs, cudaStream_t stream) {
   const long long nwork = (long long)a.nlit * a.nframes;
   if (nwork == 0) return cudaSuccess;
   a.TS = mm > 0 ? (8192 / mm < 1 ? 1 : (8192 / mm > kPostMaxTS ? kPostMaxTS : 8192 / mm)) : 1;
-  const int smem = (a.TS * mm + (a.centWeightDim == 2 ? mm : 0)) * (int)sizeof(float);
+  const bool pois = (a.mode & kNoiseCounter) && a.addPoisson == 1 && a.calsource == 0;
+  const PoisTab* tab = nullptr;
+  if (pois) {
+    cudaError_t et = pois_table_device(&tab);
+    if (et != cudaSuccess) return et;
+  }
+  const int smem = (a.TS * mm + (a.centWeightDim == 2 ? mm : 0)) * (int)sizeof(float) +
+                   (pois ? (int)sizeof(PoisTab) : 0);
   cudaError_t e = cudaFuncSetAttribute(wfs_post_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   int ctas = 0;
@@ -146,7 +160,7 @@ cudaError_t launch_post(const WfsArgs& a0, int numSMs, cudaStream_t stream) {
   const long long ntiles = (nwork + a.TS - 1) / a.TS;
   const long long cap = (long long)numSMs * ctas;
   const int grid = (int)(ntiles < cap ? ntiles : cap);
-  wfs_post_kernel<<<grid, kPostThreads, smem, stream>>>(a);
+  wfs_post_kernel<<<grid, kPostThreads, smem, stream>>>(a, tab);
   return cudaGetLastError();
 }
 

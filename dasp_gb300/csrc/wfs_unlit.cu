@@ -73,18 +73,25 @@ cudaError_t launch_set_counter(unsigned long long* ctr, unsigned long long v, cu
 // standard normal), element i from the stream of (seed, frame, i), as the
 // pipeline draws one pixel's noise
 __global__ void sample_noise_kernel(const float* __restrict__ lam, long long n, unsigned long long seed,
-                                    unsigned long long frame, int kind, float* __restrict__ out) {
+                                    unsigned long long frame, int kind, float* __restrict__ out,
+                                    const PoisTab* __restrict__ tab) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     CounterStream st(seed, frame, (int)(i >> 16), (int)(i & 0xffff), 2);
-    out[i] = kind == 0 ? poisson_counter(st, lam[i]) : normal_counter(st);
+    out[i] = kind == 0 ? poisson_counter(st, lam[i])
+                       : (kind == 2 ? poisson_counter_tab(st, lam[i], *tab) : normal_counter(st));
   }
 }
 
 cudaError_t launch_sample_noise(const float* lam, long long n, unsigned long long seed, unsigned long long frame,
                                 int kind, float* out, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
+  const PoisTab* tab = nullptr;
+  if (kind == 2) {
+    cudaError_t e = pois_table_device(&tab);
+    if (e != cudaSuccess) return e;
+  }
   const long long blocks = (n + 255) / 256 < 152 * 16 ? (n + 255) / 256 : 152 * 16;
-  sample_noise_kernel<<<(int)blocks, 256, 0, stream>>>(lam, n, seed, frame, kind, out);
+  sample_noise_kernel<<<(int)blocks, 256, 0, stream>>>(lam, n, seed, frame, kind, out, tab);
   return cudaGetLastError();
 }
 

@@ -45,20 +45,25 @@ def _chi2_poisson(x, lam):
     return stats.chi2.sf(chi2, len(obs) - 1)
 
 
-@pytest.mark.parametrize("lam", [0.05, 0.7, 1.0, 2.5, 3.99, 4.0, 9.7, 17.3, 29.9, 30.5, 63.9, 64.0, 150.0, 1000.0])
-def test_poisson_chi_square(lam):
-    x = _draw(0, lam, 1 << 21)
+@pytest.mark.parametrize("kind", [0, 2])
+@pytest.mark.parametrize("lam", [0.05, 0.7, 1.0, 2.5, 3.99, 4.0, 9.7, 10.0, 17.3, 29.9, 30.5, 63.9, 64.0, 150.0, 1000.0])
+def test_poisson_chi_square(lam, kind):
+    """kind 0: the fused FP32 kernel's sampler (modal inversion / PTRS);
+    kind 2: the tensor-core forms' tabulated sampler (CDF table of
+    Poisson(floor lam) + inversion of the fractional remainder / PTRS)."""
+    x = _draw(kind, lam, 1 << 21)
     p = _chi2_poisson(x, lam)
     assert p > 1e-6, "chi-square p-value %g at lambda %g" % (p, lam)
     assert abs(x.mean() - lam) < 6 * np.sqrt(lam / x.size)
 
 
-def test_poisson_zero_and_negative_mean():
+@pytest.mark.parametrize("kind", [0, 2])
+def test_poisson_zero_and_negative_mean(kind):
     from dasp_gb300 import _lib
-    lam = torch.tensor([0.0, -1.0, 0.0], device="cuda")
-    out = torch.full((3,), 7.0, device="cuda")
-    _lib.check(_lib.lib().shwfs_sample_noise(0, lam.data_ptr(), 3, 1, 0, out.data_ptr(), None), "sample_noise")
-    assert out.cpu().tolist() == [0.0, 0.0, 0.0]
+    lam = torch.tensor([0.0, -1.0, 0.0, float("nan")], device="cuda")
+    out = torch.full((4,), 7.0, device="cuda")
+    _lib.check(_lib.lib().shwfs_sample_noise(kind, lam.data_ptr(), 4, 1, 0, out.data_ptr(), None), "sample_noise")
+    assert out.cpu().tolist() == [0.0, 0.0, 0.0, 0.0]
 
 
 def test_normal_moments_and_shape():
