@@ -32,6 +32,7 @@ struct GemmGeom {
   int noc;     // output chunks of 64 complex outputs (GEMM1 N = 128 columns each)
   int N2;      // GEMM2 N: nimg^2 rounded up to 16
   int NW, NK;  // ring stages for W2 and Kc chunks
+  int dbE;     // 1: two field (GEMM1 A operand) buffers, the next tile's built during this one
   const uint8_t* w2;   // [noc][nkc] x {hi[, lo]} x [128 x KCB bytes], tensor-core smem order
   const uint8_t* kc2;  // [noc] x {hi[, lo]} x [N2 x 64 elements], tensor-core smem order
 };
@@ -52,7 +53,7 @@ __host__ __device__ inline GemmSmem gemm_smem_layout(const GemmGeom& g) {
   L.kHalf = (uint32_t)g.N2 * 64u * esz;
   L.kStage = L.kHalf * hl;
   L.a1 = 0;
-  L.a2 = (L.a1 + L.a1Half * hl + 1023u) & ~1023u;
+  L.a2 = (L.a1 + L.a1Half * hl * (g.dbE ? 2u : 1u) + 1023u) & ~1023u;
   L.w = (L.a2 + L.a2Half * hl + 1023u) & ~1023u;
   L.k = (L.w + (uint32_t)g.NW * L.wStage + 1023u) & ~1023u;
   L.total = L.k + (uint32_t)g.NK * L.kStage;

@@ -217,8 +217,10 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       for (int s0 = 0; s0 < g.NW && nextLoad < totalJ; s0++) wload(s0);
       // descriptors: the 14-bit start-address field (bits 0-13, in 16-byte
       // units) advances by 16 per k-step of 256 bytes; all addresses < 256 KB
-      const uint64_t dEh = tc::smem_desc(tc::smem_addr(A1hi), kLBO, sboE);
-      const uint64_t dEl = tc::smem_desc(tc::smem_addr(A1lo), kLBO, sboE);
+      // field buffer of tile lt: (lt & 1) when double buffered
+      const uint64_t dEh0 = tc::smem_desc(tc::smem_addr(A1hi), kLBO, sboE);
+      const uint64_t dEl0 = tc::smem_desc(tc::smem_addr(A1lo), kLBO, sboE);
+      const uint64_t dEstep = (uint64_t)((L.a1Half * (SPLIT ? 2u : 1u)) >> 4);
       int cs = 0, ps = 0;
       uint32_t cph = 0, pph = 0;
       bool first = true;
@@ -226,6 +228,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       for (int lt = 0; lt < myTiles; lt++) {
         wait(&bars.efull, lt & 1);
         tc::fence_after_sync();
+        const uint64_t dEh = dEh0 + ((g.dbE && (lt & 1)) ? dEstep : 0);
+        const uint64_t dEl = dEl0 + ((g.dbE && (lt & 1)) ? dEstep : 0);
         for (int oc = 0; oc < g.noc; oc++, gC++) {
           const uint32_t buf = gC & 1;
           if (gC >= 2) wait(&bars.d1free[buf], ((gC >> 1) - 1) & 1);
@@ -234,7 +238,6 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
           int ks = 0;
           for (int kc = 0; kc < g.nkc; kc++) {
             wait(&bars.wfull[cs], cph);
-            tc::fence_after_sync();
             const uint64_t dWh = tc::smem_desc(wbase + (uint32_t)cs * L.wStage, kLBO, sboW);
             const uint64_t dWl = dWh + (L.wHalf >> 4);
             const int ks1 = min(K1B, (kc + 1) * g.KCB) >> 5;
@@ -326,173 +329,234 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     const bool vecPhs = (p & 1) == 0 && (a.W & 1) == 0 && (a.phsFrameStride & 1) == 0 && ((uintptr_t)a.phs & 7) == 0;
     const bool vecOut = (mm & 3) == 0 && (a.bimgFrameStride & 3) == 0 && ((uintptr_t)a.bimg & 15) == 0;
     const uint32_t lanebase = (uint32_t)(32 * (warp & 3)) << 16;
+    const int ngroups = (ppr / 8 + 3) / 4;  // pixel groups of 8 per thread (at most)
     uint32_t gC = 0, gA = 0;
-    // the previous tile's row (its D2 is read after this tile's E is built)
-    bool pLive = false;
-    int pSub = 0, pFrm = 0;
-    for (int lt = 0; lt <= myTiles; lt++) {
-      const long long tile = blockIdx.x + (long long)lt * gridDim.x;
-      bool live = false;
-      int sub = 0, frm = 0;
-      if (lt < myTiles) {
-        const long long w = tile * kTileSubaps + r;
-        live = w < nwork;
-        if (live) {
-          frm = (int)(w / a.nlit);
-          sub = a.lit[w % a.nlit];
+
+    struct Row {
+      bool live;
+      int sub, frm;
+    };
+    // this thread's row (subaperture-frame) of tile lt
+    auto row_of = [&](int lt) {
+      Row o{false, 0, 0};
+      const long long w = (blockIdx.x + (long long)lt * gridDim.x) * kTileSubaps + r;
+      if (lt < myTiles && w < nwork) {
+        o.live = true;
+        o.frm = (int)(w / a.nlit);
+        o.sub = a.lit[w % a.nlit];
+      }
+      return o;
+    };
+
+    // E = pup*exp(i(phs - tilt)) of this row, pixel groups i0 <= i < i1 of
+    // this thread (group g8 = q + 4i covers pixels 8*g8 .. +7), Re at
+    // K = pix, Im at K = ppr + pix, into field buffer eb
+    auto build_E = [&](int eb, const Row& R, int i0, int i1) {
+      uint8_t* Ehi = A1hi + (size_t)eb * L.a1Half * (SPLIT ? 2 : 1);
+      uint8_t* Elo = Ehi + L.a1Half;
+      const int sy = R.sub / a.nsubx, sx = R.sub - sy * a.nsubx;
+      const float* ph = a.phs + (long long)R.frm * a.phsFrameStride + (long long)sy * p * a.W + sx * p;
+      const float* pu = a.pup + (long long)R.sub * pp;
+      for (int i = i0; i < i1; i++) {
+        const int g8 = q + 4 * i;
+        if (g8 * 8 >= ppr) break;
+        float er[8], ei[8], phv[8], puv[8];
+        const int pix0 = g8 * 8;
+        // vector loads where the layout allows: each lane reads its own
+        // subaperture's row, so wide loads cut the memory transactions
+        if (R.live && vecPup && pix0 + 8 <= pp) {
+          const float4 u0 = *reinterpret_cast<const float4*>(pu + pix0);
+          const float4 u1 = *reinterpret_cast<const float4*>(pu + pix0 + 4);
+          puv[0] = u0.x; puv[1] = u0.y; puv[2] = u0.z; puv[3] = u0.w;
+          puv[4] = u1.x; puv[5] = u1.y; puv[6] = u1.z; puv[7] = u1.w;
+        } else {
+#pragma unroll
+          for (int e = 0; e < 8; e++) puv[e] = (R.live && pix0 + e < pp) ? pu[pix0 + e] : 0.f;
         }
-        // ---- E = pup*exp(i(phs - tilt)) for this row: groups of 8 pixels,
-        // Re at K = pix, Im at K = ppr + pix ----
-        if (lt >= 1) wait(&bars.efree, (lt - 1) & 1);
-        const int sy = sub / a.nsubx, sx = sub - sy * a.nsubx;
-        const float* ph = a.phs + (long long)frm * a.phsFrameStride + (long long)sy * p * a.W + sx * p;
-        const float* pu = a.pup + (long long)sub * pp;
-        for (int g8 = q; g8 * 8 < ppr; g8 += 4) {
-          float er[8], ei[8], phv[8], puv[8];
-          const int pix0 = g8 * 8;
-          // vector loads where the layout allows: each lane reads its own
-          // subaperture's row, so wide loads cut the memory transactions
-          if (live && vecPup && pix0 + 8 <= pp) {
-            const float4 u0 = *reinterpret_cast<const float4*>(pu + pix0);
-            const float4 u1 = *reinterpret_cast<const float4*>(pu + pix0 + 4);
-            puv[0] = u0.x; puv[1] = u0.y; puv[2] = u0.z; puv[3] = u0.w;
-            puv[4] = u1.x; puv[5] = u1.y; puv[6] = u1.z; puv[7] = u1.w;
-          } else {
+        if (R.live && vecPhs) {
 #pragma unroll
-            for (int e = 0; e < 8; e++) puv[e] = (live && pix0 + e < pp) ? pu[pix0 + e] : 0.f;
-          }
-          if (live && vecPhs) {
-#pragma unroll
-            for (int e = 0; e < 8; e += 2) {
-              const int pix = pix0 + e;
-              if (pix < pp) {
-                const int ii = pix / p, jj = pix - ii * p;  // jj even: the pair stays in the row
-                const float2 v2 = *reinterpret_cast<const float2*>(ph + (long long)ii * a.W + jj);
-                phv[e] = v2.x;
-                phv[e + 1] = v2.y;
-              } else {
-                phv[e] = phv[e + 1] = 0.f;
-              }
-            }
-          } else {
-#pragma unroll
-            for (int e = 0; e < 8; e++) {
-              const int pix = pix0 + e;
-              const int ii = pix / p, jj = pix - ii * p;
-              phv[e] = (live && pix < pp) ? ph[(long long)ii * a.W + jj] : 0.f;
+          for (int e = 0; e < 8; e += 2) {
+            const int pix = pix0 + e;
+            if (pix < pp) {
+              const int ii = pix / p, jj = pix - ii * p;  // jj even: the pair stays in the row
+              const float2 v2 = *reinterpret_cast<const float2*>(ph + (long long)ii * a.W + jj);
+              phv[e] = v2.x;
+              phv[e + 1] = v2.y;
+            } else {
+              phv[e] = phv[e + 1] = 0.f;
             }
           }
+        } else {
 #pragma unroll
           for (int e = 0; e < 8; e++) {
             const int pix = pix0 + e;
-            er[e] = 0.f;
-            ei[e] = 0.f;
-            if (live && pix < pp) {
-              const float t = phv[e] - s_tilt[pix];
-              float sn, cs;
-              if constexpr (SPLIT) {
-                sincosf(t, &sn, &cs);
-              } else {
-                sincos_reduced(t, &sn, &cs);
-              }
-              er[e] = puv[e] * cs;
-              ei[e] = puv[e] * sn;
+            const int ii = pix / p, jj = pix - ii * p;
+            phv[e] = (R.live && pix < pp) ? ph[(long long)ii * a.W + jj] : 0.f;
+          }
+        }
+#pragma unroll
+        for (int e = 0; e < 8; e++) {
+          const int pix = pix0 + e;
+          er[e] = 0.f;
+          ei[e] = 0.f;
+          if (R.live && pix < pp) {
+            const float t = phv[e] - s_tilt[pix];
+            float sn, cs;
+            if constexpr (SPLIT) {
+              sincosf(t, &sn, &cs);
+            } else {
+              sincos_reduced(t, &sn, &cs);
             }
-          }
-          store8<FMT, SPLIT>(A1hi, A1lo, kmaj(r, g8 * 8, ESZ, sboE), er);
-          store8<FMT, SPLIT>(A1hi, A1lo, kmaj(r, ppr + g8 * 8, ESZ, sboE), ei);
-        }
-        // zero K padding beyond 2*ppr (none when 2*ppr is a multiple of 16)
-        for (int k = 2 * ppr + q; k < g.K1; k += 4) {
-          const uint32_t off = kmaj(r, k, ESZ, sboE);
-          if constexpr (ESZ == 4) {
-            *reinterpret_cast<uint32_t*>(A1hi + off) = 0u;
-          } else {
-            *reinterpret_cast<uint16_t*>(A1hi + off) = 0;
-            if constexpr (SPLIT) *reinterpret_cast<uint16_t*>(A1lo + off) = 0;
+            er[e] = puv[e] * cs;
+            ei[e] = puv[e] * sn;
           }
         }
-        tc::fence_async_smem();
-        __syncwarp();
-        if (lane == 0) tc::mbar_arrive(&bars.efull);
+        store8<FMT, SPLIT>(Ehi, Elo, kmaj(r, pix0, ESZ, sboE), er);
+        store8<FMT, SPLIT>(Ehi, Elo, kmaj(r, ppr + pix0, ESZ, sboE), ei);
       }
-      // ---- previous tile: binned image from D2, normalise, sky -> bimg ----
-      if (lt >= 1) {
-        wait(&bars.d2full, (lt - 1) & 1);
-        tc::fence_after_sync();
-        const int i = pSub;
-        const float totsig = a.totsig[i];
-        const float fr = a.frac[i];
-        float scale = totsig > 0.f ? (a.sigArr ? a.sigArr[i] / totsig : a.sig * fr / totsig) : 1.f;
-        if (iscale) scale = scale / iscale[i];  // undo the fp16 range scaling
-        const float skyv = a.sky * fr;
-        float* out = a.bimg + (long long)pFrm * a.bimgFrameStride + (long long)i * mm;
-        const float* skyA = a.skyArr ? a.skyArr + (long long)i * mm : nullptr;
-        for (int cb = q * 32; cb < mm; cb += 128) {
-          uint32_t v[32];
-          tc::tmem_ld32(tmem + 256 + lanebase + cb, v);
-          tc::tmem_ld_wait();
-          if (!pLive) continue;
-          const int n = min(32, mm - cb);
-          float x[32];
-#pragma unroll
-          for (int e = 0; e < 32; e++) {
-            x[e] = __uint_as_float(v[e]);
-            if (totsig > 0.f || iscale) x[e] *= scale;
-            if (skyv > 0.f) x[e] += skyv;
-            if (skyA && e < n) x[e] += skyA[cb + e];
-          }
-          if (vecOut) {  // n is a multiple of 4 here
-#pragma unroll
-            for (int e = 0; e < 32; e += 4)
-              if (e < n) *reinterpret_cast<float4*>(out + cb + e) = make_float4(x[e], x[e + 1], x[e + 2], x[e + 3]);
-          } else {
-#pragma unroll
-            for (int e = 0; e < 32; e++)
-              if (e < n) out[cb + e] = x[e];
-          }
+    };
+    // zero K padding beyond 2*ppr (none when 2*ppr is a multiple of 16)
+    auto pad_E = [&](int eb) {
+      uint8_t* Ehi = A1hi + (size_t)eb * L.a1Half * (SPLIT ? 2 : 1);
+      uint8_t* Elo = Ehi + L.a1Half;
+      for (int k = 2 * ppr + q; k < g.K1; k += 4) {
+        const uint32_t off = kmaj(r, k, ESZ, sboE);
+        if constexpr (ESZ == 4) {
+          *reinterpret_cast<uint32_t*>(Ehi + off) = 0u;
+        } else {
+          *reinterpret_cast<uint16_t*>(Ehi + off) = 0;
+          if constexpr (SPLIT) *reinterpret_cast<uint16_t*>(Elo + off) = 0;
         }
-        tc::fence_before_sync();
-        __syncwarp();
-        if (lane == 0) tc::mbar_arrive(&bars.d2free);
       }
-      if (lt == myTiles) break;
-      pLive = live;
-      pSub = sub;
-      pFrm = frm;
-      const float isc = (iscale && live) ? iscale[sub] : 1.f;
-      // ---- output chunks: |F|^2 of 64 complex outputs; this thread reads
-      // columns 32q .. 32q+31 (16 outputs) of its row ----
-      for (int oc = 0; oc < g.noc; oc++, gC++, gA++) {
-        const uint32_t buf = gC & 1;
-        wait(&bars.d1full[buf], (gC >> 1) & 1);
-        tc::fence_after_sync();
-        float I[16];
-        {
-          uint32_t v[32];
-          tc::tmem_ld32(tmem + buf * 128 + lanebase + q * 32, v);
-          tc::tmem_ld_wait();
+    };
+    auto e_done = [&]() {
+      tc::fence_async_smem();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&bars.efull);
+    };
+
+    // binned image of tile lt (row P) from D2: normalise, sky -> bimg
+    auto read_D2 = [&](int lt, const Row& P) {
+      wait(&bars.d2full, lt & 1);
+      tc::fence_after_sync();
+      const int i = P.sub;
+      const float totsig = a.totsig[i];
+      const float fr = a.frac[i];
+      float scale = totsig > 0.f ? (a.sigArr ? a.sigArr[i] / totsig : a.sig * fr / totsig) : 1.f;
+      if (iscale) scale = scale / iscale[i];  // undo the fp16 range scaling
+      const float skyv = a.sky * fr;
+      float* out = a.bimg + (long long)P.frm * a.bimgFrameStride + (long long)i * mm;
+      const float* skyA = a.skyArr ? a.skyArr + (long long)i * mm : nullptr;
+      for (int cb = q * 32; cb < mm; cb += 128) {
+        uint32_t v[32];
+        tc::tmem_ld32(tmem + 256 + lanebase + cb, v);
+        tc::tmem_ld_wait();
+        if (!P.live) continue;
+        const int n = min(32, mm - cb);
+        float x[32];
 #pragma unroll
-          for (int e = 0; e < 16; e++) {
-            const float re = __uint_as_float(v[2 * e]), im = __uint_as_float(v[2 * e + 1]);
-            I[e] = (re * re + im * im) * isc;
+        for (int e = 0; e < 32; e++) {
+          x[e] = __uint_as_float(v[e]);
+          if (totsig > 0.f || iscale) x[e] *= scale;
+          if (skyv > 0.f) x[e] += skyv;
+          if (skyA && e < n) x[e] += skyA[cb + e];
+        }
+        if (vecOut) {  // n is a multiple of 4 here
+#pragma unroll
+          for (int e = 0; e < 32; e += 4)
+            if (e < n) *reinterpret_cast<float4*>(out + cb + e) = make_float4(x[e], x[e + 1], x[e + 2], x[e + 3]);
+        } else {
+#pragma unroll
+          for (int e = 0; e < 32; e++)
+            if (e < n) out[cb + e] = x[e];
+        }
+      }
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&bars.d2free);
+    };
+
+    // one output chunk of the current tile: |F|^2 of the 16 complex outputs
+    // in columns 32q .. 32q+31 of this row -> the GEMM2 operand
+    auto chunk = [&](float isc) {
+      const uint32_t buf = gC & 1;
+      wait(&bars.d1full[buf], (gC >> 1) & 1);
+      tc::fence_after_sync();
+      float I[16];
+      {
+        uint32_t v[32];
+        tc::tmem_ld32(tmem + buf * 128 + lanebase + q * 32, v);
+        tc::tmem_ld_wait();
+#pragma unroll
+        for (int e = 0; e < 16; e++) {
+          const float re = __uint_as_float(v[2 * e]), im = __uint_as_float(v[2 * e + 1]);
+          I[e] = (re * re + im * im) * isc;
+        }
+      }
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&bars.d1free[buf]);
+      // A2 is free once the previous chunk's GEMM2 has completed
+      if (gA >= 1) wait(&bars.a2free, (gA - 1) & 1);
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        float x8[8];
+#pragma unroll
+        for (int e = 0; e < 8; e++) x8[e] = I[h * 8 + e];
+        store8<FMT, SPLIT>(A2hi, A2lo, kmaj(r, q * 16 + h * 8, ESZ, sbo2), x8);
+      }
+      tc::fence_async_smem();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&bars.a2full);
+      gC++;
+      gA++;
+    };
+
+    if (myTiles > 0) {
+      if (!g.dbE) {
+        // one field buffer: tile lt's field is built once GEMM1 of tile
+        // lt-1 has finished with the buffer
+        Row prev{false, 0, 0};
+        for (int lt = 0; lt <= myTiles; lt++) {
+          const Row cur = row_of(lt);
+          if (lt < myTiles) {
+            if (lt >= 1) wait(&bars.efree, (lt - 1) & 1);
+            build_E(0, cur, 0, ngroups);
+            pad_E(0);
+            e_done();
           }
+          if (lt >= 1) read_D2(lt - 1, prev);
+          if (lt == myTiles) break;
+          const float isc = (iscale && cur.live) ? iscale[cur.sub] : 1.f;
+          for (int oc = 0; oc < g.noc; oc++) chunk(isc);
+          prev = cur;
         }
-        tc::fence_before_sync();
-        __syncwarp();
-        if (lane == 0) tc::mbar_arrive(&bars.d1free[buf]);
-        // A2 is free once the previous chunk's GEMM2 has completed
-        if (gA >= 1) wait(&bars.a2free, (gA - 1) & 1);
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-          float x8[8];
-#pragma unroll
-          for (int e = 0; e < 8; e++) x8[e] = I[h * 8 + e];
-          store8<FMT, SPLIT>(A2hi, A2lo, kmaj(r, q * 16 + h * 8, ESZ, sbo2), x8);
+      } else {
+        // two field buffers: the next tile's field is built in slices
+        // between this tile's output chunks, overlapping GEMM1
+        Row cur = row_of(0);
+        build_E(0, cur, 0, ngroups);
+        pad_E(0);
+        pad_E(1);
+        e_done();
+        Row prev{false, 0, 0};
+        for (int lt = 0; lt < myTiles; lt++) {
+          const Row next = row_of(lt + 1);
+          const bool more = lt + 1 < myTiles;
+          const float isc = (iscale && cur.live) ? iscale[cur.sub] : 1.f;
+          for (int oc = 0; oc < g.noc; oc++) {
+            if (more) {
+              if (oc == 0 && lt >= 1) wait(&bars.efree, (lt - 1) & 1);
+              build_E((lt + 1) & 1, next, (oc * ngroups) / g.noc, ((oc + 1) * ngroups) / g.noc);
+              if (oc == g.noc - 1) e_done();
+            }
+            if (oc == 0 && lt >= 1) read_D2(lt - 1, prev);
+            chunk(isc);
+          }
+          prev = cur;
+          cur = next;
         }
-        tc::fence_async_smem();
-        __syncwarp();
-        if (lane == 0) tc::mbar_arrive(&bars.a2full);
+        read_D2(myTiles - 1, prev);
       }
     }
   }
@@ -587,24 +651,30 @@ bool gemm_geometry(const GemmSpec& sp, int fmt, int passes, GemmGeom* g) {
   g->K1 = K1;
   g->N2 = N2;
   g->noc = (sp.c * sp.c + 63) / 64;
-  g->KCB = 64;  // bytes of K per row in one streamed W2 chunk (two k-steps)
+  // bytes of K per row in one streamed W2 chunk: four k-steps for one-pass
+  // formats, two for the split form (whose stages carry hi and lo)
+  g->KCB = passes == 1 ? 128 : 64;
   g->nkc = (K1 * esz + g->KCB - 1) / g->KCB;
   // dynamic limit: 227 KB minus the kernel's static shared memory (< 2 KB)
   const uint32_t limit = 227 * 1024 - 4096;
-  for (int nk = 2; nk >= 1; nk--) {
-    GemmGeom t = *g;
-    t.NK = nk;
-    t.NW = 0;
-    const GemmSmem base = gemm_smem_layout(t);
-    if (base.total > limit) continue;
-    const uint32_t wst = gemm_smem_layout(t).wStage;
-    int nw = (int)((limit - base.total) / wst);
-    if (nw > kGemmMaxNW) nw = kGemmMaxNW;
-    // prefer two Kc stages only when the W2 ring keeps at least 4 stages
-    if (nw < (nk == 2 ? 4 : 2)) continue;
-    g->NK = nk;
-    g->NW = nw;
-    return true;
+  // prefer two field buffers (one-pass 16-bit formats), then two Kc stages,
+  // as long as the W2 ring keeps enough stages
+  for (int db = (passes == 1 && esz == 2) ? 1 : 0; db >= 0; db--) {
+    for (int nk = 2; nk >= 1; nk--) {
+      GemmGeom t = *g;
+      t.dbE = db;
+      t.NK = nk;
+      t.NW = 0;
+      const GemmSmem base = gemm_smem_layout(t);
+      if (base.total > limit) continue;
+      int nw = (int)((limit - base.total) / base.wStage);
+      if (nw > kGemmMaxNW) nw = kGemmMaxNW;
+      if (nw < (nk == 2 ? 4 : (db ? 3 : 2))) continue;
+      g->dbE = db;
+      g->NK = nk;
+      g->NW = nw;
+      return true;
+    }
   }
   return false;
 }
