@@ -279,6 +279,101 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- serving workload
+
+def serving_systems(nsys=64, seed=5):
+    """64 simulated AO systems: subaperture counts from {8,16,32,40,74,84}^2,
+    fftsize 16-32 (phasesize N/2, nimg N/2), half NGS (Gaussian spot), half
+    LGS (per-subaperture elongated spots), nintegrations 1-4, Poisson
+    request rates 500-2000 Hz."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(nsys):
+        nsubx = int(rng.choice([8, 16, 32, 40, 74, 84]))
+        N = int(rng.choice([16, 20, 24, 32]))
+        out.append(dict(nsubx=nsubx, N=N, p=N // 2, m=N // 2, lgs=bool(rng.random() < 0.5),
+                        nint=int(rng.integers(1, 5)), rate=float(rng.uniform(500.0, 2000.0)),
+                        sig=float(rng.uniform(300.0, 2000.0)), rn=float(rng.uniform(1.0, 3.0)), seed=1000 + k))
+    return out
+
+
+def serving_kwargs(sysd, screens_cache):
+    """centcmod arguments and device phase frames of one serving system."""
+    import torch
+    from dasp_gb300.screens import gaussian_psf, lgs_psfs, von_karman_screen
+    from dasp_gb300.tel import Pupil
+    nsubx, p, N, m = sysd["nsubx"], sysd["p"], sysd["N"], sysd["m"]
+    npup = nsubx * p
+    pup = Pupil(npup, npup / 2.0, npup / 2.0 * 0.2)
+    if sysd["lgs"]:
+        frac = pup.getSubarea(nsubx) / (p * p)
+        psf = lgs_psfs(nsubx, N, 1.2, 6.0, subap_area=frac)
+    else:
+        psf = gaussian_psf(N, 1.5)
+    if npup not in screens_cache:
+        screens_cache[npup] = von_karman_screen(npup, nsubx * 0.5, 0.15, 30.0, 77 + npup, 640.0)
+    base = screens_cache[npup]
+    frames = [torch.from_numpy(np.ascontiguousarray(np.roll(base, (31 * j + sysd["seed"]) % npup, axis=j % 2)))
+              .cuda() for j in range(2)]
+    kw = dict(nthreads=8, nsubx=nsubx, ncen=m, fftsize=N, clipsize=N, nimg=m, phasesize=p, readnoise=sysd["rn"],
+              readbg=0.0, addPoisson=1, noiseFloor=2 * sysd["rn"], sig=sysd["sig"], skybrightness=5.0, calsource=0,
+              pxlPower=1.0, nintegrations=sysd["nint"], nlatency=0, seed=sysd["seed"], phs=base, pup=pup,
+              spotpsf=psf, cents=np.zeros(nsubx * nsubx * 2, np.float32),
+              bimg=np.zeros((nsubx * nsubx, m, m), np.float32), minarea=0.5, opticalBinning=0, centWeight=None,
+              correlationCentroiding=0, corrThresh=0.0, corrPattern=None, corrimg=None, threshType=0, imageOnly=0,
+              useBrightest=0, preBinningFactor=1, parabolicFit=0, gaussianFitVals=None)
+    return kw, frames
+
+
+def run_serving(args):
+    """Serving loop on device-resident state: 64 systems, Poisson arrivals,
+    HBM-budget admission; p50/p99 frame latency and subap-frames/s for the
+    tensor-core (fp16) and FP32 forms."""
+    import torch
+    from dasp_gb300.serving import WfsServer, poisson_schedule, run_schedule
+    torch.cuda.set_device(0)
+    systems = serving_systems()
+    cache = {}
+    prepared = [serving_kwargs(sd, cache) for sd in systems]
+    duration = float(args.serve_seconds)
+    sched = poisson_schedule([sd["rate"] for sd in systems], duration, seed=11)
+    budget = 120 << 30
+    res = {}
+    with ClockSampler(0) as clk:
+        for form in ("fp16", "fp32"):
+            srv = WfsServer(budget, max_inflight=args.serve_inflight)
+            ids = [srv.add_system(form=form, **kw) for kw, _ in prepared]
+            t_end = time.time() + 120
+            while srv.stats()["admitted"] < len(ids) and time.time() < t_end:
+                time.sleep(0.05)
+            # warm-up: one frame per system
+            for i, (_, fr) in zip(ids, prepared):
+                srv.submit(i, fr[0])
+            srv.drain(120)
+            r = run_schedule(srv, ids, [fr for _, fr in prepared], sched)
+            st = srv.stats()
+            r["hbm_used_gb"] = st["used_bytes"] / 1e9
+            res[form] = r
+            srv.close()
+    head = res["fp16"]
+    lit = {}
+    line = {
+        "metric": "serving: p99 WFS-frame latency, 64 simulated AO systems (Poisson arrivals 500-2000 Hz)",
+        "value": head["latency_ms"]["p99"], "unit": "ms", "n_gpus": 1, "steps": len(sched), "warmup": len(systems),
+        "ms_per_step": head["latency_ms"]["mean"], "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp16 (GEMM-DFT; LGS systems with per-subaperture PSFs run FP32)",
+        "data": "synthetic: seeded von Karman screens, Gaussian NGS and elongated LGS spots",
+        "config": {"workload": "serving_64_systems", "systems": len(systems), "duration_s": duration,
+                   "requests": len(sched), "hbm_budget_gb": budget / 2 ** 30, "max_inflight": args.serve_inflight,
+                   "nsubx_choices": [8, 16, 32, 40, 74, 84], "fftsize_choices": [16, 20, 24, 32],
+                   "lgs_systems": sum(sd["lgs"] for sd in systems),
+                   "offered_subap_frames_per_s": sum(sd["rate"] / sd["nint"] * sd["nsubx"] ** 2 * 0.75
+                                                     for sd in systems)},
+        "forms": res, "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------------- our arm
 
 def main():
@@ -290,8 +385,18 @@ def main():
     ap.add_argument("--frames", type=int, default=FPSTEP, help="frames per step")
     ap.add_argument("--e2e-frames", type=int, default=400)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="ngs74", choices=["ngs74", "serving"],
+                    help="ngs74: the headline 74x74 NGS sensor; serving: 64 AO systems through the serving loop")
+    ap.add_argument("--serve-seconds", type=float, default=1.0)
+    ap.add_argument("--serve-inflight", type=int, default=16)
     args = ap.parse_args()
     ws, rank, local = dist_env()
+    if args.workload == "serving" and args.impl == "ours":
+        if rank == 0:
+            from dasp_gb300 import build
+            build.build()
+            run_serving(args)
+        return
 
     if args.impl == "reference":
         if ws > 1:

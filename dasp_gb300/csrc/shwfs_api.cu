@@ -153,6 +153,7 @@ struct shwfs_handle {
   DevBuf<uint8_t> d_w2, d_kc2;
   DevBuf<float> d_iscale;  // fp16 form: 1 / (sum of the subaperture's pupil)^2
   cudaEvent_t splitEvent = nullptr;  // recorded between image formation and post stages
+  const PoisTab* poisTab = nullptr;  // Poisson CDF tables on this device
   std::vector<float> psfHost, binTHost, binNHost;
   std::vector<int> binIdxHost;
   // CUDA-graph batches: bumped whenever a launch captured from this handle
@@ -551,6 +552,7 @@ WfsArgs make_args(shwfs_handle* h, const float* phs, float* cents, float* bimg, 
   a.seed = h->seed;
   a.frame0 = h->framesRead;
   a.frameCtr = h->graphCtr;
+  a.poisTab = h->poisTab;
   a.mode = mode;
   return a;
 }
@@ -995,6 +997,7 @@ shwfs_status shwfs_initialise(const shwfs_init* in, shwfs_handle** out) {
   CK(h->d_pup.upload(h->pup.data(), h->pup.size()));
   CK(h->d_frac.upload(h->frac.data(), nsa));
   CK(h->d_poisFlag.alloc(nsa));
+  CK(pois_table_device(&h->poisTab));
   CK(h->d_status.alloc(1));
   CK(cudaMemset(h->d_status.p, 0, sizeof(int)));
 

@@ -71,6 +71,8 @@ struct WfsArgs {
   // when set (CUDA-graph replays), the noise frame index is read from this
   // device counter instead of frame0
   const unsigned long long* frameCtr;
+  // CDF tables of the tabulated Poisson sampler (device global memory)
+  const struct PoisTab* poisTab;
   int mode;
 };
 

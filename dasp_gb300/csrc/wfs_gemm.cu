@@ -200,17 +200,22 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
 
   if (warp == kConsumers / 32) {
     // ================= GEMM1 producer =================
-    // Ring bookkeeping without divisions: chunk gJ sits in stage cs with
-    // phase bit cph; the previous chunk's stage/phase are ps/pph; lseq is the
-    // W2 chunk (mod nseq) of the next load.
-    if (lane == 0 && myTiles > 0) {
+    // The whole warp runs the loop (so that counters and descriptors stay
+    // warp-uniform); lane 0 issues the single-thread operations (bulk copies,
+    // MMAs, commits).  Ring bookkeeping without divisions: chunk gJ sits in
+    // stage cs with phase bit cph; the previous chunk's stage/phase are
+    // ps/pph; lseq is the W2 chunk (mod nseq) of the next load.
+    if (myTiles > 0) {
+      const bool leader = lane == 0;
       const int totalJ = myTiles * nseq;
       constexpr uint32_t idesc1 = tc::idesc_f32acc(FMT, 128, 128);
       const uint32_t wbase = tc::smem_addr(smem + L.w);
       int nextLoad = 0, lseq = 0;
       auto wload = [&](int s) {  // chunk lseq -> stage s
-        tc::mbar_expect_tx(&bars.wfull[s], L.wStage);
-        tc::bulk_g2s(smem + L.w + (size_t)s * L.wStage, g.w2 + (size_t)lseq * L.wStage, L.wStage, &bars.wfull[s]);
+        if (leader) {
+          tc::mbar_expect_tx(&bars.wfull[s], L.wStage);
+          tc::bulk_g2s(smem + L.w + (size_t)s * L.wStage, g.w2 + (size_t)lseq * L.wStage, L.wStage, &bars.wfull[s]);
+        }
         nextLoad++;
         if (++lseq == nseq) lseq = 0;
       };
@@ -221,6 +226,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       const uint64_t dEh0 = tc::smem_desc(tc::smem_addr(A1hi), kLBO, sboE);
       const uint64_t dEl0 = tc::smem_desc(tc::smem_addr(A1lo), kLBO, sboE);
       const uint64_t dEstep = (uint64_t)((L.a1Half * (SPLIT ? 2u : 1u)) >> 4);
+      const uint64_t dW0 = tc::smem_desc(wbase, kLBO, sboW);
+      const uint64_t dWstage = (uint64_t)(L.wStage >> 4), dWlo = (uint64_t)(L.wHalf >> 4);
       int cs = 0, ps = 0;
       uint32_t cph = 0, pph = 0;
       bool first = true;
@@ -238,18 +245,20 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
           int ks = 0;
           for (int kc = 0; kc < g.nkc; kc++) {
             wait(&bars.wfull[cs], cph);
-            const uint64_t dWh = tc::smem_desc(wbase + (uint32_t)cs * L.wStage, kLBO, sboW);
-            const uint64_t dWl = dWh + (L.wHalf >> 4);
+            const uint64_t dWh = dW0 + (uint64_t)cs * dWstage;
             const int ks1 = min(K1B, (kc + 1) * g.KCB) >> 5;
-            for (uint64_t wo = 0; ks < ks1; ks++, wo += 16) {
-              const uint64_t eo = (uint64_t)ks * 16;
-              tc::mma<FMT>(dcol, dEh + eo, dWh + wo, idesc1, ks > 0 ? 1u : 0u);
-              if constexpr (SPLIT) {
-                tc::mma<FMT>(dcol, dEh + eo, dWl + wo, idesc1, 1u);
-                tc::mma<FMT>(dcol, dEl + eo, dWh + wo, idesc1, 1u);
+            if (leader) {
+              for (uint64_t wo = 0; ks < ks1; ks++, wo += 16) {
+                const uint64_t eo = (uint64_t)ks * 16;
+                tc::mma<FMT>(dcol, dEh + eo, dWh + wo, idesc1, ks > 0 ? 1u : 0u);
+                if constexpr (SPLIT) {
+                  tc::mma<FMT>(dcol, dEh + eo, dWh + dWlo + wo, idesc1, 1u);
+                  tc::mma<FMT>(dcol, dEl + eo, dWh + wo, idesc1, 1u);
+                }
               }
+              tc::mma_commit(&bars.wfree[cs]);
             }
-            tc::mma_commit(&bars.wfree[cs]);
+            ks = ks1;
             // refill the stage of the previous chunk (its MMAs were issued a
             // chunk ago) while this chunk's MMAs stay queued
             if (!first && nextLoad < totalJ) {
@@ -264,28 +273,34 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
               cph ^= 1u;
             }
           }
-          tc::mma_commit(&bars.d1full[buf]);
+          if (leader) tc::mma_commit(&bars.d1full[buf]);
         }
-        tc::mma_commit(&bars.efree);
+        if (leader) tc::mma_commit(&bars.efree);
       }
     }
     __syncwarp();
   } else if (warp == kConsumers / 32 + 1) {
-    // ================= GEMM2 producer =================
-    if (lane == 0 && myTiles > 0) {
+    // ================= GEMM2 producer (whole warp, lane 0 issues) =================
+    if (myTiles > 0) {
+      const bool leader = lane == 0;
       const int totalK = myTiles * g.noc;
       const uint32_t idesc2 = tc::idesc_f32acc(FMT, 128, g.N2);
       const uint32_t kbase = tc::smem_addr(smem + L.k);
       int nextK = 0, kseq = 0;
       auto kload = [&](int s) {  // chunk kseq -> stage s
-        tc::mbar_expect_tx(&bars.kfull[s], L.kStage);
-        tc::bulk_g2s(smem + L.k + (size_t)s * L.kStage, g.kc2 + (size_t)kseq * L.kStage, L.kStage, &bars.kfull[s]);
+        if (leader) {
+          tc::mbar_expect_tx(&bars.kfull[s], L.kStage);
+          tc::bulk_g2s(smem + L.k + (size_t)s * L.kStage, g.kc2 + (size_t)kseq * L.kStage, L.kStage,
+                       &bars.kfull[s]);
+        }
         nextK++;
         if (++kseq == g.noc) kseq = 0;
       };
       for (int s0 = 0; s0 < g.NK && nextK < totalK; s0++) kload(s0);
       const uint64_t dAh = tc::smem_desc(tc::smem_addr(A2hi), kLBO, sbo2);
       const uint64_t dAl = tc::smem_desc(tc::smem_addr(A2lo), kLBO, sbo2);
+      const uint64_t dK0 = tc::smem_desc(kbase, kLBO, sbo2);
+      const uint64_t dKstage = (uint64_t)(L.kStage >> 4), dKlo = (uint64_t)(L.kHalf >> 4);
       const uint32_t dcol = tmem + 256;
       int ksg = 0;
       uint32_t kph = 0, aph = 0;
@@ -295,20 +310,21 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
           wait(&bars.a2full, aph);
           wait(&bars.kfull[ksg], kph);
           tc::fence_after_sync();
-          const uint64_t dKh = tc::smem_desc(kbase + (uint32_t)ksg * L.kStage, kLBO, sbo2);
-          const uint64_t dKl = dKh + (L.kHalf >> 4);
-          for (int ks = 0; ks < 2 * ESZ; ks++) {
-            const uint64_t o = (uint64_t)ks * 16;
-            const uint32_t acc0 = (oc > 0 || ks > 0) ? 1u : 0u;
-            tc::mma<FMT>(dcol, dAh + o, dKh + o, idesc2, acc0);
-            if constexpr (SPLIT) {
-              tc::mma<FMT>(dcol, dAh + o, dKl + o, idesc2, 1u);
-              tc::mma<FMT>(dcol, dAl + o, dKh + o, idesc2, 1u);
+          const uint64_t dKh = dK0 + (uint64_t)ksg * dKstage;
+          if (leader) {
+            for (int ks = 0; ks < 2 * ESZ; ks++) {
+              const uint64_t o = (uint64_t)ks * 16;
+              const uint32_t acc0 = (oc > 0 || ks > 0) ? 1u : 0u;
+              tc::mma<FMT>(dcol, dAh + o, dKh + o, idesc2, acc0);
+              if constexpr (SPLIT) {
+                tc::mma<FMT>(dcol, dAh + o, dKh + dKlo + o, idesc2, 1u);
+                tc::mma<FMT>(dcol, dAl + o, dKh + o, idesc2, 1u);
+              }
             }
+            tc::mma_commit(&bars.a2free);
+            tc::mma_commit(&bars.kfree[ksg]);
+            if (oc == g.noc - 1) tc::mma_commit(&bars.d2full);
           }
-          tc::mma_commit(&bars.a2free);
-          tc::mma_commit(&bars.kfree[ksg]);
-          if (oc == g.noc - 1) tc::mma_commit(&bars.d2full);
           if (nextK < totalK) {
             wait(&bars.kfree[ksg], kph);
             kload(ksg);
@@ -651,29 +667,31 @@ bool gemm_geometry(const GemmSpec& sp, int fmt, int passes, GemmGeom* g) {
   g->K1 = K1;
   g->N2 = N2;
   g->noc = (sp.c * sp.c + 63) / 64;
-  // bytes of K per row in one streamed W2 chunk: four k-steps for one-pass
-  // formats, two for the split form (whose stages carry hi and lo)
-  g->KCB = passes == 1 ? 128 : 64;
-  g->nkc = (K1 * esz + g->KCB - 1) / g->KCB;
   // dynamic limit: 227 KB minus the kernel's static shared memory (< 2 KB)
   const uint32_t limit = 227 * 1024 - 4096;
-  // prefer two field buffers (one-pass 16-bit formats), then two Kc stages,
-  // as long as the W2 ring keeps enough stages
-  for (int db = (passes == 1 && esz == 2) ? 1 : 0; db >= 0; db--) {
-    for (int nk = 2; nk >= 1; nk--) {
-      GemmGeom t = *g;
-      t.dbE = db;
-      t.NK = nk;
-      t.NW = 0;
-      const GemmSmem base = gemm_smem_layout(t);
-      if (base.total > limit) continue;
-      int nw = (int)((limit - base.total) / base.wStage);
-      if (nw > kGemmMaxNW) nw = kGemmMaxNW;
-      if (nw < (nk == 2 ? 4 : (db ? 3 : 2))) continue;
-      g->dbE = db;
-      g->NK = nk;
-      g->NW = nw;
-      return true;
+  // bytes of K per row in one streamed W2 chunk: four k-steps for one-pass
+  // formats, two for the split form (whose stages carry hi and lo), two
+  // when four do not fit; prefer two field buffers (one-pass 16-bit
+  // formats), then two Kc stages, as long as the W2 ring keeps enough stages
+  for (int kcb = passes == 1 ? 128 : 64; kcb >= 64; kcb -= 64) {
+    g->KCB = kcb;
+    g->nkc = (K1 * esz + kcb - 1) / kcb;
+    for (int db = (passes == 1 && esz == 2) ? 1 : 0; db >= 0; db--) {
+      for (int nk = 2; nk >= 1; nk--) {
+        GemmGeom t = *g;
+        t.dbE = db;
+        t.NK = nk;
+        t.NW = 0;
+        const GemmSmem base = gemm_smem_layout(t);
+        if (base.total > limit) continue;
+        int nw = (int)((limit - base.total) / base.wStage);
+        if (nw > kGemmMaxNW) nw = kGemmMaxNW;
+        if (nw < (nk == 2 ? 4 : (db ? 3 : 2))) continue;
+        g->dbE = db;
+        g->NK = nk;
+        g->NW = nw;
+        return true;
+      }
     }
   }
   return false;

@@ -714,7 +714,7 @@ __global__ void __launch_bounds__(kThreads) wfs_plain_kernel(const WfsArgs a) {
         // uniforms, the Poisson sampler continues from the third
         CounterStream st(a.seed, fr, i, pix, 0);
         const float g = rn != 0.f ? normal_counter(st) : 0.f;
-        if (pois && SCAL(s)[0] != 0.f) v = poisson_counter(st, v);
+        if (pois && SCAL(s)[0] != 0.f) v = poisson_counter_tab(st, v, *a.poisTab);
         if (rn != 0.f)
           v += rn * g + a.readBg;
         else

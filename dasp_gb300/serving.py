@@ -142,10 +142,13 @@ def poisson_schedule(rates_hz, duration_s: float, seed: int = 0):
     return ev
 
 
-def run_schedule(server: WfsServer, sids, phases, schedule, lead_s: float = 0.05, timeout_s: float = 120.0):
+def run_schedule(server: WfsServer, sids, phases, schedule, lead_s: float | None = None, timeout_s: float = 120.0):
     """Submit a whole arrival schedule (released on the server clock from now
-    + lead_s), drain it, and summarise latency and throughput.  ``phases[k]``
-    is a list of device phase frames of system k, used round-robin."""
+    + lead_s, by default long enough for the submissions themselves), drain
+    it, and summarise latency and throughput.  ``phases[k]`` is a list of
+    device phase frames of system k, used round-robin."""
+    if lead_s is None:
+        lead_s = 0.05 + 3e-5 * len(schedule)
     t0 = server.clock() + lead_s
     nph = [0] * len(sids)
     for t, k in schedule:
