@@ -65,26 +65,11 @@ __global__ void __launch_bounds__(kPostThreads, 4) wfs_post_kernel(const WfsArgs
     }
     __syncthreads();
     const float inv_mm = 1.0f / (float)mm;
-    const int npx = ns * mm;
-    constexpr int kBatch = 4;  // pixels whose loads are issued together
-    for (int wb = tid; wb < npx; wb += kBatch * blockDim.x) {
-      float vb[kBatch];
-#pragma unroll
-      for (int u = 0; u < kBatch; u++) {
-        const int w = wb + u * blockDim.x;
-        if (w < npx) {
-          const int s = div_small(w, mm, inv_mm);
-          vb[u] = a.bimg[(long long)s_frame[s] * a.bimgFrameStride + (long long)s_subap[s] * mm + (w - s * mm)];
-        }
-      }
-#pragma unroll 1
-    for (int u = 0; u < kBatch; u++) {
-      const int w = wb + u * blockDim.x;
-      if (w >= npx) break;
+    for (int w = tid; w < ns * mm; w += blockDim.x) {
       const int s = div_small(w, mm, inv_mm), pix = w - s * mm;
       const int i = s_subap[s];
       float* gp = a.bimg + (long long)s_frame[s] * a.bimgFrameStride + (long long)i * mm + pix;
-      float v = vb[u];
+      float v = *gp;
       if (noise) {
         // one stream per pixel: the read-noise normal takes the first two
         // uniforms, the Poisson sampler continues from the third
@@ -106,7 +91,6 @@ __global__ void __launch_bounds__(kPostThreads, 4) wfs_post_kernel(const WfsArgs
         *gp = v;
       }
       imgs[s * mm + pix] = v;
-    }
     }
     __syncthreads();
     if (!simple) {
