@@ -33,6 +33,7 @@ struct GemmGeom {
   int N2;      // GEMM2 N: nimg^2 rounded up to 16
   int NW, NK;  // ring stages for W2 and Kc chunks
   int dbE;     // 1: two field (GEMM1 A operand) buffers, the next tile's built during this one
+  int dbA2;    // 1: two |F|^2 (GEMM2 A operand) buffers, alternating between output chunks
   const uint8_t* w2;   // [noc][nkc] x {hi[, lo]} x [128 x KCB bytes], tensor-core smem order
   const uint8_t* kc2;  // [noc] x {hi[, lo]} x [N2 x 64 elements], tensor-core smem order
 };
@@ -54,7 +55,7 @@ __host__ __device__ inline GemmSmem gemm_smem_layout(const GemmGeom& g) {
   L.kStage = L.kHalf * hl;
   L.a1 = 0;
   L.a2 = (L.a1 + L.a1Half * hl * (g.dbE ? 2u : 1u) + 1023u) & ~1023u;
-  L.w = (L.a2 + L.a2Half * hl + 1023u) & ~1023u;
+  L.w = (L.a2 + L.a2Half * hl * (g.dbA2 ? 2u : 1u) + 1023u) & ~1023u;
   L.k = (L.w + (uint32_t)g.NW * L.wStage + 1023u) & ~1023u;
   L.total = L.k + (uint32_t)g.NK * L.kStage;
   return L;

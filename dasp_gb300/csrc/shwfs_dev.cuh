@@ -236,16 +236,20 @@ struct PoisTab {
   uint8_t guide[kPoisTabL][kPoisGuide];
 };
 
+// Poisson(L), integer 0 <= L < 64, by guided inversion of u
+__device__ __forceinline__ int poisson_table_int(const PoisTab& T, int L, float u) {
+  if (L <= 0) return 0;
+  const float* C = T.cdf + T.off[L];
+  const int n = T.len[L];
+  int k = T.guide[L][(int)(u * (float)kPoisGuide)];
+  while (k < n - 1 && u > C[k]) k++;
+  return k;
+}
+
 __device__ __forceinline__ float poisson_tab(const PoisTab& T, float u3, float u4, float lam) {
   const int L = (int)lam;
   const float d = lam - (float)L;  // exact
-  int k = 0;
-  if (L > 0) {
-    const float* C = T.cdf + T.off[L];
-    const int n = T.len[L];
-    k = T.guide[L][(int)(u3 * (float)kPoisGuide)];
-    while (k < n - 1 && u3 > C[k]) k++;
-  }
+  int k = poisson_table_int(T, L, u3);
   if (d > 0.0f) {
     float p = __expf(-d), F = p;
     int k2 = 0;
@@ -288,13 +292,22 @@ __device__ __forceinline__ float poisson_counter(CounterStream& st, float lam) {
 // (pois_table.cu)
 cudaError_t pois_table_device(const PoisTab** out);
 
-// As poisson_counter, with the tabulated sampler below lambda 64 (two
-// uniforms from the pixel's stream)
+// Poisson(lam) from the pixel's stream with the tables: below lambda 1024,
+// lam = 63 n + L + d is drawn as n independent Poisson(63) (one uniform
+// each, tabulated) plus Poisson(L + d) (two uniforms, poisson_tab) -- a sum
+// of independent Poisson variables is Poisson; above, PTRS.
+constexpr float kTabMaxLam = 1024.0f;
 __device__ __forceinline__ float poisson_counter_tab(CounterStream& st, float lam, const PoisTab& T) {
   if (!(lam > 0.0f)) return 0.0f;
-  if (lam < kModalMaxLam) {
+  if (lam < kTabMaxLam) {
+    int k = 0;
+    float rem = lam;
+    while (rem >= 64.0f) {  // exact: rem < 2^24
+      k += poisson_table_int(T, 63, st.uniform());
+      rem -= 63.0f;
+    }
     const float u3 = st.uniform(), u4 = st.uniform();
-    return poisson_tab(T, u3, u4, lam);
+    return (float)k + poisson_tab(T, u3, u4, rem);
   }
   return poisson_counter(st, lam);
 }

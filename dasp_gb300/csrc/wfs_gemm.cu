@@ -131,7 +131,7 @@ struct Bars {
   uint64_t kfull[kGemmMaxNK], kfree[kGemmMaxNK];
   uint64_t efull, efree;
   uint64_t d1full[2], d1free[2];
-  uint64_t a2full, a2free;
+  uint64_t a2full[2], a2free[2];  // per GEMM2 operand buffer
   uint64_t d2full, d2free;
 };
 
@@ -179,8 +179,10 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       tc::mbar_init(&bars.d1full[i], 1);
       tc::mbar_init(&bars.d1free[i], kConsumers / 32);
     }
-    tc::mbar_init(&bars.a2full, kConsumers / 32);
-    tc::mbar_init(&bars.a2free, 1);
+    for (int i = 0; i < 2; i++) {
+      tc::mbar_init(&bars.a2full[i], kConsumers / 32);
+      tc::mbar_init(&bars.a2free[i], 1);
+    }
     tc::mbar_init(&bars.d2full, 1);
     tc::mbar_init(&bars.d2free, kConsumers / 32);
     tc::fence_mbar_init();
@@ -297,17 +299,22 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         if (++kseq == g.noc) kseq = 0;
       };
       for (int s0 = 0; s0 < g.NK && nextK < totalK; s0++) kload(s0);
-      const uint64_t dAh = tc::smem_desc(tc::smem_addr(A2hi), kLBO, sbo2);
-      const uint64_t dAl = tc::smem_desc(tc::smem_addr(A2lo), kLBO, sbo2);
+      // GEMM2 operand buffer of chunk gK: (gK & 1) when double buffered
+      const uint64_t dAh0 = tc::smem_desc(tc::smem_addr(A2hi), kLBO, sbo2);
+      const uint64_t dAl0 = tc::smem_desc(tc::smem_addr(A2lo), kLBO, sbo2);
+      const uint64_t dAstep = (uint64_t)((L.a2Half * (SPLIT ? 2u : 1u)) >> 4);
+      uint32_t gK = 0;
       const uint64_t dK0 = tc::smem_desc(kbase, kLBO, sbo2);
       const uint64_t dKstage = (uint64_t)(L.kStage >> 4), dKlo = (uint64_t)(L.kHalf >> 4);
       const uint32_t dcol = tmem + 256;
       int ksg = 0;
-      uint32_t kph = 0, aph = 0;
+      uint32_t kph = 0;
       for (int lt = 0; lt < myTiles; lt++) {
         for (int oc = 0; oc < g.noc; oc++) {
           if (oc == 0 && lt >= 1) wait(&bars.d2free, (lt - 1) & 1);
-          wait(&bars.a2full, aph);
+          const uint32_t ab = g.dbA2 ? (gK & 1) : 0;
+          wait(&bars.a2full[ab], g.dbA2 ? ((gK >> 1) & 1) : (gK & 1));
+          const uint64_t dAh = dAh0 + (ab ? dAstep : 0), dAl = dAl0 + (ab ? dAstep : 0);
           wait(&bars.kfull[ksg], kph);
           tc::fence_after_sync();
           const uint64_t dKh = dK0 + (uint64_t)ksg * dKstage;
@@ -321,7 +328,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
                 tc::mma<FMT>(dcol, dAl + o, dKh + o, idesc2, 1u);
               }
             }
-            tc::mma_commit(&bars.a2free);
+            tc::mma_commit(&bars.a2free[ab]);
             tc::mma_commit(&bars.kfree[ksg]);
             if (oc == g.noc - 1) tc::mma_commit(&bars.d2full);
           }
@@ -329,7 +336,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
             wait(&bars.kfree[ksg], kph);
             kload(ksg);
           }
-          aph ^= 1u;
+          gK++;
           if (++ksg == g.NK) {
             ksg = 0;
             kph ^= 1u;
@@ -513,17 +520,24 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&bars.d1free[buf]);
       // A2 is free once the previous chunk's GEMM2 has completed
-      if (gA >= 1) wait(&bars.a2free, (gA - 1) & 1);
+      const uint32_t ab = g.dbA2 ? (gA & 1) : 0;
+      if (g.dbA2) {
+        if (gA >= 2) wait(&bars.a2free[ab], ((gA >> 1) - 1) & 1);
+      } else if (gA >= 1) {
+        wait(&bars.a2free[0], (gA - 1) & 1);
+      }
+      uint8_t* Ahi = A2hi + (size_t)ab * L.a2Half * (SPLIT ? 2 : 1);
+      uint8_t* Alo = Ahi + L.a2Half;
 #pragma unroll
       for (int h = 0; h < 2; h++) {
         float x8[8];
 #pragma unroll
         for (int e = 0; e < 8; e++) x8[e] = I[h * 8 + e];
-        store8<FMT, SPLIT>(A2hi, A2lo, kmaj(r, q * 16 + h * 8, ESZ, sbo2), x8);
+        store8<FMT, SPLIT>(Ahi, Alo, kmaj(r, q * 16 + h * 8, ESZ, sbo2), x8);
       }
       tc::fence_async_smem();
       __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&bars.a2full);
+      if (lane == 0) tc::mbar_arrive(&bars.a2full[ab]);
       gC++;
       gA++;
     };
@@ -677,20 +691,24 @@ bool gemm_geometry(const GemmSpec& sp, int fmt, int passes, GemmGeom* g) {
     g->KCB = kcb;
     g->nkc = (K1 * esz + kcb - 1) / kcb;
     for (int db = (passes == 1 && esz == 2) ? 1 : 0; db >= 0; db--) {
-      for (int nk = 2; nk >= 1; nk--) {
-        GemmGeom t = *g;
-        t.dbE = db;
-        t.NK = nk;
-        t.NW = 0;
-        const GemmSmem base = gemm_smem_layout(t);
-        if (base.total > limit) continue;
-        int nw = (int)((limit - base.total) / base.wStage);
-        if (nw > kGemmMaxNW) nw = kGemmMaxNW;
-        if (nw < (nk == 2 ? 4 : (db ? 3 : 2))) continue;
-        g->dbE = db;
-        g->NK = nk;
-        g->NW = nw;
-        return true;
+      for (int da = 1; da >= 0; da--) {
+        for (int nk = 2; nk >= 1; nk--) {
+          GemmGeom t = *g;
+          t.dbE = db;
+          t.dbA2 = da;
+          t.NK = nk;
+          t.NW = 0;
+          const GemmSmem base = gemm_smem_layout(t);
+          if (base.total > limit) continue;
+          int nw = (int)((limit - base.total) / base.wStage);
+          if (nw > kGemmMaxNW) nw = kGemmMaxNW;
+          if (nw < (nk == 2 ? 3 : 2)) continue;
+          g->dbE = db;
+          g->dbA2 = da;
+          g->NK = nk;
+          g->NW = nw;
+          return true;
+        }
       }
     }
   }
