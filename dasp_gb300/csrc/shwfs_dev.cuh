@@ -292,22 +292,15 @@ __device__ __forceinline__ float poisson_counter(CounterStream& st, float lam) {
 // (pois_table.cu)
 cudaError_t pois_table_device(const PoisTab** out);
 
-// Poisson(lam) from the pixel's stream with the tables: below lambda 1024,
-// lam = 63 n + L + d is drawn as n independent Poisson(63) (one uniform
-// each, tabulated) plus Poisson(L + d) (two uniforms, poisson_tab) -- a sum
-// of independent Poisson variables is Poisson; above, PTRS.
-constexpr float kTabMaxLam = 1024.0f;
+// Poisson(lam) from the pixel's stream: below lambda 64 the tabulated
+// sampler (two uniforms, poisson_tab), above PTRS (poisson_counter).  (Summing
+// tabulated Poisson(63) parts for larger lambda is exact too, but measured
+// slower than PTRS from lambda 64 on.)
 __device__ __forceinline__ float poisson_counter_tab(CounterStream& st, float lam, const PoisTab& T) {
   if (!(lam > 0.0f)) return 0.0f;
-  if (lam < kTabMaxLam) {
-    int k = 0;
-    float rem = lam;
-    while (rem >= 64.0f) {  // exact: rem < 2^24
-      k += poisson_table_int(T, 63, st.uniform());
-      rem -= 63.0f;
-    }
+  if (lam < kModalMaxLam) {
     const float u3 = st.uniform(), u4 = st.uniform();
-    return (float)k + poisson_tab(T, u3, u4, rem);
+    return poisson_tab(T, u3, u4, lam);
   }
   return poisson_counter(st, lam);
 }

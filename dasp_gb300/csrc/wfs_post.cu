@@ -20,12 +20,16 @@ namespace {
 
 constexpr int kPostThreads = 256;
 constexpr int kPostMaxTS = 64;
+constexpr int kPostBright = 512;  // queued bright pixels per tile (overflow: drawn in place)
 
 __global__ void __launch_bounds__(kPostThreads, 4) wfs_post_kernel(const WfsArgs a, const PoisTab* __restrict__ tab) {
   extern __shared__ __align__(16) float smem_post[];
   __shared__ int s_subap[kPostMaxTS];
   __shared__ int s_frame[kPostMaxTS];
   __shared__ unsigned char s_pflag[kPostMaxTS];
+  __shared__ int s_nbright;
+  __shared__ int s_bright[kPostBright];
+  __shared__ float s_brightv[kPostBright];
   const int tid = threadIdx.x;
   const int mm = a.m * a.m;
   const bool cw2d = a.centWeightDim == 2;
@@ -63,13 +67,13 @@ __global__ void __launch_bounds__(kPostThreads, 4) wfs_post_kernel(const WfsArgs
       s_subap[s] = i;
       s_pflag[s] = a.totsig[i] > 0.f || a.sky * a.frac[i] > 0.f || a.skyArr;
     }
+    if (tid == 0) s_nbright = 0;
     __syncthreads();
     const float inv_mm = 1.0f / (float)mm;
-    for (int w = tid; w < ns * mm; w += blockDim.x) {
+    // noise, threshold [, power, bimg write] of pixel w of the tile
+    auto pixel = [&](int w, float v) {
       const int s = div_small(w, mm, inv_mm), pix = w - s * mm;
       const int i = s_subap[s];
-      float* gp = a.bimg + (long long)s_frame[s] * a.bimgFrameStride + (long long)i * mm + pix;
-      float v = *gp;
       if (noise) {
         // one stream per pixel: the read-noise normal takes the first two
         // uniforms, the Poisson sampler continues from the third
@@ -88,10 +92,30 @@ __global__ void __launch_bounds__(kPostThreads, 4) wfs_post_kernel(const WfsArgs
           v = v * v;
         else if (a.pxlPower != 1.f && a.pxlPower != 0.f)
           v = powf(v, a.pxlPower);
-        *gp = v;
+        a.bimg[(long long)s_frame[s] * a.bimgFrameStride + (long long)i * mm + pix] = v;
       }
       imgs[s * mm + pix] = v;
+    };
+    // Pixels whose Poisson mean needs the rejection sampler (lambda >= 64)
+    // are queued and drawn afterwards with the whole CTA, so that one bright
+    // pixel does not hold the other 31 lanes of its warp (same streams, same
+    // draws).
+    for (int w = tid; w < ns * mm; w += blockDim.x) {
+      const int s = div_small(w, mm, inv_mm);
+      const float v = a.bimg[(long long)s_frame[s] * a.bimgFrameStride + (long long)s_subap[s] * mm + (w - s * mm)];
+      if (noise && pois && s_pflag[s] && v >= kModalMaxLam) {
+        const int slot = atomicAdd(&s_nbright, 1);
+        if (slot < kPostBright) {
+          s_bright[slot] = w;
+          s_brightv[slot] = v;
+          continue;
+        }
+      }
+      pixel(w, v);
     }
+    __syncthreads();
+    const int nb = min(s_nbright, kPostBright);
+    for (int k = tid; k < nb; k += blockDim.x) pixel(s_bright[k], s_brightv[k]);
     __syncthreads();
     if (!simple) {
       post_tile(a, ns, s_subap, s_frame, s_cw, [&](int s) { return imgs + s * mm; }, [&](int) { return mm; });

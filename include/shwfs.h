@@ -260,8 +260,8 @@ shwfs_status shwfs_set_split_event(shwfs_handle* h, void* event);
 /* Draws of the engine's counter-based noise for testing its samplers (no
  * reference counterpart; the reference draws through rk_poisson/gsl,
  * cmod/src/centmodule.c:722-784).  kind 2: out[i] ~ Poisson(lam[i]) by the
- * tabulated sampler every compute form uses (sum of tabulated parts below
- * lambda 1024, PTRS above); kind 1: out[i] ~ N(0, 1) (lam
+ * tabulated sampler every compute form uses (tables below lambda 64, PTRS
+ * above); kind 1: out[i] ~ N(0, 1) (lam
  * unused); kind 0: out[i] ~ Poisson(lam[i]) by the table-free modal
  * inversion (an independent exact sampler, kept to cross-check kind 2).  Element i uses the stream of
  * (seed, frame, i).  lam and out are device pointers; with stream NULL the

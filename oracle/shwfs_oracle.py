@@ -227,7 +227,7 @@ class CentOracle:
                  seed=1, nthreads=1, spotpsf=None, opticalBinning=0, centWeight=None,
                  threshType=0, imageOnly=0, useBrightest=0, preBinningFactor=1,
                  parabolicFit=0, gaussianFit=0, gaussianMinVal=0.0, gaussianReplaceVal=0.0,
-                 correlationCentroiding=0, mode="f32"):
+                 correlationCentroiding=0, corrThresh=0.0, corrPattern=None, mode="f32"):
         self.mode = mode
         self.dt = np.float32 if mode == "f32" else np.float64
         self.nsubx = nsubx
@@ -259,9 +259,16 @@ class CentOracle:
         self.gaussianMinVal = np.float32(gaussianMinVal)
         self.gaussianReplaceVal = np.float32(gaussianReplaceVal)
         self.correlationCentroiding = int(correlationCentroiding)
-        if self.correlationCentroiding:
-            raise NotImplementedError("correlation centroiding is not restated in the oracle")
-        self.corrsize = self.m
+        self.corrThresh = np.float32(corrThresh)
+        self.corrPattern = None
+        self.corrPatternSize = 0
+        if corrPattern is not None:
+            cp = np.asarray(corrPattern, np.float32)
+            self.corrPattern = cp.reshape(self.nsubaps, cp.shape[-2], cp.shape[-1]).copy()
+            self.corrPatternSize = cp.shape[-1]
+        self.corrsize = self.corrPatternSize if (self.correlationCentroiding and self.corrPattern is not None) \
+            else self.m
+        self.corrimg = None
         self.fitMx = None
         self.fitMxParam = 0
         self.refCents = None
@@ -439,6 +446,17 @@ class CentOracle:
             self.set_use_brightest(val)
         elif code == INTEGSTEPS:
             self.nintegrations = int(val)
+        elif code == CORRELATIONCENTROIDING:
+            self.correlationCentroiding = int(val)
+            self.corrsize = self.corrPatternSize if self.correlationCentroiding else self.m
+        elif code == CORRTHRESH:
+            self.corrThresh = np.float32(val)
+        elif code == CORRPATTERN:
+            if val is None:
+                self.corrPattern = None
+            else:
+                cp = np.asarray(val, np.float32)
+                self.corrPattern = cp.reshape(self.nsubaps, cp.shape[-2], cp.shape[-1]).copy()
         else:
             raise ValueError("code %d not handled by the oracle" % code)
 
@@ -817,6 +835,8 @@ class CentOracle:
                     cents[2 * i + 1] = 0
         vec_cog = (self.imageOnly == 0 and self.opticalBinning != 1 and self.parabolicFit == 0
                    and self.gaussianFit <= 0 and self.correlationCentroiding == 0)
+        if self.corrimg is None or self.corrimg.shape[-1] != self.corrsize:
+            self.corrimg = np.zeros((self.nsubaps, self.corrsize, self.corrsize), np.float32)
         for k, i in enumerate(lit):
             flat = img[k].reshape(-1)
             if self.calsource == 0:
@@ -830,23 +850,7 @@ class CentOracle:
                 flat[:nexp] = np.power(flat[:nexp], self.dt(self.pxlPower)).astype(self.dt)
             bimg[i] = img[k].astype(np.float32)
             if self.imageOnly == 0 and not vec_cog:
-                if self.opticalBinning == 1:
-                    cx, cy = self._ob_cents(flat)
-                elif self.parabolicFit != 0 or self.gaussianFit > 0:
-                    cx, cy = self._fit(img[k], self.parabolicFit + self.gaussianFit, self.gaussianFit,
-                                       self.correlationCentroiding)
-                else:
-                    if self.centWeightDim == 2:
-                        w = self.centWeight
-                    elif self.centWeightDim == 4:
-                        w = self.centWeight[i]
-                    else:
-                        w = None
-                    cob = self.correlationCentroiding
-                    if cob == 5:
-                        cob = 1
-                    cx, cy = self._cog(img[k], w, cob)
-                cx, cy = self._calibrate(i, cx, cy)
+                cx, cy = self._centroid(i, img[k])
                 cents[2 * i] = cx
                 cents[2 * i + 1] = cy
 
@@ -862,6 +866,48 @@ class CentOracle:
                 cxk, cyk = self._calibrate(i, cx[k], cy[k])
                 cents[2 * i] = cxk
                 cents[2 * i + 1] = cyk
+
+    def _correlate(self, i, img):
+        """The correlation image of subap i (centroidsFromPhase :1898-1925):
+        written to corrimg and returned, or the image itself when off."""
+        cc = self.correlationCentroiding
+        if cc == 0 or self.corrPattern is None:
+            return img
+        n, cs, dt = self.m, self.corrsize, self.dt
+        pat = self.corrPattern[i]
+        if cc == 1:
+            out = calc_correlation(n, cs, pat, img, dt)
+        elif 1 < cc < 5:
+            out = diff_correlation(n, cs, self.ncen, img, pat, cc - 1, dt)
+        else:
+            out = brute_correlation(n, cs, self.ncen, img, pat, dt)
+        threshold_correlation(out, self.corrThresh, dt)
+        self.corrimg[i] = out.astype(np.float32)
+        return out
+
+    def _centroid(self, i, img):
+        """correlation (optional), then optical-binning/fit/CoG, calibration
+        and references for one lit subap (:1898-1961)."""
+        flat = img.reshape(-1)
+        if self.opticalBinning == 1:
+            cx, cy = self._ob_cents(flat)
+        else:
+            cimg = self._correlate(i, img)
+            if self.parabolicFit != 0 or self.gaussianFit > 0:
+                cx, cy = self._fit(cimg, self.parabolicFit + self.gaussianFit, self.gaussianFit,
+                                   self.correlationCentroiding)
+            else:
+                if self.centWeightDim == 2:
+                    w = self.centWeight
+                elif self.centWeightDim == 4:
+                    w = self.centWeight[i]
+                else:
+                    w = None
+                cob = self.correlationCentroiding
+                if cob == 5:
+                    cob = 1
+                cx, cy = self._cog(cimg, w, cob)
+        return self._calibrate(i, cx, cy)
 
     def _cog_vec(self, img, weight):
         """computeCoG with a centred window, vectorised over subaps.
@@ -933,21 +979,9 @@ class CentOracle:
                         b[:nexp] = np.power(b[:nexp], np.float32(self.pxlPower))
                     bimg[i] = b.reshape(m, m)
                     if self.imageOnly == 0:
-                        img = b.reshape(m, m).astype(self.dt)
-                        if self.opticalBinning == 1:
-                            cx, cy = self._ob_cents(img.reshape(-1))
-                        elif self.parabolicFit != 0 or self.gaussianFit > 0:
-                            cx, cy = self._fit(img, self.parabolicFit + self.gaussianFit, self.gaussianFit,
-                                               self.correlationCentroiding)
-                        else:
-                            if self.centWeightDim == 2:
-                                w = self.centWeight
-                            elif self.centWeightDim == 4:
-                                w = self.centWeight[i]
-                            else:
-                                w = None
-                            cx, cy = self._cog(img, w, self.correlationCentroiding)
-                        cx, cy = self._calibrate(i, cx, cy)
+                        if self.corrimg is None or self.corrimg.shape[-1] != self.corrsize:
+                            self.corrimg = np.zeros((self.nsubaps, self.corrsize, self.corrsize), np.float32)
+                        cx, cy = self._centroid(i, b.reshape(m, m).astype(self.dt))
                         cents[2 * i] = cx
                         cents[2 * i + 1] = cy
                 else:
@@ -978,6 +1012,187 @@ class CentOracle:
 
 
 # ----------------------------------------------------------------------------
+# correlation centroiding (cmod/src/centmodule.c:1203-1505)
+
+def r2hc_2d(x: np.ndarray) -> np.ndarray:
+    """FFTW's 2-D r2r transform with kinds (R2HC, R2HC): the unnormalised
+    1-D real-to-halfcomplex transform along each axis (r_k at k, i_k at n-k)."""
+    def r2hc(a, axis):
+        n = a.shape[axis]
+        X = np.fft.fft(a, axis=axis)
+        out = np.real(X).copy()
+        idx = np.arange(n)
+        im = np.imag(X)
+        # i_k goes to position n-k for 0 < k < (n+1)/2
+        ks = np.arange(1, (n + 1) // 2)
+        take = np.take(im, ks, axis=axis)
+        put = [slice(None)] * a.ndim
+        put[axis] = n - ks
+        out[tuple(put)] = take
+        return out
+    return r2hc(r2hc(np.asarray(x, np.float64), 1), 0)
+
+
+def hc2r_2d(h: np.ndarray) -> np.ndarray:
+    """FFTW's 2-D r2r transform with kinds (HC2R, HC2R): the unnormalised
+    inverse of r2hc_2d along each axis (hc2r_2d(r2hc_2d(x)) = n^2 x)."""
+    def hc2r(a, axis):
+        n = a.shape[axis]
+        a = np.moveaxis(np.asarray(a, np.float64), axis, 0)
+        j = np.arange(n)[:, None]
+        out = np.repeat(a[0:1], n, axis=0).astype(np.float64)
+        for k in range(1, (n + 1) // 2):
+            ang = 2 * np.pi * j * k / n
+            out = out + 2 * (np.cos(ang).reshape((n,) + (1,) * (a.ndim - 1)) * a[k]
+                             - np.sin(ang).reshape((n,) + (1,) * (a.ndim - 1)) * a[n - k])
+        if n % 2 == 0:
+            out = out + ((-1.0) ** np.arange(n)).reshape((n,) + (1,) * (a.ndim - 1)) * a[n // 2]
+        return np.moveaxis(out, 0, axis)
+    return hc2r(hc2r(h, 1), 0)
+
+
+def calc_correlation(nimg, corrsize, pattern, img, dt):
+    """calcCorrelation (:1403-1486): zero-pad the image to corrsize, r2hc,
+    multiply by the half-complex pattern, hc2r (all unnormalised).  The
+    half-complex product is the product of the complex spectra, so this is
+    the circular convolution of the padded image with hc2r_2d(pattern)."""
+    tmp = np.zeros((corrsize, corrsize), np.float64)
+    o = (corrsize - nimg) // 2
+    tmp[o:o + nimg, o:o + nimg] = img
+    n = corrsize
+    a = r2hc_2d(tmp)
+    B = np.asarray(pattern, np.float64)
+    out = a.copy()
+    m = n
+    neven, meven = n % 2 == 0, m % 2 == 0
+    out[0, 0] = a[0, 0] * B[0, 0]
+    if neven:
+        out[0, n // 2] = a[0, n // 2] * B[0, n // 2]
+    if meven:
+        out[m // 2, 0] = a[m // 2, 0] * B[m // 2, 0]
+        if neven:
+            out[m // 2, n // 2] = a[m // 2, n // 2] * B[m // 2, n // 2]
+    for i in range(1, (n + 1) // 2):
+        out[0, i] = a[0, i] * B[0, i] - a[0, n - i] * B[0, n - i]
+        out[0, n - i] = a[0, i] * B[0, n - i] + a[0, n - i] * B[0, i]
+        if meven:
+            r = m // 2
+            out[r, i] = a[r, i] * B[r, i] - a[r, n - i] * B[r, n - i]
+            out[r, n - i] = a[r, i] * B[r, n - i] + a[r, n - i] * B[r, i]
+    for i in range(1, (m + 1) // 2):
+        out[i, 0] = a[i, 0] * B[i, 0] - a[m - i, 0] * B[m - i, 0]
+        out[m - i, 0] = a[i, 0] * B[m - i, 0] + a[m - i, 0] * B[i, 0]
+        if neven:
+            c = n // 2
+            out[i, c] = a[i, c] * B[i, c] - a[m - i, c] * B[m - i, c]
+            out[m - i, c] = a[i, c] * B[m - i, c] + a[m - i, c] * B[i, c]
+        for j in range(1, (n + 1) // 2):
+            out[i, j] = (a[i, j] * B[i, j] + a[m - i, n - j] * B[m - i, n - j] - a[i, n - j] * B[i, n - j]
+                         - a[m - i, j] * B[m - i, j])
+            out[m - i, n - j] = (a[i, j] * B[m - i, n - j] + a[m - i, n - j] * B[i, j] + a[m - i, j] * B[i, n - j]
+                                 + a[i, n - j] * B[m - i, j])
+            out[i, n - j] = (a[i, j] * B[i, n - j] - a[m - i, n - j] * B[m - i, j] + a[i, n - j] * B[i, j]
+                             - a[m - i, j] * B[m - i, n - j])
+            out[m - i, j] = (a[i, j] * B[m - i, j] - a[m - i, n - j] * B[i, n - j] + a[m - i, j] * B[i, j]
+                             - a[i, n - j] * B[m - i, n - j])
+    return hc2r_2d(out).astype(dt)
+
+
+def _overlap(i, nimg, corrsize, ncen):
+    """offsets/extent of the reference/image overlap for output offset i
+    (diffCorrelation/bruteCorrelation, :1228-1240)."""
+    off = i - ncen // 2
+    mm = min(corrsize, nimg)
+    sref = max(0, -off - (nimg - corrsize) // 2)
+    sin_ = max(0, (nimg - corrsize) // 2 + off)
+    if sin_ + mm > nimg:
+        mm = nimg - sin_
+    if sref + mm > corrsize:
+        mm = corrsize - sref
+    return sref, sin_, mm
+
+
+def diff_correlation(nimg, corrsize, ncen, img, pattern, mode, dt):
+    """diffCorrelation (:1203-1338); mode 1: mean squared difference, 3:
+    squared difference over the product of the fluxes, 2: the reference's
+    abs-difference branch (with its own indexing)."""
+    out = np.zeros((corrsize, corrsize), dt)
+    c0 = (corrsize - ncen) // 2
+    if mode in (1, 3):
+        for i in range(ncen):
+            srefy, siny, my = _overlap(i, nimg, corrsize, ncen)
+            for j in range(ncen):
+                srefx, sinx, mx = _overlap(j, nimg, corrsize, ncen)
+                s = dt(0)
+                tot = dt(0)
+                tot2 = dt(0)
+                for y in range(my):
+                    for x in range(mx):
+                        b = dt(img[siny + y, sinx + x])
+                        c = dt(pattern[srefy + y, srefx + x])
+                        d = dt(c - b)
+                        s = dt(s + d * d)
+                        tot = dt(tot + b)
+                        tot2 = dt(tot2 + c)
+                if mode == 1:
+                    if mx != 0 and my != 0:
+                        out[i + c0, j + c0] = dt(s / (mx * my))
+                elif tot != 0 and tot2 != 0:
+                    out[i + c0, j + c0] = dt(s / (tot * tot2))
+    else:
+        flat_out = out.reshape(-1)
+        for i in range(ncen):
+            my = corrsize - abs(ncen // 2 - i)
+            for j in range(ncen):
+                mx = corrsize - abs(ncen // 2 - j)
+                s = dt(0)
+                for y in range(my):
+                    for x in range(mx):
+                        if i < ncen // 2:
+                            if j < ncen // 2:
+                                d = pattern.flat[y * corrsize + x] - img.flat[(ncen // 2 - i + y) * nimg + ncen // 2 - j + x]
+                            else:
+                                d = pattern.flat[y * corrsize + j - ncen // 2 + x] - img.flat[(ncen // 2 - i + y) * nimg + x]
+                        else:
+                            if j < ncen // 2:
+                                d = pattern.flat[(i - ncen // 2 + y) * corrsize + x] - img.flat[y * nimg + ncen // 2 - j + x]
+                            else:
+                                d = pattern.flat[(i - ncen // 2 + y) * corrsize + j - ncen // 2 + x] - img.flat[y * nimg + x]
+                        s = dt(s + abs(dt(d)))
+                flat_out[(i + (nimg - ncen) // 2) * corrsize + j + (nimg - ncen) // 2] = dt(s * s / (my * mx))
+    return out
+
+
+def brute_correlation(nimg, corrsize, ncen, img, pattern, dt):
+    """bruteCorrelation (:1339-1398): overlap sums of the product."""
+    out = np.zeros((corrsize, corrsize), dt)
+    c0 = (corrsize - ncen) // 2
+    for i in range(ncen):
+        srefy, siny, my = _overlap(i, nimg, corrsize, ncen)
+        for j in range(ncen):
+            srefx, sinx, mx = _overlap(j, nimg, corrsize, ncen)
+            s = dt(0)
+            for y in range(my):
+                for x in range(mx):
+                    s = dt(s + dt(pattern[srefy + y, srefx + x] * img[siny + y, sinx + x]))
+            if mx != 0 and my != 0:
+                out[i + c0, j + c0] = s
+    return out
+
+
+def threshold_correlation(img, thresh, dt):
+    """thresholdCorrelation (:1488-1505), in place on the flat image."""
+    flat = img.reshape(-1)
+    t = dt(thresh)
+    if 0 < thresh <= 1:
+        mx = dt(0)
+        for v in flat:
+            if v > mx:
+                mx = v
+        t = dt(mx * t)
+    flat[:] = np.where(flat < t, dt(0), (flat - t).astype(dt))
+
+
 # counter-based stream of the engine's default noise mode
 # ----------------------------------------------------------------------------
 

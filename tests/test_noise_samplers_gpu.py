@@ -49,10 +49,9 @@ def _chi2_poisson(x, lam):
 @pytest.mark.parametrize("lam", [0.05, 0.7, 1.0, 2.5, 3.99, 4.0, 9.7, 10.0, 17.3, 29.9, 30.5, 63.9, 64.0, 127.5, 150.0,
                                  500.0, 1000.0, 2000.0])
 def test_poisson_chi_square(lam, kind):
-    """kind 2: the sampler every compute form uses (below 1024: tabulated
-    Poisson(63) parts + tabulated Poisson(floor of the rest) + inversion of
-    the fractional remainder; PTRS above); kind 0: the table-free modal
-    inversion below 64 / PTRS."""
+    """kind 2: the sampler every compute form uses (below 64: tabulated
+    Poisson(floor lam) + inversion of the fractional remainder; PTRS above);
+    kind 0: the table-free modal inversion below 64 / PTRS."""
     x = _draw(kind, lam, 1 << 21)
     p = _chi2_poisson(x, lam)
     assert p > 1e-6, "chi-square p-value %g at lambda %g" % (p, lam)
