@@ -112,6 +112,7 @@ struct shwfs_handle {
   float gMin = 0, gRep = 0, corrThresh = 0;
   int psfDim = 0, psfsize = 0, padded = 0, phaseAmp = 0, W = 0;
   int centWeightDim = 0;
+  int cwSize = 0;  // image size the centroid weights are for
   int noiseMode = SHWFS_NOISE_COUNTER;
   uint64_t framesRead = 0;
   bool haveCalData = false, haveCalCoeff = false, haveRef = false;
@@ -154,6 +155,15 @@ struct shwfs_handle {
   DevBuf<float> d_iscale;  // fp16 form: 1 / (sum of the subaperture's pupil)^2
   cudaEvent_t splitEvent = nullptr;  // recorded between image formation and post stages
   const PoisTab* poisTab = nullptr;  // Poisson CDF tables on this device
+  // correlation centroiding: pattern (host copy), its size, the per-mode
+  // device kernel, and the corrimg output (borrowed; device mirror)
+  std::vector<float> corrPatHost;
+  int corrPatternSize = 0;
+  int corrKMode = -1;  // mode the device kernel was built for
+  DevBuf<float> d_corrK;
+  shwfs_array corrimg{};
+  DevBuf<float> d_corrimg;
+  std::vector<float> corrimgStage;
   std::vector<float> psfHost, binTHost, binNHost;
   std::vector<int> binIdxHost;
   // CUDA-graph batches: bumped whenever a launch captured from this handle
@@ -359,11 +369,89 @@ shwfs_status plan(shwfs_handle* h) {
   return SHWFS_OK;
 }
 
+// corrsize: the pattern's size while correlating with a pattern, else nimg
+// (cmod/src/centmodule.c:2717-2721, 3006)
+int corr_size(const shwfs_handle* h) {
+  return (h->correlationCentroiding && !h->corrPatHost.empty()) ? h->corrPatternSize : h->nimg;
+}
+
+// correlation images are computed (patterns set, centroids wanted)
+bool corr_active(const shwfs_handle* h) {
+  return h->correlationCentroiding != 0 && !h->corrPatHost.empty() && h->imageOnly == 0 && h->opticalBinning != 1;
+}
+
+// hc2r x hc2r (FFTW's unnormalised half-complex inverse along each axis) of
+// an n x n half-complex array, in double
+void hc2r_2d(const float* h, int n, std::vector<double>& out) {
+  std::vector<double> cs(n * n), sn(n * n), t((size_t)n * n);
+  for (int j = 0; j < n; j++)
+    for (int k = 0; k < n; k++) {
+      const double a = 2.0 * M_PI * (double)((long long)j * k % n) / n;
+      cs[j * n + k] = cos(a);
+      sn[j * n + k] = sin(a);
+    }
+  auto line = [&](const double* in, double* o, int stride) {  // one 1-D inverse
+    for (int j = 0; j < n; j++) {
+      double y = in[0];
+      for (int k = 1; k < (n + 1) / 2; k++) y += 2.0 * (in[k * stride] * cs[j * n + k] - in[(n - k) * stride] * sn[j * n + k]);
+      if (n % 2 == 0) y += ((j & 1) ? -1.0 : 1.0) * in[(n / 2) * stride];
+      o[j * stride] = y;
+    }
+  };
+  std::vector<double> src((size_t)n * n);
+  for (int i = 0; i < n * n; i++) src[i] = h[i];
+  for (int r = 0; r < n; r++) line(&src[(size_t)r * n], &t[(size_t)r * n], 1);  // along rows
+  out.assign((size_t)n * n, 0.0);
+  for (int c = 0; c < n; c++) line(&t[c], &out[c], n);  // along columns
+}
+
+shwfs_status load_corr_pattern(shwfs_handle* h, const shwfs_array& cp) {
+  h->corrKMode = -1;
+  if (is_none(cp)) {
+    h->corrPatHost.clear();
+    h->d_corrK.reset();
+    return SHWFS_OK;
+  }
+  if (check_f32(cp, "corrPattern") || cp.ndim != 4 || cp.shape[0] * cp.shape[1] != h->nsubaps ||
+      cp.shape[2] != cp.shape[3] || cp.shape[2] < h->nimg)
+    return fail(SHWFS_ERR_INVALID, "corrPattern wrong shape or type - should be (nsubx,nsubx,>=nimg,>=nimg), float32");
+  if (cp.shape[2] > 64) return fail(SHWFS_ERR_UNSUPPORTED, "correlation patterns larger than 64 pixels");
+  h->corrPatternSize = (int)cp.shape[2];
+  h->corrPatHost = to_host<float>(cp);
+  return SHWFS_OK;
+}
+
+shwfs_status set_corr_pattern(shwfs_handle* h, const shwfs_array& cp) {
+  if (shwfs_status s = load_corr_pattern(h, cp)) return s;
+  return plan(h);
+}
+
+// the device kernel for the current mode: hc2r of each pattern (mode 1) or
+// the patterns themselves
+shwfs_status prepare_corr(shwfs_handle* h) {
+  if (!corr_active(h) || h->corrKMode == h->correlationCentroiding) return SHWFS_OK;
+  const int n = h->corrPatternSize, cc = n * n;
+  std::vector<float> K(h->corrPatHost.size());
+  if (h->correlationCentroiding == 1) {
+    std::vector<double> o;
+    for (int i = 0; i < h->nsubaps; i++) {
+      hc2r_2d(h->corrPatHost.data() + (size_t)i * cc, n, o);
+      for (int k = 0; k < cc; k++) K[(size_t)i * cc + k] = (float)o[k];
+    }
+  } else {
+    K = h->corrPatHost;
+  }
+  CK(h->d_corrK.upload(K.data(), K.size()));
+  if (h->d_corrimg.n < (size_t)h->nsubaps * cc) CK(h->d_corrimg.alloc((size_t)h->nsubaps * cc));
+  h->corrKMode = h->correlationCentroiding;
+  return SHWFS_OK;
+}
+
 shwfs_status set_cent_weight(shwfs_handle* h, const shwfs_array& cw) {
   h->centWeightDim = 0;
   h->d_cw.reset();
   if (is_none(cw)) return SHWFS_OK;
-  const int corr = h->nimg;
+  const int corr = corr_size(h);
   if (cw.ndim != 2 && cw.ndim != 4) return fail(SHWFS_ERR_INVALID, "centWeight not 2d or 4d");
   if (check_f32(cw, "centWeight")) return SHWFS_ERR_INVALID;
   if (cw.shape[cw.ndim - 2] != corr || cw.shape[cw.ndim - 1] != corr)
@@ -373,6 +461,7 @@ shwfs_status set_cent_weight(shwfs_handle* h, const shwfs_array& cw) {
   std::vector<float> v = to_host<float>(cw);
   CK(h->d_cw.upload(v.data(), v.size()));
   h->centWeightDim = cw.ndim;
+  h->cwSize = corr;
   return SHWFS_OK;
 }
 
@@ -553,6 +642,7 @@ WfsArgs make_args(shwfs_handle* h, const float* phs, float* cents, float* bimg, 
   a.frame0 = h->framesRead;
   a.frameCtr = h->graphCtr;
   a.poisTab = h->poisTab;
+  a.skipCents = corr_active(h) ? 1 : 0;
   a.mode = mode;
   return a;
 }
@@ -614,10 +704,36 @@ shwfs_status build_gemm(shwfs_handle* h) {
   return SHWFS_OK;
 }
 
+// device buffer the correlation images of a frame go to
+float* corrimg_dev(shwfs_handle* h) {
+  if (!is_none(h->corrimg) && h->corrimg.on_device) return (float*)h->corrimg.data;
+  return h->d_corrimg.p;
+}
+
+// correlation images and centroids from the final images in bimg
+shwfs_status enqueue_corr(shwfs_handle* h, float* cents, float* bimg, int nframes, cudaStream_t st) {
+  if (!corr_active(h) || h->lit.empty()) return SHWFS_OK;
+  const int cs = h->corrPatternSize;
+  if (!is_none(h->corrimg) && numel(h->corrimg) < (int64_t)h->nsubaps * cs * cs)
+    return fail(SHWFS_ERR_INVALID, "corrimg must hold nsubx*nsubx*corrsize*corrsize values");
+  WfsArgs a = make_args(h, nullptr, cents, bimg, nframes, 0, kPost);
+  a.centWeight = h->d_cw.p;
+  CorrArgs c{};
+  c.mode = h->correlationCentroiding;
+  c.cs = cs;
+  c.thresh = h->corrThresh;
+  c.K = h->d_corrK.p;
+  c.corrimg = corrimg_dev(h);
+  c.corrimgFrameStride = 0;  // one frame at a time
+  CK(launch_corr(a, c, h->numSMs, st));
+  return SHWFS_OK;
+}
+
 // queue one readout over nframes frames (device pointers)
 // device-side state a readout needs that is built lazily (the fit matrix);
 // run before a graph capture so that nothing allocates while capturing
 shwfs_status prepare_readout(shwfs_handle* h) {
+  if (shwfs_status s = prepare_corr(h)) return s;
   if (h->fitMxParam != h->parabolicFit + h->gaussianFit && (h->parabolicFit || h->gaussianFit > 0)) {
     int fs = h->parabolicFit + h->gaussianFit;
     shwfs_status s = make_fit_mx(h, fs < 0 ? 3 : (fs < 3 ? 3 : fs));
@@ -634,6 +750,8 @@ shwfs_status enqueue_readout(shwfs_handle* h, const float* phs, float* cents, fl
   const long long ntiles = (nwork + h->TS - 1) / h->TS;
   const int grid = (int)std::max<long long>(1, std::min<long long>(ntiles, (long long)h->numSMs * h->ctasPerSM));
   if (shwfs_status s = prepare_readout(h)) return s;
+  if (corr_active(h) && nframes != 1)
+    return fail(SHWFS_ERR_UNSUPPORTED, "correlation centroiding runs one frame at a time");
   if (h->noiseMode == SHWFS_NOISE_REFERENCE) {
     if (nframes != 1) return fail(SHWFS_ERR_UNSUPPORTED, "reference-stream noise runs one frame at a time");
     if (nlit) {
@@ -684,7 +802,7 @@ shwfs_status enqueue_readout(shwfs_handle* h, const float* phs, float* cents, fl
       CK(launch_unlit(a, h->d_unlit.p, (int)h->unlit.size(), st));
     }
   }
-  return SHWFS_OK;
+  return enqueue_corr(h, cents, bimg, 1, st);
 }
 
 // the integration state machine of centroidsFromPhase (cmod/src/centmodule.c:
@@ -699,6 +817,14 @@ int readout_frame(const shwfs_handle* h) {
 // publish exactly what the reference writes on a readout frame: every
 // centroid unless imageOnly; every image with imageOnly, else the lit ones
 shwfs_status publish_outputs(shwfs_handle* h, cudaStream_t st, bool* sync) {
+  if (corr_active(h) && !is_none(h->corrimg) && !h->corrimg.on_device) {
+    // the reference writes the correlation images of lit subapertures
+    const size_t nc = (size_t)h->nsubaps * h->corrPatternSize * h->corrPatternSize;
+    h->corrimgStage.resize(nc);
+    CK(cudaMemcpyAsync(h->corrimgStage.data(), h->d_corrimg.p, nc * sizeof(float), cudaMemcpyDeviceToHost, st));
+    h->scatterPending = true;
+    *sync = true;
+  }
   if (!h->cents.on_device && !h->imageOnly)
     CK(cudaMemcpyAsync((void*)h->cents.data, h->d_cents.p, (size_t)h->nsubaps * 2 * sizeof(float),
                        cudaMemcpyDeviceToHost, st));
@@ -720,6 +846,7 @@ shwfs_status publish_outputs(shwfs_handle* h, cudaStream_t st, bool* sync) {
 
 // queue one image-input frame (centroidsFromImage)
 shwfs_status enqueue_slope(shwfs_handle* h, cudaStream_t st) {
+  if (shwfs_status s = prepare_readout(h)) return s;
   const float* img = (const float*)h->inputImage.data;
   if (!h->inputImage.on_device) {
     CK(cudaMemcpyAsync(h->d_image.p, h->inputImage.data, (size_t)numel(h->inputImage) * sizeof(float),
@@ -758,7 +885,7 @@ shwfs_status enqueue_slope(shwfs_handle* h, cudaStream_t st) {
       CK(launch_unlit(a, h->d_unlit.p, (int)h->unlit.size(), st));
     }
   }
-  return SHWFS_OK;
+  return enqueue_corr(h, cents, bimg, 1, st);
 }
 
 shwfs_status run_impl(shwfs_handle* h, cudaStream_t st, bool sync, float* elapsed, bool slope = false) {
@@ -795,9 +922,18 @@ shwfs_status run_impl(shwfs_handle* h, cudaStream_t st, bool sync, float* elapse
   if (sync) {
     CK(cudaStreamSynchronize(st));
     if (h->scatterPending) {
-      const size_t mm = (size_t)h->nimg * h->nimg;
-      float* dst = (float*)h->bimg.data;
-      for (int i : h->lit) memcpy(dst + i * mm, h->bimgStage.data() + i * mm, mm * sizeof(float));
+      if (!h->bimgStage.empty() && !h->bimg.on_device) {
+        const size_t mm = (size_t)h->nimg * h->nimg;
+        float* dst = (float*)h->bimg.data;
+        for (int i : h->lit) memcpy(dst + i * mm, h->bimgStage.data() + i * mm, mm * sizeof(float));
+        h->bimgStage.clear();
+      }
+      if (!h->corrimgStage.empty()) {
+        const size_t cc = (size_t)h->corrPatternSize * h->corrPatternSize;
+        float* dst = (float*)h->corrimg.data;
+        for (int i : h->lit) memcpy(dst + i * cc, h->corrimgStage.data() + i * cc, cc * sizeof(float));
+        h->corrimgStage.clear();
+      }
       h->scatterPending = false;
     }
     if ((h->noiseMode == SHWFS_NOISE_REFERENCE || gemm_active(h)) && readout) {
@@ -853,8 +989,6 @@ shwfs_status shwfs_initialise(const shwfs_init* in, shwfs_handle** out) {
                 h->ncen);
   if ((h->parabolicFit < 0 || h->gaussianFit > 0) && h->ncen < 3)
     return fail(SHWFS_ERR_INVALID, "a fit needs a centroid window of at least 3 pixels");
-  if (in->correlationCentroiding != 0)
-    return fail(SHWFS_ERR_UNSUPPORTED, "correlation centroiding is not implemented by this engine yet");
   // arrays: validation as py_initialise, plus size checks the C code trusts;
   // everything that needs no GPU is checked before the first CUDA call
   const int p = h->phasesize, nsa = h->nsubaps, m = h->nimg;
@@ -1009,6 +1143,11 @@ shwfs_status shwfs_initialise(const shwfs_init* in, shwfs_handle** out) {
   CK(h->d_tilt.upload(tilt.data(), tilt.size()));
 
   if ((s = set_spot_psf(h, in->spotpsf))) return s;
+  if ((s = load_corr_pattern(h, in->corrPattern))) return s;
+  if (!is_none(in->corrimg)) {
+    if (check_f32(in->corrimg, "corrimg")) return fail(SHWFS_ERR_INVALID, "corrimg must be float and contiguous");
+    h->corrimg = in->corrimg;
+  }
   if ((s = set_cent_weight(h, in->centWeight))) return s;
   if ((s = setup_threads(h, in->nthreads))) return s;
   if ((s = prepare_bin(h))) return s;
@@ -1161,17 +1300,25 @@ shwfs_status shwfs_update(shwfs_handle* h, int code, const shwfs_value* v) {
     }
     case SHWFS_CORRELATIONCENTROIDING:
       if ((s = need(SHWFS_VAL_INT, "int"))) return s;
-      if (v->ival != 0) return fail(SHWFS_ERR_UNSUPPORTED, "correlation centroiding is not implemented by this engine yet");
-      h->correlationCentroiding = 0;
-      break;
+      if (v->ival < 0 || v->ival > 5) return fail(SHWFS_ERR_INVALID, "correlationCentroiding must be 0..5");
+      h->correlationCentroiding = (int)v->ival;
+      // centWeight of the wrong size is dropped, as the reference does
+      if (h->centWeightDim && h->cwSize != corr_size(h)) {
+        h->centWeightDim = 0;
+        h->d_cw.reset();
+      }
+      return plan(h);
     case SHWFS_CORRTHRESH:
       if ((s = num("corrThresh", &d))) return s;
       h->corrThresh = (float)d;
       break;
-    case SHWFS_CORRPATTERN:
-      if (v->kind == SHWFS_VAL_ARRAY)
-        return fail(SHWFS_ERR_UNSUPPORTED, "correlation centroiding is not implemented by this engine yet");
-      break;
+    case SHWFS_CORRPATTERN: {
+      shwfs_array none{};
+      const bool arr = v->kind == SHWFS_VAL_ARRAY;
+      if (arr && h->corrPatternSize && v->arr[0].ndim == 4 && v->arr[0].shape[2] != h->corrPatternSize)
+        return fail(SHWFS_ERR_INVALID, "centmodule - corrPattern has changed size - please don't do that");
+      return set_corr_pattern(h, arr ? v->arr[0] : none);
+    }
     case SHWFS_CALDATA: {
       if (v->kind == SHWFS_VAL_NONE) {
         h->haveCalData = false;

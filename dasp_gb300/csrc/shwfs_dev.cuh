@@ -73,6 +73,9 @@ struct WfsArgs {
   const unsigned long long* frameCtr;
   // CDF tables of the tabulated Poisson sampler (device global memory)
   const struct PoisTab* poisTab;
+  // 1: the post stages write bimg but no centroids (correlation
+  // centroiding computes them afterwards from bimg)
+  int skipCents;
   int mode;
 };
 

@@ -192,80 +192,15 @@ __device__ inline void fit_centroid(const WfsArgs& a, float* img, float& ocx, fl
   ocy = cy;
 }
 
-// Stages 7-9 on a tile of ns subapertures whose images are in shared memory
-// (img_of(s)): brightest-pixel selection, pixel power, bimg write, centroids
-// with calibration and reference subtraction.  nexp_of(s) is the number of
-// exposed pixels of subaperture s (cmod/src/centmodule.c:1883-1961,
-// 2033-2107).
-template <class ImgOf, class NexpOf>
-__device__ __forceinline__ void post_tile(const WfsArgs& a, int ns, const int* s_subap, const int* s_frame,
-                                          const float* s_cw, ImgOf img_of, NexpOf nexp_of) {
+// Stage 9 on a tile of ns subapertures whose images (a.m x a.m) are in shared
+// memory (img_of(s)): centroids (optical binning, fit or CoG), calibration,
+// reference subtraction (cmod/src/centmodule.c:1925-1961, 2069-2107).  Used on
+// the correlation images too, with a.m the correlation size.
+template <class ImgOf>
+__device__ __forceinline__ void centroid_tile(const WfsArgs& a, int ns, const int* s_subap, const int* s_frame,
+                                              const float* s_cw, ImgOf img_of) {
     const int tid = threadIdx.x;
     const int m = a.m, mm = m * m;
-    // ---- 7: brightest-pixel selection (one warp per subap) ----
-    if (a.calsource == 0 && (a.useBrightest != 0 || a.useBrightestArr)) {
-      const int warp = tid >> 5, lane = tid & 31, nwarps = blockDim.x >> 5;
-      for (int s = warp; s < ns; s += nwarps) {
-        int ub = a.useBrightestArr ? a.useBrightestArr[s_subap[s]] : a.useBrightest;
-        bool subtract = false;
-        if (ub < 0) {
-          ub = -ub;
-          subtract = true;
-        }
-        if (!(ub > 0 && ub < nexp_of(s))) continue;
-        float* img = img_of(s);
-        const int pos = nexp_of(s) - ub;  // ascending sorted index of the threshold
-        float thr = 0.f;
-        bool found = false;
-        for (int j = lane; j < nexp_of(s); j += 32) {
-          const float xj = img[j];
-          int lt = 0, le = 0;
-          for (int k = 0; k < nexp_of(s); k++) {
-            lt += img[k] < xj;
-            le += img[k] <= xj;
-          }
-          if (lt <= pos && pos < le) {
-            thr = xj;
-            found = true;
-          }
-        }
-        const unsigned bal = __ballot_sync(0xffffffffu, found);
-        if (bal == 0u) continue;  // only with NaN pixels: leave the image as is
-        thr = __shfl_sync(0xffffffffu, thr, __ffs(bal) - 1);
-        float sub = 0.f;
-        if (subtract) {
-          float best = -INFINITY;
-          for (int j = lane; j < nexp_of(s); j += 32)
-            if (img[j] < thr) best = fmaxf(best, img[j]);
-          for (int o = 16; o; o >>= 1) best = fmaxf(best, __shfl_xor_sync(0xffffffffu, best, o));
-          sub = best == -INFINITY ? 0.f : best;
-        }
-        __syncwarp();
-        for (int j = lane; j < nexp_of(s); j += 32) {
-          const float v = img[j];
-          img[j] = v < thr ? 0.f : (subtract ? v - sub : v);
-        }
-      }
-      __syncthreads();
-    }
-
-    // ---- 8: pixel power, bimg write ----
-    const float inv_mm = 1.0f / (float)mm;
-    for (int w = tid; w < ns * mm; w += blockDim.x) {
-      const int s = div_small(w, mm, inv_mm), pix = w - s * mm;
-      float v = img_of(s)[pix];
-      if (pix < nexp_of(s)) {
-        if (a.pxlPower == 2.f)
-          v = v * v;
-        else if (a.pxlPower != 1.f && a.pxlPower != 0.f)
-          v = powf(v, a.pxlPower);
-        img_of(s)[pix] = v;
-      }
-      a.bimg[(long long)s_frame[s] * a.bimgFrameStride + (long long)s_subap[s] * mm + pix] = v;
-    }
-    if (a.imageOnly != 0) return;
-    __syncthreads();
-
     // ---- 9: centroids, calibration, reference subtraction ----
     const bool seqMode = a.opticalBinning == 1 || a.fitSize != 0 || a.gaussianFit > 0 || a.cob != 0;
     if (seqMode) {
@@ -364,6 +299,82 @@ __device__ __forceinline__ void post_tile(const WfsArgs& a, int ns, const int* s
         }
       }
     }
+}
+
+// Stages 7-9 on a tile of ns subapertures whose images are in shared memory
+// (img_of(s)): brightest-pixel selection, pixel power, bimg write, centroids
+// with calibration and reference subtraction.  nexp_of(s) is the number of
+// exposed pixels of subaperture s (cmod/src/centmodule.c:1883-1961,
+// 2033-2107).
+template <class ImgOf, class NexpOf>
+__device__ __forceinline__ void post_tile(const WfsArgs& a, int ns, const int* s_subap, const int* s_frame,
+                                          const float* s_cw, ImgOf img_of, NexpOf nexp_of) {
+    const int tid = threadIdx.x;
+    const int m = a.m, mm = m * m;
+    // ---- 7: brightest-pixel selection (one warp per subap) ----
+    if (a.calsource == 0 && (a.useBrightest != 0 || a.useBrightestArr)) {
+      const int warp = tid >> 5, lane = tid & 31, nwarps = blockDim.x >> 5;
+      for (int s = warp; s < ns; s += nwarps) {
+        int ub = a.useBrightestArr ? a.useBrightestArr[s_subap[s]] : a.useBrightest;
+        bool subtract = false;
+        if (ub < 0) {
+          ub = -ub;
+          subtract = true;
+        }
+        if (!(ub > 0 && ub < nexp_of(s))) continue;
+        float* img = img_of(s);
+        const int pos = nexp_of(s) - ub;  // ascending sorted index of the threshold
+        float thr = 0.f;
+        bool found = false;
+        for (int j = lane; j < nexp_of(s); j += 32) {
+          const float xj = img[j];
+          int lt = 0, le = 0;
+          for (int k = 0; k < nexp_of(s); k++) {
+            lt += img[k] < xj;
+            le += img[k] <= xj;
+          }
+          if (lt <= pos && pos < le) {
+            thr = xj;
+            found = true;
+          }
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, found);
+        if (bal == 0u) continue;  // only with NaN pixels: leave the image as is
+        thr = __shfl_sync(0xffffffffu, thr, __ffs(bal) - 1);
+        float sub = 0.f;
+        if (subtract) {
+          float best = -INFINITY;
+          for (int j = lane; j < nexp_of(s); j += 32)
+            if (img[j] < thr) best = fmaxf(best, img[j]);
+          for (int o = 16; o; o >>= 1) best = fmaxf(best, __shfl_xor_sync(0xffffffffu, best, o));
+          sub = best == -INFINITY ? 0.f : best;
+        }
+        __syncwarp();
+        for (int j = lane; j < nexp_of(s); j += 32) {
+          const float v = img[j];
+          img[j] = v < thr ? 0.f : (subtract ? v - sub : v);
+        }
+      }
+      __syncthreads();
+    }
+
+    // ---- 8: pixel power, bimg write ----
+    const float inv_mm = 1.0f / (float)mm;
+    for (int w = tid; w < ns * mm; w += blockDim.x) {
+      const int s = div_small(w, mm, inv_mm), pix = w - s * mm;
+      float v = img_of(s)[pix];
+      if (pix < nexp_of(s)) {
+        if (a.pxlPower == 2.f)
+          v = v * v;
+        else if (a.pxlPower != 1.f && a.pxlPower != 0.f)
+          v = powf(v, a.pxlPower);
+        img_of(s)[pix] = v;
+      }
+      a.bimg[(long long)s_frame[s] * a.bimgFrameStride + (long long)s_subap[s] * mm + pix] = v;
+    }
+    if (a.imageOnly != 0 || a.skipCents) return;
+    __syncthreads();
+    centroid_tile(a, ns, s_subap, s_frame, s_cw, img_of);
 }
 
 template <int N, int P>
@@ -738,6 +749,18 @@ __global__ void __launch_bounds__(kThreads) wfs_plain_kernel(const WfsArgs a) {
 
 // launcher of the unlit-subaperture kernel (wfs_unlit.cu)
 cudaError_t launch_unlit(const WfsArgs& a, const int* unlit, int nunlit, cudaStream_t stream);
+// correlation centroiding (wfs_corr.cu)
+struct CorrArgs {
+  int mode;       // correlationCentroiding, 1..5
+  int cs;         // corrsize
+  float thresh;   // corrThresh
+  const float* K; // per subaperture cs*cs: mode 1 the convolution kernel hc2r(pattern), else the pattern
+  float* corrimg; // [frame][nsubaps][cs*cs] output
+  long long corrimgFrameStride;
+  int TS;         // subapertures per CTA tile (set by the launcher)
+};
+cudaError_t launch_corr(const WfsArgs& a, CorrArgs c, int numSMs, cudaStream_t stream);
+
 // increment n device counters (graph replays of a batch)
 cudaError_t launch_bump_counters(unsigned long long* const* ctrs, int n, cudaStream_t stream);
 // counter-based noise draws for testing the samplers (kind 0 Poisson, 1 normal)

@@ -68,8 +68,18 @@ __global__ void __launch_bounds__(kPostThreads, 4) wfs_post_kernel(const WfsArgs
       s_pflag[s] = a.totsig[i] > 0.f || a.sky * a.frac[i] > 0.f || a.skyArr;
     }
     if (tid == 0) s_nbright = 0;
-    __syncthreads();
     const float inv_mm = 1.0f / (float)mm;
+    // the tile's pre-noise pixels into shared memory with asynchronous
+    // copies: every load is in flight at once instead of one per iteration
+    for (int w = tid; w < ns * mm; w += blockDim.x) {
+      const int s = div_small(w, mm, inv_mm);
+      const float* src = a.bimg + (long long)s_frame[s] * a.bimgFrameStride + (long long)s_subap[s] * mm + (w - s * mm);
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(imgs + w)),
+                   "l"(src)
+                   : "memory");
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncthreads();
     // noise, threshold [, power, bimg write] of pixel w of the tile
     auto pixel = [&](int w, float v) {
       const int s = div_small(w, mm, inv_mm), pix = w - s * mm;
@@ -102,7 +112,7 @@ __global__ void __launch_bounds__(kPostThreads, 4) wfs_post_kernel(const WfsArgs
     // draws).
     for (int w = tid; w < ns * mm; w += blockDim.x) {
       const int s = div_small(w, mm, inv_mm);
-      const float v = a.bimg[(long long)s_frame[s] * a.bimgFrameStride + (long long)s_subap[s] * mm + (w - s * mm)];
+      const float v = imgs[w];
       if (noise && pois && s_pflag[s] && v >= kModalMaxLam) {
         const int slot = atomicAdd(&s_nbright, 1);
         if (slot < kPostBright) {
@@ -121,7 +131,7 @@ __global__ void __launch_bounds__(kPostThreads, 4) wfs_post_kernel(const WfsArgs
       post_tile(a, ns, s_subap, s_frame, s_cw, [&](int s) { return imgs + s * mm; }, [&](int) { return mm; });
       continue;
     }
-    if (a.imageOnly != 0) continue;
+    if (a.imageOnly != 0 || a.skipCents) continue;
     // centred-window CoG (post_tile's stage 9, same summation order): one
     // warp per subaperture, lanes over the window pixels
     const int warp = tid >> 5, lane = tid & 31, nwarps = blockDim.x >> 5;

@@ -90,7 +90,9 @@ class Case:
                           preBinningFactor=p["preBinningFactor"], parabolicFit=p["parabolicFit"],
                           gaussianFit=0 if gf is None else 1,
                           gaussianMinVal=0.0 if gf is None else gf[0],
-                          gaussianReplaceVal=0.0 if gf is None else gf[1], mode=mode)
+                          gaussianReplaceVal=0.0 if gf is None else gf[1],
+                          correlationCentroiding=p["correlationCentroiding"], corrThresh=p["corrThresh"],
+                          corrPattern=p["corrPattern"], mode=mode)
 
     def oracle_run(self, orc, phs=None, cents=None, bimg=None):
         phs = self.phs if phs is None else phs
