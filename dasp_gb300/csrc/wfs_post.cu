@@ -68,6 +68,7 @@ __global__ void __launch_bounds__(kPostThreads, 4) wfs_post_kernel(const WfsArgs
       s_pflag[s] = a.totsig[i] > 0.f || a.sky * a.frac[i] > 0.f || a.skyArr;
     }
     if (tid == 0) s_nbright = 0;
+    __syncthreads();  // the tile's subaperture list is complete
     const float inv_mm = 1.0f / (float)mm;
     // the tile's pre-noise pixels into shared memory with asynchronous
     // copies: every load is in flight at once instead of one per iteration
