@@ -592,6 +592,7 @@ WfsArgs make_args(shwfs_handle* h, const float* phs, float* cents, float* bimg, 
   a.nframes = nframes;
   a.TS = h->TS;
   a.lit = h->d_lit.p;
+  a.subflag = h->d_subflag.p;
   a.phs = phs;
   a.pup = h->d_pup.p;
   a.tilt = h->d_tilt.p;

@@ -27,6 +27,7 @@ struct WfsArgs {
   int nlit, nframes;
   int TS;  // subapertures per CTA tile
   const int* lit;
+  const int* subflag;  // per subaperture: 1 = lit
   const float* phs;
   const float* pup;
   const float* tilt;

@@ -24,9 +24,13 @@
 // limit) and tf32 (one pass, kind::tf32).  Accumulation is always f32.
 //
 // Warp roles (576 threads):
-//   warps 0-15  consumers: thread t owns MMA row r = t & 127 (its subaperture)
-//               and column quarter q = t >> 7; they build E, read D1 and
-//               write |F|^2, read D2 and store the image
+//   warps 0-7   epilogue: thread t owns MMA row r = t & 127 (its
+//               subaperture, TMEM lane) and column half t >> 7; reads D1 and
+//               writes |F|^2 into the GEMM2 operand, reads D2 and stores the
+//               image
+//   warps 8-15  field build: E of the next tile (row r, every other pixel
+//               group), one tile ahead of GEMM1 when two field buffers fit,
+//               so that its global loads overlap the epilogue and the MMAs
 //   warp 16     GEMM1 producer: streams W2 chunks through an NW-stage ring
 //               with bulk asynchronous copies and issues the GEMM1 MMAs
 //   warp 17     GEMM2 producer: streams Kc chunks (NK-stage ring) and
@@ -54,6 +58,8 @@ namespace shwfs {
 namespace {
 
 constexpr int kConsumers = 512;
+constexpr int kEpiWarps = 8;    // warps 0-7: D1/D2 epilogue
+constexpr int kFieldWarps = 8;  // warps 8-15: field build
 constexpr int kGemmThreads = kConsumers + 64;
 constexpr int kTileSubaps = 128;
 constexpr uint32_t kTmemCols = 512;
@@ -129,7 +135,7 @@ __device__ __forceinline__ void sincos_reduced(float t, float* s, float* c) {
 struct Bars {
   uint64_t wfull[kGemmMaxNW], wfree[kGemmMaxNW];
   uint64_t kfull[kGemmMaxNK], kfree[kGemmMaxNK];
-  uint64_t efull, efree;
+  uint64_t efull[2], efree[2];  // per field buffer
   uint64_t d1full[2], d1free[2];
   uint64_t a2full[2], a2free[2];  // per GEMM2 operand buffer
   uint64_t d2full, d2free;
@@ -173,18 +179,20 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       tc::mbar_init(&bars.kfull[i], 1);
       tc::mbar_init(&bars.kfree[i], 1);
     }
-    tc::mbar_init(&bars.efull, kConsumers / 32);
-    tc::mbar_init(&bars.efree, 1);
     for (int i = 0; i < 2; i++) {
-      tc::mbar_init(&bars.d1full[i], 1);
-      tc::mbar_init(&bars.d1free[i], kConsumers / 32);
+      tc::mbar_init(&bars.efull[i], kFieldWarps);
+      tc::mbar_init(&bars.efree[i], 1);
     }
     for (int i = 0; i < 2; i++) {
-      tc::mbar_init(&bars.a2full[i], kConsumers / 32);
+      tc::mbar_init(&bars.d1full[i], 1);
+      tc::mbar_init(&bars.d1free[i], kEpiWarps);
+    }
+    for (int i = 0; i < 2; i++) {
+      tc::mbar_init(&bars.a2full[i], kEpiWarps);
       tc::mbar_init(&bars.a2free[i], 1);
     }
     tc::mbar_init(&bars.d2full, 1);
-    tc::mbar_init(&bars.d2free, kConsumers / 32);
+    tc::mbar_init(&bars.d2free, kEpiWarps);
     tc::fence_mbar_init();
   }
   tc::fence_before_sync();
@@ -235,10 +243,12 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       bool first = true;
       uint32_t gC = 0;
       for (int lt = 0; lt < myTiles; lt++) {
-        wait(&bars.efull, lt & 1);
+        // field buffer eb; its uses alternate when double buffered
+        const int eb = g.dbE ? (lt & 1) : 0;
+        wait(&bars.efull[eb], (uint32_t)((g.dbE ? (lt >> 1) : lt) & 1));
         tc::fence_after_sync();
-        const uint64_t dEh = dEh0 + ((g.dbE && (lt & 1)) ? dEstep : 0);
-        const uint64_t dEl = dEl0 + ((g.dbE && (lt & 1)) ? dEstep : 0);
+        const uint64_t dEh = dEh0 + (eb ? dEstep : 0);
+        const uint64_t dEl = dEl0 + (eb ? dEstep : 0);
         for (int oc = 0; oc < g.noc; oc++, gC++) {
           const uint32_t buf = gC & 1;
           if (gC >= 2) wait(&bars.d1free[buf], ((gC >> 1) - 1) & 1);
@@ -277,7 +287,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
           }
           if (leader) tc::mma_commit(&bars.d1full[buf]);
         }
-        if (leader) tc::mma_commit(&bars.efree);
+        if (leader) tc::mma_commit(&bars.efree[eb]);
       }
     }
     __syncwarp();
@@ -347,13 +357,14 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     __syncwarp();
   } else {
     // ================= consumers =================
-    const int r = tid & 127, q = tid >> 7;
+    // warps 0-7: epilogue (TMEM lane quarter warp & 3, column half h);
+    // warps 8-15: field build (row r, pixel-group parity h)
+    const int r = tid & 127, h = (tid >> 7) & 1;
+    const bool fieldRole = warp >= kEpiWarps;
     const bool vecPup = (pp & 3) == 0 && ((uintptr_t)a.pup & 15) == 0;
     const bool vecPhs = (p & 1) == 0 && (a.W & 1) == 0 && (a.phsFrameStride & 1) == 0 && ((uintptr_t)a.phs & 7) == 0;
     const bool vecOut = (mm & 3) == 0 && (a.bimgFrameStride & 3) == 0 && ((uintptr_t)a.bimg & 15) == 0;
     const uint32_t lanebase = (uint32_t)(32 * (warp & 3)) << 16;
-    const int ngroups = (ppr / 8 + 3) / 4;  // pixel groups of 8 per thread (at most)
-    uint32_t gC = 0, gA = 0;
 
     struct Row {
       bool live;
@@ -371,22 +382,13 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       return o;
     };
 
-    // E = pup*exp(i(phs - tilt)) of this row, pixel groups i0 <= i < i1 of
-    // this thread (group g8 = q + 4i covers pixels 8*g8 .. +7), Re at
-    // K = pix, Im at K = ppr + pix, into field buffer eb
-    auto build_E = [&](int eb, const Row& R, int i0, int i1) {
-      uint8_t* Ehi = A1hi + (size_t)eb * L.a1Half * (SPLIT ? 2 : 1);
-      uint8_t* Elo = Ehi + L.a1Half;
-      const int sy = R.sub / a.nsubx, sx = R.sub - sy * a.nsubx;
-      const float* ph = a.phs + (long long)R.frm * a.phsFrameStride + (long long)sy * p * a.W + sx * p;
-      const float* pu = a.pup + (long long)R.sub * pp;
-      for (int i = i0; i < i1; i++) {
-        const int g8 = q + 4 * i;
-        if (g8 * 8 >= ppr) break;
-        float er[8], ei[8], phv[8], puv[8];
+    if (fieldRole) {
+      // ---- field build: E = pup*exp(i(phs - tilt)) of this row, pixel
+      // groups g8 = h, h+2, ... (8 pixels each), Re at K = pix, Im at
+      // K = ppr + pix; two groups' loads are in flight before either is used
+      auto load_group = [&](const Row& R, const float* ph, const float* pu, int g8, float (&phv)[8],
+                            float (&puv)[8]) {
         const int pix0 = g8 * 8;
-        // vector loads where the layout allows: each lane reads its own
-        // subaperture's row, so wide loads cut the memory transactions
         if (R.live && vecPup && pix0 + 8 <= pp) {
           const float4 u0 = *reinterpret_cast<const float4*>(pu + pix0);
           const float4 u1 = *reinterpret_cast<const float4*>(pu + pix0 + 4);
@@ -417,6 +419,11 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
             phv[e] = (R.live && pix < pp) ? ph[(long long)ii * a.W + jj] : 0.f;
           }
         }
+      };
+      auto emit_group = [&](uint8_t* Ehi, uint8_t* Elo, const Row& R, int g8, const float (&phv)[8],
+                            const float (&puv)[8]) {
+        const int pix0 = g8 * 8;
+        float er[8], ei[8];
 #pragma unroll
         for (int e = 0; e < 8; e++) {
           const int pix = pix0 + e;
@@ -436,158 +443,149 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         }
         store8<FMT, SPLIT>(Ehi, Elo, kmaj(r, pix0, ESZ, sboE), er);
         store8<FMT, SPLIT>(Ehi, Elo, kmaj(r, ppr + pix0, ESZ, sboE), ei);
-      }
-    };
-    // zero K padding beyond 2*ppr (none when 2*ppr is a multiple of 16)
-    auto pad_E = [&](int eb) {
-      uint8_t* Ehi = A1hi + (size_t)eb * L.a1Half * (SPLIT ? 2 : 1);
-      uint8_t* Elo = Ehi + L.a1Half;
-      for (int k = 2 * ppr + q; k < g.K1; k += 4) {
-        const uint32_t off = kmaj(r, k, ESZ, sboE);
-        if constexpr (ESZ == 4) {
-          *reinterpret_cast<uint32_t*>(Ehi + off) = 0u;
-        } else {
-          *reinterpret_cast<uint16_t*>(Ehi + off) = 0;
-          if constexpr (SPLIT) *reinterpret_cast<uint16_t*>(Elo + off) = 0;
-        }
-      }
-    };
-    auto e_done = [&]() {
-      tc::fence_async_smem();
-      __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&bars.efull);
-    };
-
-    // binned image of tile lt (row P) from D2: normalise, sky -> bimg
-    auto read_D2 = [&](int lt, const Row& P) {
-      wait(&bars.d2full, lt & 1);
-      tc::fence_after_sync();
-      const int i = P.sub;
-      const float totsig = a.totsig[i];
-      const float fr = a.frac[i];
-      float scale = totsig > 0.f ? (a.sigArr ? a.sigArr[i] / totsig : a.sig * fr / totsig) : 1.f;
-      if (iscale) scale = scale / iscale[i];  // undo the fp16 range scaling
-      const float skyv = a.sky * fr;
-      float* out = a.bimg + (long long)P.frm * a.bimgFrameStride + (long long)i * mm;
-      const float* skyA = a.skyArr ? a.skyArr + (long long)i * mm : nullptr;
-      for (int cb = q * 32; cb < mm; cb += 128) {
-        uint32_t v[32];
-        tc::tmem_ld32(tmem + 256 + lanebase + cb, v);
-        tc::tmem_ld_wait();
-        if (!P.live) continue;
-        const int n = min(32, mm - cb);
-        float x[32];
-#pragma unroll
-        for (int e = 0; e < 32; e++) {
-          x[e] = __uint_as_float(v[e]);
-          if (totsig > 0.f || iscale) x[e] *= scale;
-          if (skyv > 0.f) x[e] += skyv;
-          if (skyA && e < n) x[e] += skyA[cb + e];
-        }
-        if (vecOut) {  // n is a multiple of 4 here
-#pragma unroll
-          for (int e = 0; e < 32; e += 4)
-            if (e < n) *reinterpret_cast<float4*>(out + cb + e) = make_float4(x[e], x[e + 1], x[e + 2], x[e + 3]);
-        } else {
-#pragma unroll
-          for (int e = 0; e < 32; e++)
-            if (e < n) out[cb + e] = x[e];
-        }
-      }
-      tc::fence_before_sync();
-      __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&bars.d2free);
-    };
-
-    // one output chunk of the current tile: |F|^2 of the 16 complex outputs
-    // in columns 32q .. 32q+31 of this row -> the GEMM2 operand
-    auto chunk = [&](float isc) {
-      const uint32_t buf = gC & 1;
-      wait(&bars.d1full[buf], (gC >> 1) & 1);
-      tc::fence_after_sync();
-      float I[16];
-      {
-        uint32_t v[32];
-        tc::tmem_ld32(tmem + buf * 128 + lanebase + q * 32, v);
-        tc::tmem_ld_wait();
-#pragma unroll
-        for (int e = 0; e < 16; e++) {
-          const float re = __uint_as_float(v[2 * e]), im = __uint_as_float(v[2 * e + 1]);
-          I[e] = (re * re + im * im) * isc;
-        }
-      }
-      tc::fence_before_sync();
-      __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&bars.d1free[buf]);
-      // A2 is free once the previous chunk's GEMM2 has completed
-      const uint32_t ab = g.dbA2 ? (gA & 1) : 0;
-      if (g.dbA2) {
-        if (gA >= 2) wait(&bars.a2free[ab], ((gA >> 1) - 1) & 1);
-      } else if (gA >= 1) {
-        wait(&bars.a2free[0], (gA - 1) & 1);
-      }
-      uint8_t* Ahi = A2hi + (size_t)ab * L.a2Half * (SPLIT ? 2 : 1);
-      uint8_t* Alo = Ahi + L.a2Half;
-#pragma unroll
-      for (int h = 0; h < 2; h++) {
-        float x8[8];
-#pragma unroll
-        for (int e = 0; e < 8; e++) x8[e] = I[h * 8 + e];
-        store8<FMT, SPLIT>(Ahi, Alo, kmaj(r, q * 16 + h * 8, ESZ, sbo2), x8);
-      }
-      tc::fence_async_smem();
-      __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&bars.a2full[ab]);
-      gC++;
-      gA++;
-    };
-
-    if (myTiles > 0) {
-      if (!g.dbE) {
-        // one field buffer: tile lt's field is built once GEMM1 of tile
-        // lt-1 has finished with the buffer
-        Row prev{false, 0, 0};
-        for (int lt = 0; lt <= myTiles; lt++) {
-          const Row cur = row_of(lt);
-          if (lt < myTiles) {
-            if (lt >= 1) wait(&bars.efree, (lt - 1) & 1);
-            build_E(0, cur, 0, ngroups);
-            pad_E(0);
-            e_done();
-          }
-          if (lt >= 1) read_D2(lt - 1, prev);
-          if (lt == myTiles) break;
-          const float isc = (iscale && cur.live) ? iscale[cur.sub] : 1.f;
-          for (int oc = 0; oc < g.noc; oc++) chunk(isc);
-          prev = cur;
-        }
-      } else {
-        // two field buffers: the next tile's field is built in slices
-        // between this tile's output chunks, overlapping GEMM1
-        Row cur = row_of(0);
-        build_E(0, cur, 0, ngroups);
-        pad_E(0);
-        pad_E(1);
-        e_done();
-        Row prev{false, 0, 0};
-        for (int lt = 0; lt < myTiles; lt++) {
-          const Row next = row_of(lt + 1);
-          const bool more = lt + 1 < myTiles;
-          const float isc = (iscale && cur.live) ? iscale[cur.sub] : 1.f;
-          for (int oc = 0; oc < g.noc; oc++) {
-            if (more) {
-              if (oc == 0 && lt >= 1) wait(&bars.efree, (lt - 1) & 1);
-              build_E((lt + 1) & 1, next, (oc * ngroups) / g.noc, ((oc + 1) * ngroups) / g.noc);
-              if (oc == g.noc - 1) e_done();
+      };
+      const int ng8 = ppr / 8;
+      Row next = row_of(0);
+      for (int lt = 0; lt < myTiles; lt++) {
+        const Row R = next;
+        next = row_of(lt + 1);  // its index loads overlap this tile
+        const int eb = g.dbE ? (lt & 1) : 0;
+        uint8_t* Ehi = A1hi + (size_t)eb * L.a1Half * (SPLIT ? 2 : 1);
+        uint8_t* Elo = Ehi + L.a1Half;
+        const int reuse = g.dbE ? 2 : 1;  // tiles between two uses of a buffer
+        if (lt >= reuse) wait(&bars.efree[eb], (uint32_t)(((lt - reuse) / reuse) & 1));
+        if (lt < reuse) {
+          // zero K padding beyond 2*ppr once per buffer (none when 2*ppr is
+          // a multiple of 16)
+          for (int k = 2 * ppr + h; k < g.K1; k += 2) {
+            const uint32_t off = kmaj(r, k, ESZ, sboE);
+            if constexpr (ESZ == 4) {
+              *reinterpret_cast<uint32_t*>(Ehi + off) = 0u;
+            } else {
+              *reinterpret_cast<uint16_t*>(Ehi + off) = 0;
+              if constexpr (SPLIT) *reinterpret_cast<uint16_t*>(Elo + off) = 0;
             }
-            if (oc == 0 && lt >= 1) read_D2(lt - 1, prev);
-            chunk(isc);
           }
-          prev = cur;
-          cur = next;
         }
-        read_D2(myTiles - 1, prev);
+        const int sy = R.sub / a.nsubx, sx = R.sub - sy * a.nsubx;
+        const float* ph = a.phs + (long long)R.frm * a.phsFrameStride + (long long)sy * p * a.W + sx * p;
+        const float* pu = a.pup + (long long)R.sub * pp;
+        for (int g8 = h; g8 < ng8; g8 += 4) {
+          float phA[8], puA[8], phB[8], puB[8];
+          const bool two = g8 + 2 < ng8;
+          load_group(R, ph, pu, g8, phA, puA);
+          if (two) load_group(R, ph, pu, g8 + 2, phB, puB);
+          emit_group(Ehi, Elo, R, g8, phA, puA);
+          if (two) emit_group(Ehi, Elo, R, g8 + 2, phB, puB);
+        }
+        tc::fence_async_smem();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&bars.efull[eb]);
       }
+    } else {
+      // ---- epilogue ----
+      uint32_t gC = 0, gA = 0;
+      // binned image of tile lt (row P) from D2: normalise, sky -> bimg
+      auto read_D2 = [&](int lt, const Row& P) {
+        const int i = P.sub;
+        const float totsig = a.totsig[i];
+        const float fr = a.frac[i];
+        const float isc = iscale ? iscale[i] : 1.f;
+        wait(&bars.d2full, lt & 1);
+        tc::fence_after_sync();
+        float scale = totsig > 0.f ? (a.sigArr ? a.sigArr[i] / totsig : a.sig * fr / totsig) : 1.f;
+        if (iscale) scale = scale / isc;  // undo the fp16 range scaling
+        const float skyv = a.sky * fr;
+        float* out = a.bimg + (long long)P.frm * a.bimgFrameStride + (long long)i * mm;
+        const float* skyA = a.skyArr ? a.skyArr + (long long)i * mm : nullptr;
+        for (int cb = h * 32; cb < mm; cb += 64) {
+          uint32_t v[32];
+          tc::tmem_ld32(tmem + 256 + lanebase + cb, v);
+          tc::tmem_ld_wait();
+          if (!P.live) continue;
+          const int n = min(32, mm - cb);
+          float x[32];
+#pragma unroll
+          for (int e = 0; e < 32; e++) {
+            x[e] = __uint_as_float(v[e]);
+            if (totsig > 0.f || iscale) x[e] *= scale;
+            if (skyv > 0.f) x[e] += skyv;
+            if (skyA && e < n) x[e] += skyA[cb + e];
+          }
+          if (vecOut) {  // n is a multiple of 4 here
+#pragma unroll
+            for (int e = 0; e < 32; e += 4)
+              if (e < n) *reinterpret_cast<float4*>(out + cb + e) = make_float4(x[e], x[e + 1], x[e + 2], x[e + 3]);
+          } else {
+#pragma unroll
+            for (int e = 0; e < 32; e++)
+              if (e < n) out[cb + e] = x[e];
+          }
+        }
+        tc::fence_before_sync();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&bars.d2free);
+      };
+
+      // one output chunk of the current tile: |F|^2 of the 32 complex
+      // outputs in columns 64h .. 64h+63 of this row -> the GEMM2 operand
+      auto chunk = [&](float isc) {
+        const uint32_t buf = gC & 1;
+        wait(&bars.d1full[buf], (gC >> 1) & 1);
+        tc::fence_after_sync();
+        float I[32];
+#pragma unroll
+        for (int hp = 0; hp < 2; hp++) {
+          uint32_t v[32];
+          tc::tmem_ld32(tmem + buf * 128 + lanebase + h * 64 + hp * 32, v);
+          tc::tmem_ld_wait();
+#pragma unroll
+          for (int e = 0; e < 16; e++) {
+            const float re = __uint_as_float(v[2 * e]), im = __uint_as_float(v[2 * e + 1]);
+            I[hp * 16 + e] = (re * re + im * im) * isc;
+          }
+        }
+        tc::fence_before_sync();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&bars.d1free[buf]);
+        // A2 is free once the previous chunk's GEMM2 has completed
+        const uint32_t ab = g.dbA2 ? (gA & 1) : 0;
+        if (g.dbA2) {
+          if (gA >= 2) wait(&bars.a2free[ab], ((gA >> 1) - 1) & 1);
+        } else if (gA >= 1) {
+          wait(&bars.a2free[0], (gA - 1) & 1);
+        }
+        uint8_t* Ahi = A2hi + (size_t)ab * L.a2Half * (SPLIT ? 2 : 1);
+        uint8_t* Alo = Ahi + L.a2Half;
+#pragma unroll
+        for (int k8 = 0; k8 < 4; k8++) {
+          float x8[8];
+#pragma unroll
+          for (int e = 0; e < 8; e++) x8[e] = I[k8 * 8 + e];
+          store8<FMT, SPLIT>(Ahi, Alo, kmaj(r, h * 32 + k8 * 8, ESZ, sbo2), x8);
+        }
+        tc::fence_async_smem();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&bars.a2full[ab]);
+        gC++;
+        gA++;
+      };
+
+      Row prev{false, 0, 0};
+      Row cur = row_of(0);
+      float isc = (iscale && cur.live) ? iscale[cur.sub] : 1.f;
+      for (int lt = 0; lt < myTiles; lt++) {
+        const Row next = row_of(lt + 1);
+        const float iscn = (iscale && next.live) ? iscale[next.sub] : 1.f;
+        for (int oc = 0; oc < g.noc; oc++) {
+          if (oc == 0 && lt >= 1) read_D2(lt - 1, prev);
+          chunk(isc);
+        }
+        prev = cur;
+        cur = next;
+        isc = iscn;
+      }
+      if (myTiles > 0) read_D2(myTiles - 1, prev);
     }
   }
   if (!ok) atomicOr(err, 2);

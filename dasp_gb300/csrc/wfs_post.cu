@@ -170,6 +170,195 @@ __global__ void __launch_bounds__(kPostThreads, 4) wfs_post_kernel(const WfsArgs
   }
 }
 
+constexpr int kSlotThreads = 256;
+constexpr int kSlotStages = 3;
+constexpr int kSlotMaxTS = 64;
+
+// The common configuration (window CoG or image only; no brightest-pixel
+// selection, fit or optical binning) over tiles of TS consecutive
+// subaperture slots of one frame: a tile's pixels are one contiguous range
+// of bimg, so its copies into shared memory depend on nothing but the tile
+// index and run kSlotStages - 1 tiles ahead (cp.async groups), whatever the
+// lit pattern.  Unlit slots are copied but neither drawn nor written.
+// RN (read noise on) and POIS (Poisson on) are compile-time so that each
+// pixel's stream is consumed along a fixed path.  Pixels and streams are
+// those of wfs_post_kernel (same images); the window CoG sums each window
+// row first (one thread per subaperture row), then the rows.
+template <bool RN, bool POIS>
+__global__ void __launch_bounds__(kSlotThreads, 4)
+    wfs_post_slots_kernel(const WfsArgs a, const PoisTab* __restrict__ tab) {
+  extern __shared__ __align__(16) float smem_post[];
+  __shared__ int s_nbright;
+  __shared__ int s_bright[kPostBright];
+  __shared__ float s_brightv[kPostBright];
+  const int tid = threadIdx.x;
+  const int m = a.m, mm = m * m, TS = a.TS;
+  const bool cw2d = a.centWeightDim == 2;
+  PoisTab* s_tab = reinterpret_cast<PoisTab*>(smem_post);
+  float* s_cw = smem_post + (POIS ? sizeof(PoisTab) / sizeof(float) : 0);
+  // per stage: TS*mm pixels, then TS each of totsig, frac, subflag
+  float* ring = s_cw + ((cw2d ? mm : 0) + 3) / 4 * 4;
+  const int stageFloats = (TS * mm + 3 * TS + 3) / 4 * 4;
+  float* s_part = ring + kSlotStages * stageFloats;  // CoG row sums: TS*ncen pairs
+  if constexpr (POIS) {
+    const int4* src = reinterpret_cast<const int4*>(tab);
+    int4* dst = reinterpret_cast<int4*>(s_tab);
+    for (int k = tid; k < (int)(sizeof(PoisTab) / sizeof(int4)); k += blockDim.x) dst[k] = src[k];
+  }
+  if (cw2d)
+    for (int k = tid; k < mm; k += blockDim.x) s_cw[k] = a.centWeight[k];
+
+  const int tpf = (a.nsubaps + TS - 1) / TS;  // tiles per frame
+  const long long ntiles = (long long)tpf * a.nframes;
+  const bool noise = a.mode & kNoiseCounter;
+  const float rn = a.readNoise;
+  const unsigned long long fbase = frame_base(a);
+  const bool vec = (mm & 3) == 0 && (a.bimgFrameStride & 3) == 0 && ((uintptr_t)a.bimg & 15) == 0;
+  const bool cents = a.imageOnly == 0 && !a.skipCents;
+
+  // copies of tile t (k-th of this CTA) into stage k % kSlotStages; one
+  // cp.async group per tile and thread, empty past the last tile
+  auto issue = [&](long long t, int k) {
+    if (t < ntiles) {
+      float* st = ring + (k % kSlotStages) * stageFloats;
+      const int f = (int)(t / tpf), s0 = (int)(t - (long long)f * tpf) * TS;
+      const int ns = min(TS, a.nsubaps - s0);
+      const float* src = a.bimg + (long long)f * a.bimgFrameStride + (long long)s0 * mm;
+      const int n = ns * mm;
+      if (vec) {
+        for (int c = tid; c < n / 4; c += blockDim.x)
+          asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(st + 4 * c)),
+                       "l"(src + 4 * c)
+                       : "memory");
+      } else {
+        for (int c = tid; c < n; c += blockDim.x)
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(st + c)),
+                       "l"(src + c)
+                       : "memory");
+      }
+      float* info = st + TS * mm;
+      for (int c = tid; c < 3 * ns; c += blockDim.x) {
+        const int which = c / ns, s = c - which * ns;
+        const void* g = which == 0 ? (const void*)(a.totsig + s0 + s)
+                                   : (which == 1 ? (const void*)(a.frac + s0 + s) : (const void*)(a.subflag + s0 + s));
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(info + which * TS + s)),
+                     "l"(g)
+                     : "memory");
+      }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+
+  long long t = blockIdx.x;
+  int k = 0;
+  for (int d = 0; d < kSlotStages - 1; d++) issue(t + (long long)d * gridDim.x, d);
+  const int ncen = a.ncen, sx0 = (m - ncen) / 2;
+  const float inv_nc = 1.0f / (float)ncen;
+  const float inv_mm = 1.0f / (float)mm;
+  for (; t < ntiles; t += gridDim.x, k++) {
+    __syncthreads();  // the stage about to be refilled has been consumed
+    issue(t + (long long)(kSlotStages - 1) * gridDim.x, k + kSlotStages - 1);
+    asm volatile("cp.async.wait_group %0;" ::"n"(kSlotStages - 1) : "memory");
+    if (tid == 0) s_nbright = 0;
+    __syncthreads();  // tile t is in shared memory
+    float* imgs = ring + (k % kSlotStages) * stageFloats;
+    const float* s_tot = imgs + TS * mm;
+    const float* s_frac = s_tot + TS;
+    const int* s_flag = reinterpret_cast<const int*>(s_frac + TS);
+    const int f = (int)(t / tpf), s0 = (int)(t - (long long)f * tpf) * TS;
+    const int ns = min(TS, a.nsubaps - s0);
+    float* dstF = a.bimg + (long long)f * a.bimgFrameStride + (long long)s0 * mm;
+    auto pflag = [&](int s) { return s_tot[s] > 0.f || a.sky * s_frac[s] > 0.f || a.skyArr; };
+    // noise, threshold and power of pixel w; bimg and the tile written
+    auto pixel = [&](int w, float v) {
+      const int s = div_small(w, mm, inv_mm), pix = w - s * mm;
+      if (noise) {
+        CounterStream st(a.seed, fbase + f, s0 + s, pix, 0);
+        float g = 0.f;
+        if constexpr (RN) g = normal_counter(st);
+        if constexpr (POIS) {
+          if (pflag(s)) v = poisson_counter_tab(st, v, *s_tab);
+        }
+        if constexpr (RN)
+          v += rn * g + a.readBg;
+        else
+          v += a.readBg;
+        v = threshold_px(v, a.floorv, a.threshType);
+      }
+      if (a.pxlPower == 2.f)
+        v = v * v;
+      else if (a.pxlPower != 1.f && a.pxlPower != 0.f)
+        v = powf(v, a.pxlPower);
+      dstF[w] = v;
+      imgs[w] = v;
+    };
+    for (int w = tid; w < ns * mm; w += blockDim.x) {
+      const int s = div_small(w, mm, inv_mm);
+      if (s_flag[s] != 1) continue;
+      const float v = imgs[w];
+      if constexpr (POIS) {
+        // lambda >= 64 (the rejection sampler): queued and drawn after the
+        // others by the whole CTA, so that one such pixel does not hold
+        // the other lanes of its warp (same streams, same draws)
+        if (noise && v >= kModalMaxLam && pflag(s)) {
+          const int slot = atomicAdd(&s_nbright, 1);
+          if (slot < kPostBright) {
+            s_bright[slot] = w;
+            s_brightv[slot] = v;
+            continue;
+          }
+        }
+      }
+      pixel(w, v);
+    }
+    if constexpr (POIS) {
+      __syncthreads();
+      const int nb = min(s_nbright, kPostBright);
+      for (int b = tid; b < nb; b += blockDim.x) pixel(s_bright[b], s_brightv[b]);
+    }
+    if (!cents) continue;
+    __syncthreads();
+    // centred-window CoG: sums of each window row (one thread per
+    // subaperture row), then of the rows (one thread per subaperture)
+    for (int pr = tid; pr < ns * ncen; pr += blockDim.x) {
+      const int s = div_small(pr, ncen, inv_nc), rr = pr - s * ncen;
+      float ps = 0.f, px = 0.f;
+      if (s_flag[s] == 1) {
+        const int r = sx0 + rr;
+        const float* row = imgs + s * mm + r * m + sx0;
+        const float* wrow = cw2d ? s_cw + r * m + sx0
+                                 : (a.centWeightDim == 4 ? a.centWeight + (long long)(s0 + s) * mm + r * m + sx0 : nullptr);
+        for (int c = 0; c < ncen; c++) {
+          float v = row[c];
+          if (wrow) v *= wrow[c];
+          ps += v;
+          px += v * (float)(sx0 + c);
+        }
+      }
+      s_part[2 * pr] = ps;
+      s_part[2 * pr + 1] = px;
+    }
+    __syncthreads();
+    for (int s = tid; s < ns; s += blockDim.x) {
+      if (s_flag[s] != 1) continue;
+      float sum = 0.f, sxv = 0.f, syv = 0.f;
+      for (int rr = 0; rr < ncen; rr++) {
+        const float ps = s_part[2 * (s * ncen + rr)];
+        sum += ps;
+        sxv += s_part[2 * (s * ncen + rr) + 1];
+        syv += ps * (float)(sx0 + rr);
+      }
+      float cx = 0.f, cy = 0.f;
+      if (sum > 0.f) {
+        cx = sxv / sum - 0.5f * (float)(m - 1);
+        cy = syv / sum - 0.5f * (float)(m - 1);
+      }
+      calibrate_and_store(a, s0 + s, f, cx, cy);
+    }
+  }
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
 }  // namespace
 
 cudaError_t launch_post(const WfsArgs& a0, int numSMs, cudaStream_t stream) {
@@ -183,6 +372,35 @@ cudaError_t launch_post(const WfsArgs& a0, int numSMs, cudaStream_t stream) {
   if (pois) {
     cudaError_t et = pois_table_device(&tab);
     if (et != cudaSuccess) return et;
+  }
+  const bool simple = !(a.calsource == 0 && (a.useBrightest != 0 || a.useBrightestArr)) && a.opticalBinning != 1 &&
+                      a.fitSize == 0 && a.gaussianFit <= 0 && a.cob == 0;
+  const int tabB = pois ? (int)sizeof(PoisTab) : 0;
+  const int cwB = ((a.centWeightDim == 2 ? mm : 0) + 3) / 4 * 16;
+  const int perSlot = (kSlotStages * (mm + 3) + 2 * a.ncen) * (int)sizeof(float);
+  if (simple && a.subflag && tabB + cwB + 2 * perSlot <= 160 * 1024) {
+    // slot tiles: kSlotStages stages of TS slots, sized for four CTAs per SM
+    const int budget = (227 * 1024) / 4 - 1024 - 4 * kPostBright * 2 - tabB - cwB;
+    int ts = budget / perSlot - 1;
+    ts = ts < 1 ? 1 : (ts > kSlotMaxTS ? kSlotMaxTS : ts);
+    a.TS = ts;
+    const int stageFloats = (ts * mm + 3 * ts + 3) / 4 * 4;
+    const int smem = tabB + cwB + (kSlotStages * stageFloats + 2 * ts * a.ncen) * (int)sizeof(float);
+    const bool rnOn = a.calsource == 0 && a.readNoise != 0.f;
+    auto kern = pois ? (rnOn ? wfs_post_slots_kernel<true, true> : wfs_post_slots_kernel<false, true>)
+                     : (rnOn ? wfs_post_slots_kernel<true, false> : wfs_post_slots_kernel<false, false>);
+    if (a.calsource != 0) a.readNoise = 0.f;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    int ctas = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctas, kern, kSlotThreads, smem);
+    if (e != cudaSuccess) return e;
+    if (ctas < 1) return cudaErrorInvalidConfiguration;
+    const long long ntiles = (long long)((a.nsubaps + ts - 1) / ts) * a.nframes;
+    const long long cap = (long long)numSMs * ctas;
+    const int grid = (int)(ntiles < cap ? ntiles : cap);
+    kern<<<grid, kSlotThreads, smem, stream>>>(a, pois ? tab : nullptr);
+    return cudaGetLastError();
   }
   const int smem = (a.TS * mm + (a.centWeightDim == 2 ? mm : 0)) * (int)sizeof(float) +
                    (pois ? (int)sizeof(PoisTab) : 0);

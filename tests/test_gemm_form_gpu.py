@@ -120,3 +120,27 @@ def test_counter_noise_matches_fp32_form_statistics():
     z = (x.mean(0) - clean)[sel] / np.sqrt((clean[sel] + 4.0) / x.shape[0])
     assert np.abs(z).mean() < 1.2
     eng.free()
+
+
+@pytest.mark.parametrize("form,tol_all,tol_bright", [("fp16", 0.9, 0.5), ("bf16x3", 0.99, 0.9)])
+def test_counter_noise_draws_match_fp32_form(form, tol_all, tol_bright):
+    """Each pixel draws from the same (seed, frame, subaperture, pixel)
+    stream in every form: with equal up to rounding pre-noise images, the
+    noisy images agree pixel for pixel except where the two means straddle a
+    sampler boundary.  sig 2e3 puts the spot cores above lambda 64 (PTRS)."""
+    c = Case(nsubx=8, p=8, N=16, sig=2e3, addPoisson=1, readnoise=2.0, noiseFloor=-1e9, threshType=1, seed=9)
+    lit = c.lit()
+    imgs = {}
+    for f in ("fp32", form):
+        eng = c.engine()
+        eng.set_form(f)
+        for _ in range(3):
+            eng.run(0)
+        imgs[f] = c.bimg.reshape(64, -1)[lit].copy()
+        eng.free()
+    same = np.mean(imgs["fp32"] == imgs[form])
+    assert same > tol_all, same
+    bright = imgs["fp32"] > 80
+    assert bright.sum() > 20
+    same_bright = np.mean(imgs["fp32"][bright] == imgs[form][bright])
+    assert same_bright > tol_bright, same_bright
