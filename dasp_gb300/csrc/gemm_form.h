@@ -34,6 +34,7 @@ struct GemmGeom {
   int NW, NK;  // ring stages for W2 and Kc chunks
   int dbE;     // 1: two field (GEMM1 A operand) buffers, the next tile's built during this one
   int dbA2;    // 1: two |F|^2 (GEMM2 A operand) buffers, alternating between output chunks
+  int nd1;     // D1 (GEMM1 accumulator) buffers in TMEM: 3 when N2 <= 128, else 2
   const uint8_t* w2;   // [noc][nkc] x {hi[, lo]} x [128 x KCB bytes], tensor-core smem order
   const uint8_t* kc2;  // [noc] x {hi[, lo]} x [N2 x 64 elements], tensor-core smem order
 };

@@ -240,14 +240,25 @@ struct PoisTab {
   uint8_t guide[kPoisTabL][kPoisGuide];
 };
 
-// Poisson(L), integer 0 <= L < 64, by guided inversion of u
+// Poisson(L), integer 0 <= L < 64, by guided inversion of u: the answer
+// (first k with C[k] >= u) lies between the guide entries of u's bucket and
+// the next one, found by bisection.  A linear walk from the guide entry
+// would take up to ~L steps in the two tail buckets (all of the lower tail
+// shares bucket 0), and one such lane holds its whole warp.
 __device__ __forceinline__ int poisson_table_int(const PoisTab& T, int L, float u) {
   if (L <= 0) return 0;
   const float* C = T.cdf + T.off[L];
-  const int n = T.len[L];
-  int k = T.guide[L][(int)(u * (float)kPoisGuide)];
-  while (k < n - 1 && u > C[k]) k++;
-  return k;
+  const int j = (int)(u * (float)kPoisGuide);  // exact: u < 1, a power-of-two scale
+  int lo = T.guide[L][j];
+  int hi = j + 1 < kPoisGuide ? (int)T.guide[L][j + 1] : (int)T.len[L] - 1;  // C[hi] >= (j+1)/64 > u
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (C[mid] < u)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo;
 }
 
 __device__ __forceinline__ float poisson_tab(const PoisTab& T, float u3, float u4, float lam) {

@@ -60,11 +60,15 @@ namespace {
 constexpr int kConsumers = 512;
 constexpr int kEpiWarps = 8;    // warps 0-7: D1/D2 epilogue
 constexpr int kFieldWarps = 8;  // warps 8-15: field build
-constexpr int kGemmThreads = kConsumers + 64;
+constexpr int kGemmThreads = kConsumers + 96;  // + GEMM1 issuer, GEMM2 producer, W2 loader
 constexpr int kTileSubaps = 128;
 constexpr uint32_t kTmemCols = 512;
 constexpr long long kWaitCycles = 4000000000LL;  // about 2 s at the maximum SM clock
 constexpr uint32_t kLBO = 128;  // bytes between core matrices along K
+
+// TMEM columns: D1 buffers 0 and 1 at 0 and 128, D2 at 256 (N2 <= 256
+// columns), a third D1 buffer at 384 when N2 <= 128
+__device__ __forceinline__ uint32_t d1_col(int b) { return b == 2 ? 384u : (uint32_t)b * 128u; }
 
 // ---- element encodings (device) ----
 template <int FMT>
@@ -136,7 +140,7 @@ struct Bars {
   uint64_t wfull[kGemmMaxNW], wfree[kGemmMaxNW];
   uint64_t kfull[kGemmMaxNK], kfree[kGemmMaxNK];
   uint64_t efull[2], efree[2];  // per field buffer
-  uint64_t d1full[2], d1free[2];
+  uint64_t d1full[3], d1free[3];  // per D1 buffer (two or three)
   uint64_t a2full[2], a2free[2];  // per GEMM2 operand buffer
   uint64_t d2full, d2free;
 };
@@ -183,7 +187,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       tc::mbar_init(&bars.efull[i], kFieldWarps);
       tc::mbar_init(&bars.efree[i], 1);
     }
-    for (int i = 0; i < 2; i++) {
+    for (int i = 0; i < 3; i++) {
       tc::mbar_init(&bars.d1full[i], 1);
       tc::mbar_init(&bars.d1free[i], kEpiWarps);
     }
@@ -209,27 +213,15 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   const int myTiles = blockIdx.x < ntiles ? (int)((ntiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
 
   if (warp == kConsumers / 32) {
-    // ================= GEMM1 producer =================
+    // ================= GEMM1 producer (MMA issue only) =================
     // The whole warp runs the loop (so that counters and descriptors stay
-    // warp-uniform); lane 0 issues the single-thread operations (bulk copies,
-    // MMAs, commits).  Ring bookkeeping without divisions: chunk gJ sits in
-    // stage cs with phase bit cph; the previous chunk's stage/phase are
-    // ps/pph; lseq is the W2 chunk (mod nseq) of the next load.
+    // warp-uniform); lane 0 issues the MMAs and commits.  W2 chunk gJ sits
+    // in ring stage cs with phase bit cph (the loader warp fills the ring);
+    // output chunk gC goes to D1 buffer d1b in round d1r.
     if (myTiles > 0) {
       const bool leader = lane == 0;
-      const int totalJ = myTiles * nseq;
       constexpr uint32_t idesc1 = tc::idesc_f32acc(FMT, 128, 128);
       const uint32_t wbase = tc::smem_addr(smem + L.w);
-      int nextLoad = 0, lseq = 0;
-      auto wload = [&](int s) {  // chunk lseq -> stage s
-        if (leader) {
-          tc::mbar_expect_tx(&bars.wfull[s], L.wStage);
-          tc::bulk_g2s(smem + L.w + (size_t)s * L.wStage, g.w2 + (size_t)lseq * L.wStage, L.wStage, &bars.wfull[s]);
-        }
-        nextLoad++;
-        if (++lseq == nseq) lseq = 0;
-      };
-      for (int s0 = 0; s0 < g.NW && nextLoad < totalJ; s0++) wload(s0);
       // descriptors: the 14-bit start-address field (bits 0-13, in 16-byte
       // units) advances by 16 per k-step of 256 bytes; all addresses < 256 KB
       // field buffer of tile lt: (lt & 1) when double buffered
@@ -238,10 +230,10 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       const uint64_t dEstep = (uint64_t)((L.a1Half * (SPLIT ? 2u : 1u)) >> 4);
       const uint64_t dW0 = tc::smem_desc(wbase, kLBO, sboW);
       const uint64_t dWstage = (uint64_t)(L.wStage >> 4), dWlo = (uint64_t)(L.wHalf >> 4);
-      int cs = 0, ps = 0;
-      uint32_t cph = 0, pph = 0;
-      bool first = true;
-      uint32_t gC = 0;
+      int cs = 0;
+      uint32_t cph = 0;
+      int d1b = 0;
+      uint32_t d1r = 0;
       for (int lt = 0; lt < myTiles; lt++) {
         // field buffer eb; its uses alternate when double buffered
         const int eb = g.dbE ? (lt & 1) : 0;
@@ -249,11 +241,10 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         tc::fence_after_sync();
         const uint64_t dEh = dEh0 + (eb ? dEstep : 0);
         const uint64_t dEl = dEl0 + (eb ? dEstep : 0);
-        for (int oc = 0; oc < g.noc; oc++, gC++) {
-          const uint32_t buf = gC & 1;
-          if (gC >= 2) wait(&bars.d1free[buf], ((gC >> 1) - 1) & 1);
+        for (int oc = 0; oc < g.noc; oc++) {
+          if (d1r > 0) wait(&bars.d1free[d1b], (d1r - 1) & 1);
           tc::fence_after_sync();
-          const uint32_t dcol = tmem + buf * 128;
+          const uint32_t dcol = tmem + d1_col(d1b);
           int ks = 0;
           for (int kc = 0; kc < g.nkc; kc++) {
             wait(&bars.wfull[cs], cph);
@@ -271,23 +262,40 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
               tc::mma_commit(&bars.wfree[cs]);
             }
             ks = ks1;
-            // refill the stage of the previous chunk (its MMAs were issued a
-            // chunk ago) while this chunk's MMAs stay queued
-            if (!first && nextLoad < totalJ) {
-              wait(&bars.wfree[ps], pph);
-              wload(ps);
-            }
-            first = false;
-            ps = cs;
-            pph = cph;
             if (++cs == g.NW) {
               cs = 0;
               cph ^= 1u;
             }
           }
-          if (leader) tc::mma_commit(&bars.d1full[buf]);
+          if (leader) tc::mma_commit(&bars.d1full[d1b]);
+          if (++d1b == g.nd1) {
+            d1b = 0;
+            d1r++;
+          }
         }
         if (leader) tc::mma_commit(&bars.efree[eb]);
+      }
+    }
+    __syncwarp();
+  } else if (warp == kConsumers / 32 + 2) {
+    // ================= W2 loader =================
+    // refills each ring stage as soon as the MMAs that read it complete, so
+    // that the MMA issuer never waits on a copy it has to start itself
+    if (myTiles > 0) {
+      const int totalJ = myTiles * nseq;
+      int s = 0, lseq = 0;
+      uint32_t round = 0;
+      for (int J = 0; J < totalJ; J++) {
+        if (round > 0) wait(&bars.wfree[s], (round - 1) & 1);
+        if (lane == 0) {
+          tc::mbar_expect_tx(&bars.wfull[s], L.wStage);
+          tc::bulk_g2s(smem + L.w + (size_t)s * L.wStage, g.w2 + (size_t)lseq * L.wStage, L.wStage, &bars.wfull[s]);
+        }
+        if (++lseq == nseq) lseq = 0;
+        if (++s == g.NW) {
+          s = 0;
+          round++;
+        }
       }
     }
     __syncwarp();
@@ -484,7 +492,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       }
     } else {
       // ---- epilogue ----
-      uint32_t gC = 0, gA = 0;
+      int d1b = 0;
+      uint32_t d1r = 0, gA = 0;
       // binned image of tile lt (row P) from D2: normalise, sky -> bimg
       auto read_D2 = [&](int lt, const Row& P) {
         const int i = P.sub;
@@ -530,24 +539,31 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       // one output chunk of the current tile: |F|^2 of the 32 complex
       // outputs in columns 64h .. 64h+63 of this row -> the GEMM2 operand
       auto chunk = [&](float isc) {
-        const uint32_t buf = gC & 1;
-        wait(&bars.d1full[buf], (gC >> 1) & 1);
+        wait(&bars.d1full[d1b], d1r & 1);
         tc::fence_after_sync();
         float I[32];
-#pragma unroll
-        for (int hp = 0; hp < 2; hp++) {
-          uint32_t v[32];
-          tc::tmem_ld32(tmem + buf * 128 + lanebase + h * 64 + hp * 32, v);
+        {
+          // both halves in flight before one wait
+          uint32_t v0[32], v1[32];
+          const uint32_t col = tmem + d1_col(d1b) + lanebase + h * 64;
+          tc::tmem_ld32(col, v0);
+          tc::tmem_ld32(col + 32, v1);
           tc::tmem_ld_wait();
 #pragma unroll
           for (int e = 0; e < 16; e++) {
-            const float re = __uint_as_float(v[2 * e]), im = __uint_as_float(v[2 * e + 1]);
-            I[hp * 16 + e] = (re * re + im * im) * isc;
+            I[e] = (__uint_as_float(v0[2 * e]) * __uint_as_float(v0[2 * e]) +
+                    __uint_as_float(v0[2 * e + 1]) * __uint_as_float(v0[2 * e + 1])) * isc;
+            I[16 + e] = (__uint_as_float(v1[2 * e]) * __uint_as_float(v1[2 * e]) +
+                         __uint_as_float(v1[2 * e + 1]) * __uint_as_float(v1[2 * e + 1])) * isc;
           }
         }
         tc::fence_before_sync();
         __syncwarp();
-        if (lane == 0) tc::mbar_arrive(&bars.d1free[buf]);
+        if (lane == 0) tc::mbar_arrive(&bars.d1free[d1b]);
+        if (++d1b == g.nd1) {
+          d1b = 0;
+          d1r++;
+        }
         // A2 is free once the previous chunk's GEMM2 has completed
         const uint32_t ab = g.dbA2 ? (gA & 1) : 0;
         if (g.dbA2) {
@@ -567,7 +583,6 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         tc::fence_async_smem();
         __syncwarp();
         if (lane == 0) tc::mbar_arrive(&bars.a2full[ab]);
-        gC++;
         gA++;
       };
 
@@ -678,6 +693,7 @@ bool gemm_geometry(const GemmSpec& sp, int fmt, int passes, GemmGeom* g) {
   g->passes = passes;
   g->K1 = K1;
   g->N2 = N2;
+  g->nd1 = N2 <= 128 ? 3 : 2;
   g->noc = (sp.c * sp.c + 63) / 64;
   // dynamic limit: 227 KB minus the kernel's static shared memory (< 2 KB)
   const uint32_t limit = 227 * 1024 - 4096;
