@@ -374,6 +374,214 @@ def run_serving(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- precision sweep
+
+PRECISION = dict(nsubx=40, Dtel=8.0, obs=0.2, L0=25.0, wavelength=500.0, cases=[(8, 16), (16, 32), (32, 64)],
+                 r0s=[0.05, 0.1, 0.2, 0.3], sig=1e4, psf_fwhm=1.5)
+
+
+def run_precision(args):
+    """Noiseless centroid error (mean/max px over lit subapertures) and
+    image-plane relative L2 error of every compute form against the float64
+    oracle, on a 40x40-subaperture WFS, phasesize 8/16/32 with fftsize
+    16/32/64 (2x padding, nimg = phasesize), r0 0.05-0.3 m on an 8 m pupil
+    (peak-to-valley phase up to a few hundred rad).  The oracle bounds the
+    sample: --precision-frames frames per (phasesize, r0) case."""
+    import torch
+    from dasp_gb300.centcmod import centcmod
+    from dasp_gb300.screens import gaussian_psf, von_karman_screen
+    from dasp_gb300.tel import Pupil
+    from oracle.shwfs_oracle import CentOracle
+    torch.cuda.set_device(0)
+    P = PRECISION
+    nsx = P["nsubx"]
+    FORMS = ("fp32", "tf32", "bf16", "fp16", "bf16x3")
+    codes = {"fp32": 0, "bf16": 1, "bf16x3": 2, "fp16": 3, "tf32": 4}
+    nfr = int(args.precision_frames)
+    out = []
+    t0 = time.time()
+    for p, N in P["cases"]:
+        m = p
+        npup = nsx * p
+        pup = Pupil(npup, npup / 2.0, npup / 2.0 * P["obs"])
+        psf = gaussian_psf(N, P["psf_fwhm"])
+        pupfn = pup.perSubap(nsx, 0)
+        subflag = pup.getSubapFlag(nsx, 0.5)
+        frac = (pup.getSubarea(nsx) / (p * p)).astype(np.float32)
+        lit = subflag.reshape(-1) == 1
+        # one screen per case; von Karman phase scales as r0^(-5/6), and the
+        # frames are flips/transposes/rolls of it
+        base = von_karman_screen(npup, P["Dtel"], P["r0s"][0], P["L0"], 500 + p, P["wavelength"])
+        rng = np.random.default_rng(p)
+        shapes = []
+        for f in range(nfr):
+            s_ = base[::-1] if rng.random() < 0.5 else base
+            s_ = s_.T if rng.random() < 0.5 else s_
+            shapes.append(np.roll(s_, (int(rng.integers(0, npup)), int(rng.integers(0, npup))), axis=(0, 1)))
+        for r0 in P["r0s"]:
+            scale = np.float32((P["r0s"][0] / r0) ** (5.0 / 6.0))
+            frames = [np.ascontiguousarray(sh * scale, dtype=np.float32) for sh in shapes]
+            pv = float(max(fr.max() - fr.min() for fr in frames))
+            orc = CentOracle(nsubx=nsx, phasesize=p, fftsize=N, clipsize=N, nimg=m, ncen=m, pupfn=pupfn,
+                             subflag=subflag, fracSubArea=frac, sig=P["sig"], spotpsf=psf, mode="f64")
+            ref = []
+            for fr in frames:
+                c = np.zeros(nsx * nsx * 2, np.float32)
+                b = np.zeros((nsx * nsx, m, m), np.float32)
+                orc.run(np.ascontiguousarray(fr), c, b)
+                ref.append((c.reshape(-1, 2)[lit].astype(np.float64), b.reshape(nsx * nsx, -1)[lit].astype(np.float64)))
+            hp = np.ascontiguousarray(frames[0])
+            hc = np.zeros(nsx * nsx * 2, np.float32)
+            hb = np.zeros((nsx, nsx, m, m), np.float32)
+            eng = centcmod(1, nsx, m, N, N, m, p, 0.0, 0.0, 0, 0.0, P["sig"], 0.0, 0, 1.0, 1, 0, 1, hp, pup, psf,
+                           hc, hb, 0.5, 0, None, 0, 0.0, None, None, 0, 0, 0, 1, 0, None)
+            case = {"phasesize": p, "fftsize": N, "nimg": m, "r0_m": r0, "phase_pv_rad": round(pv, 1),
+                    "frames": nfr, "lit_subaps": int(lit.sum()), "forms": {}}
+            for form in FORMS:
+                eng.set_form(form)
+                if eng.info()["form_active"] != codes[form]:
+                    case["forms"][form] = {"active": False, "note": "geometry outside the tensor-core limits; FP32 form runs"}
+                    continue
+                errs, l2 = [], []
+                for fr, (rc, rb) in zip(frames, ref):
+                    hp[...] = fr
+                    eng.run(0)
+                    ec = hc.reshape(-1, 2)[lit].astype(np.float64)
+                    eb = hb.reshape(nsx * nsx, -1)[lit].astype(np.float64)
+                    errs.append(np.abs(ec - rc).ravel())
+                    l2.append(np.linalg.norm(eb - rb) / np.linalg.norm(rb))
+                e = np.concatenate(errs)
+                case["forms"][form] = {"active": True, "mean_err_px": float(e.mean()), "max_err_px": float(e.max()),
+                                       "img_rel_l2": float(np.mean(l2))}
+            eng.free()
+            out.append(case)
+            print(json.dumps({"case": case}), file=sys.stderr, flush=True)
+    worst = {f: max((c["forms"][f]["max_err_px"] for c in out if c["forms"][f].get("active")), default=None)
+             for f in FORMS}
+    line = {
+        "metric": "precision sweep: max centroid error vs FP64 oracle (px), noiseless, 40x40 subaps",
+        "value": worst["fp16"], "unit": "px", "n_gpus": 1, "steps": len(out) * nfr, "warmup": 0,
+        "ms_per_step": None, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "per form (fp32, tf32, bf16, fp16 with per-subaperture scaling, bf16x3)",
+        "data": "synthetic: seeded von Karman screens (r0 %s m at 500 nm, L0 %g m, %g m pupil)"
+                % (P["r0s"], P["L0"], P["Dtel"]),
+        "config": {"workload": "precision_sweep_40x40", "nsubx": nsx, "cases": P["cases"], "r0_m": P["r0s"],
+                   "frames_per_case": nfr, "note": "frames bounded by the float64 oracle's CPU time"},
+        "max_err_px_by_form": worst, "cases": out, "wall_s": round(time.time() - t0, 1),
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- batched multi-WFS step
+
+LGS_BATCH = dict(lgs=dict(count=6, nsubx=74, p=10, N=32, m=16, Dtel=39.0, obs=0.28),
+                 ngs=[dict(nsubx=8, p=8, N=16, m=8), dict(nsubx=16, p=16, N=32, m=16),
+                      dict(nsubx=24, p=32, N=64, m=16)])
+
+
+def run_lgs_batch(args):
+    """Batched uneven multi-WFS tomography step: 6 LGS WFS at 74x74 (p 10,
+    fftsize 32, nimg 16, per-subaperture 32x32 elongated spots) and 3 NGS at
+    8x8, 16x16, 24x24, all captured into one CUDA graph (one branch per WFS,
+    the FP32 kernels' tiles picked by the autotuner) and replayed once per
+    step; the same WFSs run one after another on one stream for comparison.
+    NGS sensors run BF16x3 where the tensor-core geometry allows, LGS
+    sensors (per-subaperture PSFs) the FP32 form.  L2 is flushed between
+    timed steps."""
+    import torch
+    from dasp_gb300.batch import WfsBatch
+    from dasp_gb300.centcmod import centcmod
+    from dasp_gb300.screens import gaussian_psf, lgs_psfs, von_karman_screen
+    from dasp_gb300.tel import Pupil
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(21)
+    specs = []
+    L = LGS_BATCH["lgs"]
+    for k in range(L["count"]):
+        specs.append(dict(L, lgs=True, sig=float(rng.uniform(300, 2000)), rn=float(rng.uniform(1, 3)),
+                          theta=60.0 * k, seed=300 + k))
+    for k, n in enumerate(LGS_BATCH["ngs"]):
+        specs.append(dict(n, lgs=False, Dtel=n["nsubx"] * 0.5, obs=0.2, sig=float(rng.uniform(300, 2000)),
+                          rn=float(rng.uniform(1, 3)), seed=400 + k))
+    engines, lit, forms, tensors = [], 0, [], []
+    screens = {}
+    for sp in specs:
+        nsx, p, N, m = sp["nsubx"], sp["p"], sp["N"], sp["m"]
+        npup = nsx * p
+        pup = Pupil(npup, npup / 2.0, npup / 2.0 * sp["obs"])
+        if sp["lgs"]:
+            frac = pup.getSubarea(nsx) / (p * p)
+            psf = lgs_psfs(nsx, N, 1.2, 6.0, launch_theta_deg=sp["theta"], subap_area=frac)
+        else:
+            psf = gaussian_psf(N, 1.5)
+        key = (npup, sp["Dtel"])
+        if key not in screens:
+            screens[key] = von_karman_screen(npup, sp["Dtel"], 0.157, 25.0, 900 + npup, 589.0)
+        ph = np.ascontiguousarray(np.roll(screens[key], 37 * sp["seed"], axis=0))
+        hc = np.zeros(nsx * nsx * 2, np.float32)
+        hb = np.zeros((nsx, nsx, m, m), np.float32)
+        eng = centcmod(1, nsx, m, N, N, m, p, sp["rn"], 0.0, 1, 2 * sp["rn"], sp["sig"], 5.0, 0, 1.0, 1, 0,
+                       sp["seed"], ph, pup, psf, hc, hb, 0.5, 0, None, 0, 0.0, None, None, 0, 0, 0, 1, 0, None)
+        if not sp["lgs"]:
+            eng.set_form("bf16x3")
+        if eng.info()["form_active"] == 0:
+            eng.autotune()
+        dp = torch.from_numpy(ph).cuda()
+        dc = torch.zeros(nsx * nsx * 2, device="cuda")
+        db = torch.zeros((nsx * nsx, m, m), device="cuda")
+        eng.set_io(dp, dc, db)
+        tensors.append((dp, dc, db))
+        engines.append(eng)
+        lit += eng.info()["nlit"]
+        forms.append({0: "fp32", 1: "bf16", 2: "bf16x3", 3: "fp16", 4: "tf32"}[eng.info()["form_active"]])
+    batch = WfsBatch(engines)
+    stream = torch.cuda.Stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1)  # L2 flush, outside the timed events
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                fn()
+                b.record(stream)
+            stream.synchronize()
+            ts.append(a.elapsed_time(b))
+        return float(np.median(ts)), float(np.mean(ts))
+
+    def run_graph():
+        batch.run(stream)
+
+    def run_seq():
+        for eng, (dp, dc, db) in zip(engines, tensors):
+            eng.run_batch(dp.unsqueeze(0), dc.unsqueeze(0), db.unsqueeze(0), stream=stream)
+
+    with ClockSampler(0) as clk:
+        g_med, g_mean = timed(run_graph)
+        s_med, s_mean = timed(run_seq)
+    batch.free()
+    for e in engines:
+        e.free()
+    line = {
+        "metric": "batched multi-WFS step: subap-frames/s (6 LGS 74x74 + 3 NGS, one CUDA graph)",
+        "value": lit / (g_med / 1e3), "unit": "subap-frames/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": g_med, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "per WFS: " + ", ".join(forms),
+        "data": "synthetic: seeded von Karman screens, elongated LGS and Gaussian NGS spots",
+        "config": {"workload": "lgs_batch_6x74_3ngs", "wfs": [{k: v for k, v in sp.items() if k != "obs"} for sp in specs],
+                   "lit_subaps_per_step": lit, "l2": "flushed between timed steps (256 MB write, untimed)"},
+        "sequential_ms_per_step": s_med, "graph_speedup_vs_sequential": s_med / g_med,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------------- our arm
 
 def main():
@@ -385,17 +593,20 @@ def main():
     ap.add_argument("--frames", type=int, default=FPSTEP, help="frames per step")
     ap.add_argument("--e2e-frames", type=int, default=400)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="ngs74", choices=["ngs74", "serving"],
-                    help="ngs74: the headline 74x74 NGS sensor; serving: 64 AO systems through the serving loop")
+    ap.add_argument("--workload", default="ngs74", choices=["ngs74", "serving", "precision", "lgs_batch"],
+                    help="ngs74: the headline 74x74 NGS sensor; serving: 64 AO systems through the serving loop; "
+                         "precision: per-form centroid error sweep vs the float64 oracle; "
+                         "lgs_batch: 6 LGS + 3 NGS sensors in one CUDA graph")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
+    ap.add_argument("--precision-frames", type=int, default=8)
     ap.add_argument("--serve-inflight", type=int, default=16)
     args = ap.parse_args()
     ws, rank, local = dist_env()
-    if args.workload == "serving" and args.impl == "ours":
+    if args.workload in ("serving", "precision", "lgs_batch") and args.impl == "ours":
         if rank == 0:
             from dasp_gb300 import build
             build.build()
-            run_serving(args)
+            {"serving": run_serving, "precision": run_precision, "lgs_batch": run_lgs_batch}[args.workload](args)
         return
 
     if args.impl == "reference":

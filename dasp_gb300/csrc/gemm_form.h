@@ -37,6 +37,7 @@ struct GemmGeom {
   int nd1;     // D1 (GEMM1 accumulator) buffers in TMEM: 3 when N2 <= 128, else 2
   const uint8_t* w2;   // [noc][nkc] x {hi[, lo]} x [128 x KCB bytes], tensor-core smem order
   const uint8_t* kc2;  // [noc] x {hi[, lo]} x [N2 x 64 elements], tensor-core smem order
+  const float* pupT;   // pupil by pixel group: [ppr/8][nlit][8], lit order
 };
 
 // dynamic shared-memory layout (byte offsets)

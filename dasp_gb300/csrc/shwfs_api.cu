@@ -153,6 +153,7 @@ struct shwfs_handle {
   GemmGeom gemm{};
   DevBuf<uint8_t> d_w2, d_kc2;
   DevBuf<float> d_iscale;  // fp16 form: 1 / (sum of the subaperture's pupil)^2
+  DevBuf<float> d_pupT;    // tensor-core forms: pupil by pixel group [ppr/8][nlit][8]
   cudaEvent_t splitEvent = nullptr;  // recorded between image formation and post stages
   const PoisTab* poisTab = nullptr;  // Poisson CDF tables on this device
   // correlation centroiding: pattern (host copy), its size, the per-mode
@@ -640,6 +641,7 @@ WfsArgs make_args(shwfs_handle* h, const float* phs, float* cents, float* bimg, 
   a.centsFrameStride = (long long)h->nsubaps * 2;
   a.poisFlag = h->d_poisFlag.p;
   a.seed = h->seed;
+  set_philox_keys(a);
   a.frame0 = h->framesRead;
   a.frameCtr = h->graphCtr;
   a.poisTab = h->poisTab;
@@ -699,6 +701,20 @@ shwfs_status build_gemm(shwfs_handle* h) {
       if (s > 0) isc[i] = (float)(1.0 / (s * s));
     }
     CK(h->d_iscale.upload(isc.data(), isc.size()));
+  }
+  {
+    // pupil of the lit subapertures grouped by 8 pixels, so that the field
+    // warps' loads (one lit subaperture per lane) are contiguous
+    const int pp = h->phasesize * h->phasesize, ng8 = ((pp + 7) & ~7) / 8;
+    const size_t nl = h->lit.size();
+    std::vector<float> pt((size_t)ng8 * nl * 8, 0.f);
+    for (int gi = 0; gi < ng8; gi++)
+      for (size_t li = 0; li < nl; li++)
+        for (int e = 0; e < 8; e++) {
+          const int k = gi * 8 + e;
+          if (k < pp) pt[((size_t)gi * nl + li) * 8 + e] = h->pup[(size_t)h->lit[li] * pp + k];
+        }
+    if (!pt.empty()) CK(h->d_pupT.upload(pt.data(), pt.size()));
   }
   h->gemm = g;
   h->gemmBuilt = true;
@@ -790,6 +806,7 @@ shwfs_status enqueue_readout(shwfs_handle* h, const float* phs, float* cents, fl
       GemmGeom g = h->gemm;
       g.w2 = h->d_w2.p;
       g.kc2 = h->d_kc2.p;
+      g.pupT = h->d_pupT.p;
       CK(launch_gemm(a, g, g.fmt == kFmtFP16 ? h->d_iscale.p : nullptr, h->numSMs, h->d_status.p, st));
       if (h->splitEvent) CK(cudaEventRecord(h->splitEvent, st));
       a.mode = kNoiseCounter | kPost;
@@ -1725,7 +1742,7 @@ int64_t engine_device_bytes(const shwfs_handle* h) {
   add(h->d_binLo); add(h->d_binHi); add(h->d_ubArr); add(h->d_calBounds); add(h->d_subflag);
   add(h->d_subapStart); add(h->d_status); add(h->d_psfSpec); add(h->d_phs); add(h->d_cents); add(h->d_bimg);
   add(h->d_image); add(h->d_subapLoc); add(h->d_poisFlag); add(h->d_rng); add(h->d_w2); add(h->d_kc2);
-  add(h->d_iscale); add(h->d_frameCtr);
+  add(h->d_iscale); add(h->d_pupT); add(h->d_frameCtr);
   return b;
 }
 

@@ -16,6 +16,13 @@ enum : int {
   kStorePreNoise = 8  // write the pre-noise image (and Poisson flag) to global memory
 };
 
+// Round keys of one seed, precomputed on the host: round r uses
+// (k0 + r*0x9E3779B9, k1 + r*0xBB67AE85), the schedule of philox4x32_10.
+// Kept in the kernel parameters, they are read as constant-bank operands.
+struct PhiloxKeys {
+  uint32_t k0[10], k1[10];
+};
+
 struct WfsArgs {
   // geometry
   int nsubx, nsubaps, p, N, C, m, ncen, P, padded, preBin;
@@ -68,6 +75,7 @@ struct WfsArgs {
   long long centsFrameStride;
   unsigned char* poisFlag;  // per subap: Poisson applies (reference-stream mode)
   unsigned long long seed;
+  PhiloxKeys philoxKeys;  // round keys of seed
   unsigned long long frame0;
   // when set (CUDA-graph replays), the noise frame index is read from this
   // device counter instead of frame0
@@ -79,6 +87,14 @@ struct WfsArgs {
   int skipCents;
   int mode;
 };
+
+// a.philoxKeys from a.seed (host side, after a.seed is set)
+inline void set_philox_keys(WfsArgs& a) {
+  for (int r = 0; r < 10; r++) {
+    a.philoxKeys.k0[r] = (uint32_t)a.seed + (uint32_t)r * 0x9E3779B9u;
+    a.philoxKeys.k1[r] = (uint32_t)(a.seed >> 32) + (uint32_t)r * 0xBB67AE85u;
+  }
+}
 
 __device__ __forceinline__ unsigned long long frame_base(const WfsArgs& a) {
   return a.frameCtr ? *a.frameCtr : a.frame0;
@@ -110,6 +126,21 @@ __device__ __forceinline__ U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
   return c;
 }
 
+__device__ __forceinline__ U4 philox4x32_10_rk(U4 c, const PhiloxKeys& K) {
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+    uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+    U4 n;
+    n.x = hi1 ^ c.y ^ K.k0[r];
+    n.y = lo1;
+    n.z = hi0 ^ c.w ^ K.k1[r];
+    n.w = lo0;
+    c = n;
+  }
+  return c;
+}
+
 // Sequential uniform stream for one (frame, subap, pixel, purpose).
 struct CounterStream {
   U4 ctr;
@@ -137,6 +168,38 @@ struct CounterStream {
     return v;
   }
   // uniform in (0, 1): 24 random bits, centred in their bin
+  __device__ __forceinline__ float uniform() {
+    return ((float)(next_u32() >> 8) + 0.5f) * (1.0f / 16777216.0f);
+  }
+};
+
+// The same stream as CounterStream(seed, ...), with the seed's round keys
+// taken from a PhiloxKeys block (kernel parameters) instead of computed
+// per block.
+struct KeyedStream {
+  const PhiloxKeys& keys;
+  U4 ctr;
+  U4 buf;
+  int avail;
+  __device__ __forceinline__ KeyedStream(const PhiloxKeys& k, unsigned long long frame, int subap, int pixel,
+                                         int purpose)
+      : keys(k) {
+    ctr.x = 0;
+    ctr.y = (uint32_t)pixel | ((uint32_t)purpose << 24);
+    ctr.z = (uint32_t)subap;
+    ctr.w = (uint32_t)frame;
+    avail = 0;
+  }
+  __device__ __forceinline__ uint32_t next_u32() {
+    if (avail == 0) {
+      buf = philox4x32_10_rk(ctr, keys);
+      ctr.x++;
+      avail = 4;
+    }
+    uint32_t v = avail == 4 ? buf.x : (avail == 3 ? buf.y : (avail == 2 ? buf.z : buf.w));
+    avail--;
+    return v;
+  }
   __device__ __forceinline__ float uniform() {
     return ((float)(next_u32() >> 8) + 0.5f) * (1.0f / 16777216.0f);
   }
@@ -282,7 +345,8 @@ __device__ __forceinline__ float poisson_tab(const PoisTab& T, float u3, float u
 // PTRS transformed rejection as in the reference (cmod/src/centmodule.c:
 // 722-758), whose quick-accept region grows with lambda.  Both draw from the
 // pixel's counter stream, so one Philox block usually suffices.
-__device__ __forceinline__ float poisson_counter(CounterStream& st, float lam) {
+template <class Stream>
+__device__ __forceinline__ float poisson_counter(Stream& st, float lam) {
   if (!(lam > 0.0f)) return 0.0f;
   if (lam < kModalMaxLam) return poisson_modal(st.uniform(), lam);
   const float slam = sqrtf(lam), loglam = __logf(lam);
@@ -311,7 +375,8 @@ cudaError_t pois_table_device(const PoisTab** out);
 // sampler (two uniforms, poisson_tab), above PTRS (poisson_counter).  (Summing
 // tabulated Poisson(63) parts for larger lambda is exact too, but measured
 // slower than PTRS from lambda 64 on.)
-__device__ __forceinline__ float poisson_counter_tab(CounterStream& st, float lam, const PoisTab& T) {
+template <class Stream>
+__device__ __forceinline__ float poisson_counter_tab(Stream& st, float lam, const PoisTab& T) {
   if (!(lam > 0.0f)) return 0.0f;
   if (lam < kModalMaxLam) {
     const float u3 = st.uniform(), u4 = st.uniform();
@@ -321,7 +386,8 @@ __device__ __forceinline__ float poisson_counter_tab(CounterStream& st, float la
 }
 
 // one standard normal deviate (Box-Muller, cosine branch)
-__device__ __forceinline__ float normal_counter(CounterStream& st) {
+template <class Stream>
+__device__ __forceinline__ float normal_counter(Stream& st) {
   const float u1 = st.uniform(), u2 = st.uniform();
   const float q = -2.0f * __logf(u1);  // > 0: u1 < 1
   const float r = q * rsqrtf(q);

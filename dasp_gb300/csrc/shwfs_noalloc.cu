@@ -150,6 +150,7 @@ extern "C" shwfs_status shwfs_image_centroids_noalloc(const shwfs_image_job* job
   a.readNoise = job->readNoise;
   a.readBg = job->readBg;
   a.seed = job->seed;
+  set_philox_keys(a);
   a.frame0 = job->frame;
   a.refCents = job->refCents;
   a.cents = job->cents;

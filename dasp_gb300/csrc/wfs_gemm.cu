@@ -23,7 +23,7 @@
 // subaperture by 1/(sum pup)^2 so that it stays far from the fp16 range
 // limit) and tf32 (one pass, kind::tf32).  Accumulation is always f32.
 //
-// Warp roles (576 threads):
+// Warp roles (608 threads):
 //   warps 0-7   epilogue: thread t owns MMA row r = t & 127 (its
 //               subaperture, TMEM lane) and column half t >> 7; reads D1 and
 //               writes |F|^2 into the GEMM2 operand, reads D2 and stores the
@@ -31,10 +31,13 @@
 //   warps 8-15  field build: E of the next tile (row r, every other pixel
 //               group), one tile ahead of GEMM1 when two field buffers fit,
 //               so that its global loads overlap the epilogue and the MMAs
-//   warp 16     GEMM1 producer: streams W2 chunks through an NW-stage ring
-//               with bulk asynchronous copies and issues the GEMM1 MMAs
+//   warp 16     GEMM1 issuer: the GEMM1 MMAs over the W2 ring, into two or
+//               three D1 accumulator buffers
 //   warp 17     GEMM2 producer: streams Kc chunks (NK-stage ring) and
 //               issues the GEMM2 MMAs
+//   warp 18     W2 loader: refills the NW-stage W2 ring with bulk
+//               asynchronous copies as soon as the MMAs reading a stage
+//               complete
 // All hand-offs are mbarriers (no block-wide barrier inside the tile loop);
 // every wait is bounded and a wait that runs out records an error for the
 // host instead of hanging.
@@ -376,16 +379,17 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
 
     struct Row {
       bool live;
-      int sub, frm;
+      int sub, frm, li;
     };
     // this thread's row (subaperture-frame) of tile lt
     auto row_of = [&](int lt) {
-      Row o{false, 0, 0};
+      Row o{false, 0, 0, 0};
       const long long w = (blockIdx.x + (long long)lt * gridDim.x) * kTileSubaps + r;
       if (lt < myTiles && w < nwork) {
         o.live = true;
         o.frm = (int)(w / a.nlit);
-        o.sub = a.lit[w % a.nlit];
+        o.li = (int)(w - (long long)o.frm * a.nlit);
+        o.sub = a.lit[o.li];
       }
       return o;
     };
@@ -397,7 +401,15 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       auto load_group = [&](const Row& R, const float* ph, const float* pu, int g8, float (&phv)[8],
                             float (&puv)[8]) {
         const int pix0 = g8 * 8;
-        if (R.live && vecPup && pix0 + 8 <= pp) {
+        if (R.live && g.pupT) {
+          // grouped copy: lanes (consecutive lit subapertures) read
+          // consecutive 32-byte entries; zero past the last pixel
+          const float* pt = g.pupT + ((long long)g8 * a.nlit + R.li) * 8;
+          const float4 u0 = *reinterpret_cast<const float4*>(pt);
+          const float4 u1 = *reinterpret_cast<const float4*>(pt + 4);
+          puv[0] = u0.x; puv[1] = u0.y; puv[2] = u0.z; puv[3] = u0.w;
+          puv[4] = u1.x; puv[5] = u1.y; puv[6] = u1.z; puv[7] = u1.w;
+        } else if (R.live && vecPup && pix0 + 8 <= pp) {
           const float4 u0 = *reinterpret_cast<const float4*>(pu + pix0);
           const float4 u1 = *reinterpret_cast<const float4*>(pu + pix0 + 4);
           puv[0] = u0.x; puv[1] = u0.y; puv[2] = u0.z; puv[3] = u0.w;
@@ -586,7 +598,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         gA++;
       };
 
-      Row prev{false, 0, 0};
+      Row prev{false, 0, 0, 0};
       Row cur = row_of(0);
       float isc = (iscale && cur.live) ? iscale[cur.sub] : 1.f;
       for (int lt = 0; lt < myTiles; lt++) {

@@ -10,7 +10,7 @@
 //
 // A separate launch rather than a stage of the tensor-core kernel: the noise
 // samplers are latency-bound scalar code that wants many resident warps,
-// while the tensor-core kernel holds one 576-thread CTA per SM.
+// while the tensor-core kernel holds one 608-thread CTA per SM.
 #include "gemm_form.h"
 #include "wfs_plain.cuh"
 
@@ -188,7 +188,7 @@ template <bool RN, bool POIS>
 __global__ void __launch_bounds__(kSlotThreads, 4)
     wfs_post_slots_kernel(const WfsArgs a, const PoisTab* __restrict__ tab) {
   extern __shared__ __align__(16) float smem_post[];
-  __shared__ int s_nbright;
+  __shared__ int s_nbright[2];  // bright-pixel queue length, alternating between tiles
   __shared__ int s_bright[kPostBright];
   __shared__ float s_brightv[kPostBright];
   const int tid = threadIdx.x;
@@ -252,15 +252,17 @@ __global__ void __launch_bounds__(kSlotThreads, 4)
   long long t = blockIdx.x;
   int k = 0;
   for (int d = 0; d < kSlotStages - 1; d++) issue(t + (long long)d * gridDim.x, d);
+  if (tid == 0) s_nbright[0] = s_nbright[1] = 0;
   const int ncen = a.ncen, sx0 = (m - ncen) / 2;
-  const float inv_nc = 1.0f / (float)ncen;
-  const float inv_mm = 1.0f / (float)mm;
+  const float inv_mm = 1.0f / (float)mm, inv_nc = 1.0f / (float)ncen;
   for (; t < ntiles; t += gridDim.x, k++) {
-    __syncthreads();  // the stage about to be refilled has been consumed
+    asm volatile("cp.async.wait_group %0;" ::"n"(kSlotStages - 2) : "memory");
+    // tile t is in shared memory and every thread is done with tile t - 1,
+    // whose stage is refilled next
+    __syncthreads();
     issue(t + (long long)(kSlotStages - 1) * gridDim.x, k + kSlotStages - 1);
-    asm volatile("cp.async.wait_group %0;" ::"n"(kSlotStages - 1) : "memory");
-    if (tid == 0) s_nbright = 0;
-    __syncthreads();  // tile t is in shared memory
+    if (tid == 0) s_nbright[(k + 1) & 1] = 0;  // the next tile's queue
+    int* nbright = &s_nbright[k & 1];
     float* imgs = ring + (k % kSlotStages) * stageFloats;
     const float* s_tot = imgs + TS * mm;
     const float* s_frac = s_tot + TS;
@@ -268,23 +270,21 @@ __global__ void __launch_bounds__(kSlotThreads, 4)
     const int f = (int)(t / tpf), s0 = (int)(t - (long long)f * tpf) * TS;
     const int ns = min(TS, a.nsubaps - s0);
     float* dstF = a.bimg + (long long)f * a.bimgFrameStride + (long long)s0 * mm;
-    auto pflag = [&](int s) { return s_tot[s] > 0.f || a.sky * s_frac[s] > 0.f || a.skyArr; };
-    // noise, threshold and power of pixel w; bimg and the tile written
-    auto pixel = [&](int w, float v) {
-      const int s = div_small(w, mm, inv_mm), pix = w - s * mm;
-      if (noise) {
-        CounterStream st(a.seed, fbase + f, s0 + s, pix, 0);
-        float g = 0.f;
-        if constexpr (RN) g = normal_counter(st);
-        if constexpr (POIS) {
-          if (pflag(s)) v = poisson_counter_tab(st, v, *s_tab);
-        }
-        if constexpr (RN)
-          v += rn * g + a.readBg;
-        else
-          v += a.readBg;
-        v = threshold_px(v, a.floorv, a.threshType);
+    // noise and threshold of pixel pix of slot s (pf: Poisson applies)
+    auto draw = [&](float v, int s, int pix, bool pf) {
+      KeyedStream st(a.philoxKeys, fbase + f, s0 + s, pix, 0);
+      float g = 0.f;
+      if constexpr (RN) g = normal_counter(st);
+      if constexpr (POIS) {
+        if (pf) v = poisson_counter_tab(st, v, *s_tab);
       }
+      if constexpr (RN)
+        v += rn * g + a.readBg;
+      else
+        v += a.readBg;
+      return threshold_px(v, a.floorv, a.threshType);
+    };
+    auto store = [&](int w, float v) {
       if (a.pxlPower == 2.f)
         v = v * v;
       else if (a.pxlPower != 1.f && a.pxlPower != 0.f)
@@ -295,26 +295,34 @@ __global__ void __launch_bounds__(kSlotThreads, 4)
     for (int w = tid; w < ns * mm; w += blockDim.x) {
       const int s = div_small(w, mm, inv_mm);
       if (s_flag[s] != 1) continue;
-      const float v = imgs[w];
-      if constexpr (POIS) {
-        // lambda >= 64 (the rejection sampler): queued and drawn after the
-        // others by the whole CTA, so that one such pixel does not hold
-        // the other lanes of its warp (same streams, same draws)
-        if (noise && v >= kModalMaxLam && pflag(s)) {
-          const int slot = atomicAdd(&s_nbright, 1);
+      float v = imgs[w];
+      if (noise) {
+        const bool pf = POIS && (s_tot[s] > 0.f || a.sky * s_frac[s] > 0.f || a.skyArr);
+        if (POIS && pf && v >= kModalMaxLam) {
+          // lambda >= 64 (the rejection sampler): queued and drawn after
+          // the others by the whole CTA, so that one such pixel does not
+          // hold the other lanes of its warp (same streams, same draws)
+          const int slot = atomicAdd(nbright, 1);
           if (slot < kPostBright) {
             s_bright[slot] = w;
             s_brightv[slot] = v;
             continue;
           }
         }
+        v = draw(v, s, w - s * mm, pf);
       }
-      pixel(w, v);
+      store(w, v);
     }
     if constexpr (POIS) {
-      __syncthreads();
-      const int nb = min(s_nbright, kPostBright);
-      for (int b = tid; b < nb; b += blockDim.x) pixel(s_bright[b], s_brightv[b]);
+      if (noise) {
+        __syncthreads();
+        const int nb = min(*nbright, kPostBright);
+        for (int b = tid; b < nb; b += blockDim.x) {
+          const int w = s_bright[b];
+          const int s = div_small(w, mm, inv_mm);
+          store(w, draw(s_brightv[b], s, w - s * mm, true));
+        }
+      }
     }
     if (!cents) continue;
     __syncthreads();
