@@ -430,7 +430,7 @@ def run_precision(args):
                 b = np.zeros((nsx * nsx, m, m), np.float32)
                 orc.run(np.ascontiguousarray(fr), c, b)
                 ref.append((c.reshape(-1, 2)[lit].astype(np.float64), b.reshape(nsx * nsx, -1)[lit].astype(np.float64)))
-            hp = np.ascontiguousarray(frames[0])
+            hp = frames[0].copy()  # the engine's bound phase buffer; frames stay intact
             hc = np.zeros(nsx * nsx * 2, np.float32)
             hb = np.zeros((nsx, nsx, m, m), np.float32)
             eng = centcmod(1, nsx, m, N, N, m, p, 0.0, 0.0, 0, 0.0, P["sig"], 0.0, 0, 1.0, 1, 0, 1, hp, pup, psf,
