@@ -1,4 +1,4 @@
-// Device copy of the Poisson CDF tables used by the tabulated sampler
+// Device copy of the Poisson alias tables used by the tabulated sampler
 // (poisson_tab in shwfs_dev.cuh), built on the host in double precision once
 // per device.
 #include <cuda_runtime.h>
@@ -17,32 +17,53 @@ __device__ PoisTab g_poistab;
 
 namespace {
 
+// Walker/Vose alias table of Poisson(L) over 0..n-1 into prob/alias[o..o+n)
+void alias_table(const std::vector<double>& P, float* prob, uint8_t* alias) {
+  const int n = (int)P.size();
+  std::vector<double> q(n);
+  std::vector<int> small, large;
+  for (int k = 0; k < n; k++) {
+    q[k] = P[k] * n;
+    (q[k] < 1.0 ? small : large).push_back(k);
+  }
+  for (int k = 0; k < n; k++) {
+    prob[k] = 1.0f;
+    alias[k] = (uint8_t)k;
+  }
+  while (!small.empty() && !large.empty()) {
+    const int l = small.back(), g = large.back();
+    small.pop_back();
+    large.pop_back();
+    prob[l] = (float)q[l];
+    alias[l] = (uint8_t)g;
+    q[g] = (q[g] + q[l]) - 1.0;
+    (q[g] < 1.0 ? small : large).push_back(g);
+  }
+  // what is left has q = 1 up to rounding: keeps its own column
+}
+
 bool build_host_table(PoisTab* t) {
   memset(t, 0, sizeof(*t));
   int pos = 0;
   t->off[0] = 0;
   t->len[0] = 1;
-  t->cdf[pos++] = 1.0f;  // Poisson(0) = 0
+  t->prob[pos] = 1.0f;  // Poisson(0) = 0
+  t->alias[pos++] = 0;
   for (int L = 1; L < kPoisTabL; L++) {
-    std::vector<float> C;
+    std::vector<double> P;
     double p = std::exp(-(double)L), c = p;
-    C.push_back((float)c);
-    for (int k = 1; 1.0 - c > 9.3e-10 && k < 400; k++) {  // tail below 2^-30
+    P.push_back(p);
+    for (int k = 1; 1.0 - c > 9.3e-10 && k < 255; k++) {  // upper tail below 2^-30
       p *= (double)L / k;
       c += p;
-      C.push_back((float)(c < 1.0 ? c : 1.0));
+      P.push_back(p);
     }
-    if (C.back() < 1.0f) C.push_back(1.0f);  // the search always ends inside the table
-    if (pos + (int)C.size() > kPoisCdfMax) return false;
+    P.back() += 1.0 - c;  // the last entry takes the remaining mass
+    if (pos + (int)P.size() > kPoisCdfMax || P.size() > 255) return false;
     t->off[L] = (uint16_t)pos;
-    t->len[L] = (uint16_t)C.size();
-    for (float v : C) t->cdf[pos++] = v;
-    for (int j = 0; j < kPoisGuide; j++) {
-      const float target = (float)j / (float)kPoisGuide;
-      int k = 0;
-      while (k < (int)C.size() - 1 && C[k] < target) k++;
-      t->guide[L][j] = (uint8_t)k;
-    }
+    t->len[L] = (uint16_t)P.size();
+    alias_table(P, t->prob + pos, t->alias + pos);
+    pos += (int)P.size();
   }
   return true;
 }

@@ -284,44 +284,35 @@ __device__ __forceinline__ float poisson_modal(float u, float lam) {
 
 // Tables for Poisson(lam) with lam < 64 as the sum of two independent parts,
 // Poisson(L) + Poisson(d), L = floor(lam), d = lam - L in [0, 1):
-//   Poisson(L): inversion of one uniform through the CDF of Poisson(L),
-//     tabulated for L = 1..63 (computed in double, rounded to float; each
-//     table runs until the CDF is 1 in float), starting from a 64-entry
-//     guide table (first k whose CDF reaches j/64);
-//   Poisson(d): inversion of a second uniform by sequential search from 0
-//     (at most a few steps for d < 1).
+//   Poisson(L): Walker's alias method (Walker 1977; table construction of
+//     Vose 1991) over the support 0..n_L-1 of Poisson(L), L = 1..63, built
+//     on the host in double (each support runs until the upper tail is
+//     below 2^-30, the last entry taking the remaining mass): one uniform u
+//     gives the column i = floor(u n_L) and, from its fractional part,
+//     either i or its alias -- two table reads, no search;
+//   Poisson(d): inversion of a second uniform, the first four CDF terms
+//     without branches, a short loop beyond them (probability < 2%).
 // The sum of independent Poisson variables is Poisson, so the draw is exact
-// up to float rounding of the tabulated CDF.  ~22 KB, staged into shared
-// memory by the kernels that use it.
+// up to the float rounding of the tables and the 2^-16 resolution of the
+// column fraction.  ~22 KB, staged into shared memory by the kernels that
+// use it.
 constexpr int kPoisTabL = 64;      // L = 0..63
-constexpr int kPoisGuide = 64;
-constexpr int kPoisCdfMax = 4480;  // >= sum of the table lengths
+constexpr int kPoisCdfMax = 4480;  // >= sum of the support lengths
 struct PoisTab {
-  float cdf[kPoisCdfMax];
+  float prob[kPoisCdfMax];   // probability of keeping the column itself
+  uint8_t alias[kPoisCdfMax];
   uint16_t off[kPoisTabL];
   uint16_t len[kPoisTabL];
-  uint8_t guide[kPoisTabL][kPoisGuide];
 };
 
-// Poisson(L), integer 0 <= L < 64, by guided inversion of u: the answer
-// (first k with C[k] >= u) lies between the guide entries of u's bucket and
-// the next one, found by bisection.  A linear walk from the guide entry
-// would take up to ~L steps in the two tail buckets (all of the lower tail
-// shares bucket 0), and one such lane holds its whole warp.
+// Poisson(L), integer 0 <= L < 64, by the alias method on u
 __device__ __forceinline__ int poisson_table_int(const PoisTab& T, int L, float u) {
   if (L <= 0) return 0;
-  const float* C = T.cdf + T.off[L];
-  const int j = (int)(u * (float)kPoisGuide);  // exact: u < 1, a power-of-two scale
-  int lo = T.guide[L][j];
-  int hi = j + 1 < kPoisGuide ? (int)T.guide[L][j + 1] : (int)T.len[L] - 1;  // C[hi] >= (j+1)/64 > u
-  while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if (C[mid] < u)
-      lo = mid + 1;
-    else
-      hi = mid;
-  }
-  return lo;
+  const int n = T.len[L], o = T.off[L];
+  const float x = u * (float)n;
+  int i = (int)x;
+  if (i > n - 1) i = n - 1;  // u n may round up to n
+  return x - (float)i < T.prob[o + i] ? i : (int)T.alias[o + i];
 }
 
 __device__ __forceinline__ float poisson_tab(const PoisTab& T, float u3, float u4, float lam) {
@@ -329,12 +320,25 @@ __device__ __forceinline__ float poisson_tab(const PoisTab& T, float u3, float u
   const float d = lam - (float)L;  // exact
   int k = poisson_table_int(T, L, u3);
   if (d > 0.0f) {
-    float p = __expf(-d), F = p;
-    int k2 = 0;
-    while (u4 > F && k2 < 40) {
-      k2++;
-      p *= __fdividef(d, (float)k2);
-      F += p;
+    // smallest j with u4 <= F_j, F_j the CDF of Poisson(d)
+    float t = __expf(-d), F = t;
+    int k2 = u4 > F ? 1 : 0;
+    t *= d;
+    F += t;
+    k2 += u4 > F ? 1 : 0;
+    t *= d * 0.5f;
+    F += t;
+    k2 += u4 > F ? 1 : 0;
+    t *= d * (1.0f / 3.0f);
+    F += t;
+    if (u4 > F) {
+      int j = 3;
+      while (u4 > F && j < 40) {
+        j++;
+        t *= __fdividef(d, (float)j);
+        F += t;
+      }
+      k2 = j;
     }
     k += k2;
   }
