@@ -170,7 +170,8 @@ __global__ void __launch_bounds__(kPostThreads, 4) wfs_post_kernel(const WfsArgs
   }
 }
 
-constexpr int kSlotThreads = 256;
+constexpr int kSlotThreads = 512;
+constexpr int kSlotCtasPerSM = 2;  // one copy of the Poisson tables per CTA
 constexpr int kSlotStages = 3;
 constexpr int kSlotMaxTS = 64;
 
@@ -185,7 +186,7 @@ constexpr int kSlotMaxTS = 64;
 // those of wfs_post_kernel (same images); the window CoG sums each window
 // row first (one thread per subaperture row), then the rows.
 template <bool RN, bool POIS>
-__global__ void __launch_bounds__(kSlotThreads, 4)
+__global__ void __launch_bounds__(kSlotThreads, kSlotCtasPerSM)
     wfs_post_slots_kernel(const WfsArgs a, const PoisTab* __restrict__ tab) {
   extern __shared__ __align__(16) float smem_post[];
   __shared__ int s_nbright[2];  // bright-pixel queue length, alternating between tiles
@@ -387,8 +388,8 @@ cudaError_t launch_post(const WfsArgs& a0, int numSMs, cudaStream_t stream) {
   const int cwB = ((a.centWeightDim == 2 ? mm : 0) + 3) / 4 * 16;
   const int perSlot = (kSlotStages * (mm + 3) + 2 * a.ncen) * (int)sizeof(float);
   if (simple && a.subflag && tabB + cwB + 2 * perSlot <= 160 * 1024) {
-    // slot tiles: kSlotStages stages of TS slots, sized for four CTAs per SM
-    const int budget = (227 * 1024) / 4 - 1024 - 4 * kPostBright * 2 - tabB - cwB;
+    // slot tiles: kSlotStages stages of TS slots, sized for kSlotCtasPerSM CTAs per SM
+    const int budget = (228 * 1024) / kSlotCtasPerSM - 1024 - 4 * kPostBright * 2 - 64 - tabB - cwB;
     int ts = budget / perSlot - 1;
     ts = ts < 1 ? 1 : (ts > kSlotMaxTS ? kSlotMaxTS : ts);
     a.TS = ts;
