@@ -82,6 +82,11 @@ def make_engine(pup, phs, cents, bimg, noiseless=False):
 
 # ---------------------------------------------------------------- algorithmic work
 
+# DRAM bytes (read + write) per launch of the 64-frame step, from one ncu
+# capture of each kernel (commands and figures in profiles/)
+NCU_TRAFFIC = {"wfs_gemm_kernel": 162.1e6, "wfs_post_slots_kernel": 189.6e6}
+
+
 def tensor_flops_per_subap():
     """Algorithmic tensor-core flops of one GEMM-DFT pass per lit subap-frame:
     2 (2c^2)(2p^2) for the cropped DFT plus 2 m^2 c^2 for the convolve+bin map
@@ -747,6 +752,7 @@ def main():
 
     F_alg, B_alg = algorithmic_per_subap()
     T_alg = tensor_flops_per_subap()
+    B_post = 8 * w["m"] * w["m"] + 8  # pre-noise image in, final image out, centroids out
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -790,13 +796,24 @@ def main():
         roof = {"bound": "hbm", "achieved": rl["hbm_gbs"], "peak": hbm_peak, "unit": "GB/s", "frac": rl["hbm_frac"],
                 "traffic": None, "peak_source": peak_src, "algorithmic_bytes_per_subap_frame": B_alg}
     else:
-        roof = {"bound": "tensor", "achieved": rl["tensor_tflops"], "peak": tensor_peak(head), "unit": "TFLOP/s",
-                "frac": rl["tensor_frac"], "traffic": None,
+        # the two kernels of the tensor-core form, each against its own
+        # roofline; "roofline" is the one that takes longer
+        gemm = {"bound": "tensor", "achieved": rl["tensor_tflops"], "peak": tensor_peak(head), "unit": "TFLOP/s",
+                "frac": rl["tensor_frac"], "traffic": NCU_TRAFFIC.get("wfs_gemm_kernel"),
                 "peak_source": peak_src + (" (bf16 burst / 2 for tf32)" if head == "tf32" else " (bf16 burst)"),
                 "algorithmic_flops_per_subap_frame": T_alg * PASSES.get(head, 1),
-                "kernel": "wfs_gemm_kernel (image formation); timed alone between engine-recorded events",
-                "formation_kernel_ms": rl["formation_kernel_ms"], "post_kernel_ms": rl["post_kernel_ms"],
-                "hbm_frac": rl["hbm_frac"]}
+                "kernel": "wfs_gemm_kernel (image formation); timed between engine-recorded events",
+                "kernel_ms": rl["formation_kernel_ms"]}
+        post_s = rl["post_kernel_ms"] / 1e3
+        post_gbs = B_post * units / post_s / 1e9
+        post = {"bound": "hbm", "achieved": post_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": post_gbs / hbm_peak,
+                "traffic": NCU_TRAFFIC.get("wfs_post_slots_kernel"), "peak_source": peak_src + " (copy bandwidth)",
+                "algorithmic_bytes_per_subap_frame": B_post,
+                "kernel": "wfs_post_slots_kernel (noise, threshold, centroids); timed between engine-recorded events",
+                "kernel_ms": rl["post_kernel_ms"],
+                "note": "issue-bound on the Philox/Poisson/normal samplers, far below its HBM roofline"}
+        roof = dict(post if rl["post_kernel_ms"] > rl["formation_kernel_ms"] else gemm)
+        roof["kernels"] = {"wfs_gemm_kernel": gemm, "wfs_post_slots_kernel": post}
     roof["step_ms_per_launch"] = per_launch_ms
     roof["units_per_launch"] = units
     line = {
