@@ -223,7 +223,9 @@ class centcmod:
         """what is one of the codes at the top of this module; val the new value.
 
         As in the reference this does not update the Python-side attributes.
-        Arrays passed here are copied into the engine at call time.
+        Arrays passed here are copied into the engine at call time, except the
+        OUTPUTPHASEARR array, which later runs write (as the reference's
+        interpolatedPhaseOutput).
         """
         keep: list = []
         v = ShwfsValue()
@@ -254,6 +256,8 @@ class centcmod:
         else:
             raise ValueError("unsupported update value of type %s" % type(val))
         check(_lib.lib().shwfs_update(self.centstruct, int(what), ctypes.byref(v)), "update(%d)" % what)
+        if what == OUTPUTPHASEARR:
+            self._interp_out = val  # written by later runs: kept alive here
 
     # -- extensions (no reference counterpart) --
     def set_noise_mode(self, mode):

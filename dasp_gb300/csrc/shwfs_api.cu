@@ -163,6 +163,13 @@ struct shwfs_handle {
   int corrKMode = -1;  // mode the device kernel was built for
   DevBuf<float> d_corrK;
   shwfs_array corrimg{};
+  // phase interpolation (interpolatePhase): the phase array is inputPhaseSize
+  // square instead of W x W; d_interp holds the resampled frames
+  bool interp = false;
+  int inputPhaseSize = 0;
+  DevBuf<float> d_interp;
+  shwfs_array interpOut{};  // OUTPUTPHASEARR: interpolated phase of the lit subapertures
+  std::vector<float> interpStage;
   DevBuf<float> d_corrimg;
   std::vector<float> corrimgStage;
   std::vector<float> psfHost, binTHost, binNHost;
@@ -762,6 +769,20 @@ shwfs_status prepare_readout(shwfs_handle* h) {
 
 shwfs_status enqueue_readout(shwfs_handle* h, const float* phs, float* cents, float* bimg, int nframes,
                              long long phsStride, cudaStream_t st) {
+  if (h->interp && phs) {
+    // resample the input frames to W x W first (interpolatePhase,
+    // cmod/src/centmodule.c:1795-1804); the pipeline then reads d_interp
+    const long long WW = (long long)h->W * h->W, in2 = (long long)h->inputPhaseSize * h->inputPhaseSize;
+    if ((size_t)(WW * nframes) > h->d_interp.n)
+      return fail(SHWFS_ERR_STATE, "interpolation buffer holds %zu frames, %d requested", h->d_interp.n / (size_t)WW,
+                  nframes);
+    CK(launch_interp_phase(phs, phsStride ? phsStride : in2, h->inputPhaseSize, h->d_interp.p, WW, h->W, nframes, st));
+    if (nframes == 1 && !is_none(h->interpOut) && h->interpOut.on_device)
+      CK(launch_copy_lit_blocks(h->d_interp.p, (float*)h->interpOut.data, h->d_lit.p, (int)h->lit.size(), h->nsubx,
+                                h->phasesize, st));
+    phs = h->d_interp.p;
+    phsStride = WW;
+  }
   const int nlit = (int)h->lit.size();
   const long long nwork = (long long)nlit * nframes;
   const long long ntiles = (nwork + h->TS - 1) / h->TS;
@@ -835,6 +856,14 @@ int readout_frame(const shwfs_handle* h) {
 // publish exactly what the reference writes on a readout frame: every
 // centroid unless imageOnly; every image with imageOnly, else the lit ones
 shwfs_status publish_outputs(shwfs_handle* h, cudaStream_t st, bool* sync) {
+  if (h->interp && !is_none(h->interpOut) && !h->interpOut.on_device) {
+    // interpolated phase of the lit subapertures to a host array
+    h->interpStage.resize((size_t)h->W * h->W);
+    CK(cudaMemcpyAsync(h->interpStage.data(), h->d_interp.p, h->interpStage.size() * sizeof(float),
+                       cudaMemcpyDeviceToHost, st));
+    h->scatterPending = true;
+    *sync = true;
+  }
   if (corr_active(h) && !is_none(h->corrimg) && !h->corrimg.on_device) {
     // the reference writes the correlation images of lit subapertures
     const size_t nc = (size_t)h->nsubaps * h->corrPatternSize * h->corrPatternSize;
@@ -946,6 +975,17 @@ shwfs_status run_impl(shwfs_handle* h, cudaStream_t st, bool sync, float* elapse
         for (int i : h->lit) memcpy(dst + i * mm, h->bimgStage.data() + i * mm, mm * sizeof(float));
         h->bimgStage.clear();
       }
+      if (!h->interpStage.empty()) {
+        const int W = h->W, p = h->phasesize;
+        float* dst = (float*)h->interpOut.data;
+        for (int i : h->lit) {
+          const int sy = i / h->nsubx, sx = i - sy * h->nsubx;
+          for (int r = 0; r < p; r++)
+            memcpy(dst + (size_t)(sy * p + r) * W + sx * p, h->interpStage.data() + (size_t)(sy * p + r) * W + sx * p,
+                   p * sizeof(float));
+        }
+        h->interpStage.clear();
+      }
       if (!h->corrimgStage.empty()) {
         const size_t cc = (size_t)h->corrPatternSize * h->corrPatternSize;
         float* dst = (float*)h->corrimg.data;
@@ -1022,9 +1062,21 @@ shwfs_status shwfs_initialise(const shwfs_init* in, shwfs_handle** out) {
       h->phaseAmp = 1;
     else
       return fail(SHWFS_ERR_INVALID, "phase should be 2D or 3D (for phase+amp)");
-    if (in->phs.shape[h->phaseAmp] != W || in->phs.shape[h->phaseAmp + 1] != W)
-      return fail(SHWFS_ERR_UNSUPPORTED, "phase of size %lldx%lld needs interpolation to %dx%d (not implemented yet)",
-                  (long long)in->phs.shape[h->phaseAmp], (long long)in->phs.shape[h->phaseAmp + 1], W, W);
+    const int64_t ny = in->phs.shape[h->phaseAmp], nx = in->phs.shape[h->phaseAmp + 1];
+    if (ny != W || nx != W) {
+      // interpolatePhase (cmod/src/centmodule.c:2929-2933): the reference
+      // takes the input as square (dims[0] both ways) and reads the
+      // amplitude plane at the output-size offset, so only square
+      // phase-only inputs have a defined meaning
+      if (h->phaseAmp)
+        return fail(SHWFS_ERR_UNSUPPORTED, "phase+amplitude of size %lldx%lld would need interpolation to %dx%d; "
+                    "the reference reads its amplitude plane at the %dx%d offset, which is not reproduced",
+                    (long long)ny, (long long)nx, W, W, W, W);
+      if (ny != nx) return fail(SHWFS_ERR_INVALID, "phase of size %lldx%lld: interpolation needs a square phase", (long long)ny, (long long)nx);
+      if (ny < 4) return fail(SHWFS_ERR_INVALID, "phase of size %lldx%lld is too small to interpolate", (long long)ny, (long long)nx);
+      h->interp = true;
+      h->inputPhaseSize = (int)ny;
+    }
   }
   // image input (cmod/src/centmodule.c:3117-3157)
   if (!is_none(in->inputImage)) {
@@ -1151,6 +1203,7 @@ shwfs_status shwfs_initialise(const shwfs_init* in, shwfs_handle** out) {
   CK(h->d_poisFlag.alloc(nsa));
   CK(pois_table_device(&h->poisTab));
   CK(h->d_status.alloc(1));
+  if (h->interp) CK(h->d_interp.alloc((size_t)h->W * h->W));
   CK(cudaMemset(h->d_status.p, 0, sizeof(int)));
 
   // tiltfn (cmod/src/centmodule.c:3074-3081)
@@ -1207,6 +1260,10 @@ shwfs_status shwfs_run_batch(shwfs_handle* h, int nframes, const float* phs, int
                              float* bimg, void* stream) {
   if (!h) return fail(SHWFS_ERR_INVALID, "null handle");
   if (nframes < 1 || !phs || !cents || !bimg) return fail(SHWFS_ERR_INVALID, "bad batch arguments");
+  if (h->interp && (size_t)nframes * h->W * h->W > h->d_interp.n) {
+    CK(cudaSetDevice(h->device));
+    CK(h->d_interp.alloc((size_t)nframes * h->W * h->W));  // grows; cudaFree waits for work in flight
+  }
   if (h->noiseMode == SHWFS_NOISE_REFERENCE && nframes != 1)
     return fail(SHWFS_ERR_UNSUPPORTED, "reference-stream noise runs one frame at a time");
   cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
@@ -1402,8 +1459,17 @@ shwfs_status shwfs_update(shwfs_handle* h, int code, const shwfs_value* v) {
       h->nintegrations = (int)v->ival;
       break;
     case SHWFS_OUTPUTPHASEARR:
-      if (v->kind == SHWFS_VAL_ARRAY)
-        return fail(SHWFS_ERR_UNSUPPORTED, "interpolated-phase output is not implemented by this engine yet");
+      // interpolatedPhaseOutput (cmod/src/centmodule.c:1745-1755): written
+      // only while the phase is interpolated, lit subapertures only
+      if (v->kind == SHWFS_VAL_ARRAY) {
+        const shwfs_array& ar = v->arr[0];
+        if (check_f32(ar, "interpolated phase output")) return SHWFS_ERR_INVALID;
+        if (numel(ar) < (int64_t)h->W * h->W)
+          return fail(SHWFS_ERR_INVALID, "interpolated phase output must hold %dx%d values", h->W, h->W);
+        h->interpOut = ar;
+      } else {
+        h->interpOut = shwfs_array{};
+      }
       break;
     case SHWFS_FORM:
       if ((s = need(SHWFS_VAL_INT, "int"))) return s;
@@ -1742,7 +1808,7 @@ int64_t engine_device_bytes(const shwfs_handle* h) {
   add(h->d_binLo); add(h->d_binHi); add(h->d_ubArr); add(h->d_calBounds); add(h->d_subflag);
   add(h->d_subapStart); add(h->d_status); add(h->d_psfSpec); add(h->d_phs); add(h->d_cents); add(h->d_bimg);
   add(h->d_image); add(h->d_subapLoc); add(h->d_poisFlag); add(h->d_rng); add(h->d_w2); add(h->d_kc2);
-  add(h->d_iscale); add(h->d_pupT); add(h->d_frameCtr);
+  add(h->d_iscale); add(h->d_pupT); add(h->d_interp); add(h->d_frameCtr);
   return b;
 }
 

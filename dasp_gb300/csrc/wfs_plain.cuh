@@ -759,6 +759,13 @@ struct CorrArgs {
   long long corrimgFrameStride;
   int TS;         // subapertures per CTA tile (set by the launcher)
 };
+// bicubic resample of nframes square nin x nin phase frames to nout x nout
+// (interpolatePhase, wfs_interp.cu)
+cudaError_t launch_interp_phase(const float* in, long long inStride, int nin, float* out, long long outStride, int nout,
+                                int nframes, cudaStream_t stream);
+// the p x p blocks of the lit subapertures of a W x W array, src -> dst
+cudaError_t launch_copy_lit_blocks(const float* src, float* dst, const int* lit, int nlit, int nsubx, int p,
+                                   cudaStream_t stream);
 cudaError_t launch_corr(const WfsArgs& a, CorrArgs c, int numSMs, cudaStream_t stream);
 
 // increment n device counters (graph replays of a batch)

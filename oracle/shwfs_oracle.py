@@ -211,6 +211,67 @@ def fit_matrix(fitsize: int) -> np.ndarray:
 # the per-frame pipeline
 # ----------------------------------------------------------------------------
 
+# Catmull-Rom basis rows (cmod/src/centmodule.c:1642), times 1/2 through t[0..3]
+_MX = ((0.0, 2.0, 0.0, 0.0), (-1.0, 0.0, 1.0, 0.0), (2.0, -5.0, 4.0, -1.0), (-1.0, 3.0, -3.0, 1.0))
+
+
+def _dot4_f32(c, v):
+    """c[0]*v[0] + c[1]*v[1] + c[2]*v[2] + c[3]*v[3], left to right, each
+    product and sum rounded to float32 (the C code's float arithmetic)."""
+    s = (np.float32(c[0]) * v[0]).astype(np.float32)
+    for k in range(1, 4):
+        s = (s + (np.float32(c[k]) * v[k]).astype(np.float32)).astype(np.float32)
+    return s
+
+
+def _dot4_f32v(w, v):
+    """Like _dot4_f32 with per-sample float32 weights w[0..3]."""
+    s = (w[0] * v[0]).astype(np.float32)
+    for k in range(1, 4):
+        s = (s + (w[k] * v[k]).astype(np.float32)).astype(np.float32)
+    return s
+
+
+def _cubic_axis(nin, nout):
+    """Per output sample: first of the four input samples (before clamping)
+    and the weights 0.5 (1, t, t^2, t^3) (cmod/src/centmodule.c:1645-1680)."""
+    scale = np.float32((nin - 1.0) / (nout - 1))
+    t = (scale * np.arange(nout).astype(np.float32)).astype(np.float32)
+    i0 = np.floor(t).astype(np.int64)
+    t = (t - i0.astype(np.float32)).astype(np.float32)
+    i0 = i0 - 1
+    t[nout - 1] = 1.0  # the last output sample: the special case of :1663-1666
+    i0[nout - 1] = nin - 3
+    w1 = (np.float32(0.5) * t).astype(np.float32)
+    w2 = (w1 * t).astype(np.float32)
+    w3 = (w2 * t).astype(np.float32)
+    return i0, [np.full(nout, 0.5, np.float32), w1, w2, w3]
+
+
+def interpolate_phase(inp, nsubx, p):
+    """interpolatePhase (cmod/src/centmodule.c:1628-1758): bicubic
+    (Catmull-Rom) resample of a square input phase to (nsubx p)^2 samples
+    spanning the same extent, in float32 with the C code's operation order:
+    four column sums of the basis rows over four input rows, weighted in y,
+    then the basis rows over those four values, weighted in x.  Samples
+    outside the input repeat the edge row/column (:1685-1728)."""
+    inp = np.asarray(inp, np.float32)
+    nin = inp.shape[0]
+    nout = nsubx * p
+    iy, wy = _cubic_axis(nin, nout)
+    ix, wx = _cubic_axis(nin, nout)
+    rows = np.clip(iy[:, None] + np.arange(4)[None, :], 0, nin - 1)  # (nout, 4)
+    cols = np.clip(ix[:, None] + np.arange(4)[None, :], 0, nin - 1)
+    wyb = [w[:, None] for w in wy]
+    pcol = []
+    for i in range(4):  # column inx+i: interpolate in y
+        f = [inp[rows[:, j][:, None], cols[:, i][None, :]] for j in range(4)]
+        tmp = [_dot4_f32(_MX[k], f) for k in range(4)]
+        pcol.append(_dot4_f32v(wyb, tmp))
+    tmp2 = [_dot4_f32(_MX[i], pcol) for i in range(4)]
+    return _dot4_f32v([w[None, :] for w in wx], tmp2)
+
+
 class CentOracle:
     """State and per-frame step of one WFS, following ``centstruct``.
 
@@ -269,6 +330,7 @@ class CentOracle:
         self.corrsize = self.corrPatternSize if (self.correlationCentroiding and self.corrPattern is not None) \
             else self.m
         self.corrimg = None
+        self.interpOut = None  # OUTPUTPHASEARR: interpolated phase of the lit subapertures
         self.fitMx = None
         self.fitMxParam = 0
         self.refCents = None
@@ -446,6 +508,8 @@ class CentOracle:
             self.set_use_brightest(val)
         elif code == INTEGSTEPS:
             self.nintegrations = int(val)
+        elif code == OUTPUTPHASEARR:
+            self.interpOut = None if val is None else val
         elif code == CORRELATIONCENTROIDING:
             self.correlationCentroiding = int(val)
             self.corrsize = self.corrPatternSize if self.correlationCentroiding else self.m
@@ -792,7 +856,20 @@ class CentOracle:
         """One frame: py_run -> centroidsFromPhase for every thread partition."""
         add = self.additive()
         if add is not None and add in (2, -1):
-            self._readout(np.asarray(phs), cents.reshape(-1), bimg.reshape(self.nsubaps, self.m, self.m), amp)
+            phs = np.asarray(phs)
+            W = self.nsubx * self.p
+            if phs.shape != (W, W):
+                # phase of another (square) size: interpolatePhase per lit
+                # subaperture (:1795-1804), here the whole array at once
+                full = interpolate_phase(phs, self.nsubx, self.p)
+                if self.interpOut is not None:
+                    out = self.interpOut.reshape(W, W)
+                    for i in np.nonzero(self.subflag == 1)[0]:
+                        sy, sx = divmod(int(i), self.nsubx)
+                        blk = (slice(sy * self.p, (sy + 1) * self.p), slice(sx * self.p, (sx + 1) * self.p))
+                        out[blk] = full[blk]
+                phs = full
+            self._readout(phs, cents.reshape(-1), bimg.reshape(self.nsubaps, self.m, self.m), amp)
         self.curInteg += 1
         if self.curInteg >= self.nintegrations + self.nlatency:
             self.curInteg = 0

@@ -101,9 +101,19 @@ def test_invalid_arguments_rejected_without_gpu(engine_lib, mutate, exc):
 def test_unsupported_paths_are_reported(engine_lib):
     import numpy as np
     c = _base_kwargs()
-    # a phase of another size needs interpolatePhase, which is not built yet
+    # phase+amplitude of another size: the reference reads the amplitude
+    # plane at the output-size offset; not reproduced
     with pytest.raises(NotImplementedError):
-        c.engine(phs=np.zeros((c.W + 4, c.W + 4), np.float32))
+        c.engine(phs=np.zeros((2, c.W + 4, c.W + 4), np.float32))
+
+
+def test_interpolated_phase_shapes_are_checked(engine_lib):
+    import numpy as np
+    c = _base_kwargs()
+    with pytest.raises(ValueError, match="square"):
+        c.engine(phs=np.zeros((c.W + 4, c.W + 6), np.float32))
+    with pytest.raises(ValueError, match="too small"):
+        c.engine(phs=np.zeros((3, 3), np.float32))
 
 
 @pytest.mark.skipif(gpu_available(), reason="checks the no-GPU error path")

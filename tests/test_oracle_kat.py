@@ -189,3 +189,53 @@ def test_integration_state_machine():
     c.oracle_run(orc, None, cents)
     assert not np.all(cents == 9.0)
     assert orc.curInteg == 0
+
+
+# ---- interpolatePhase (cmod/src/centmodule.c:1628-1758) ----
+
+def test_interpolate_phase_known_answers():
+    from oracle.shwfs_oracle import interpolate_phase
+    rng = np.random.default_rng(4)
+    # a constant stays that constant exactly
+    c = np.full((50, 50), 3.25, np.float32)
+    assert np.array_equal(interpolate_phase(c, 8, 8), np.full((64, 64), 3.25, np.float32))
+    # same size: every sample but the pinned last row/column is the input
+    # (t = 0 keeps 0.5 * 2 * f[1]); the last one is the t = 1 end of the
+    # n-3 .. n cell, equal to the last input sample up to rounding
+    a = rng.standard_normal((64, 64)).astype(np.float32)
+    b = interpolate_phase(a, 8, 8)
+    assert np.array_equal(b[:-1, :-1], a[:-1, :-1])
+    assert np.abs(b - a).max() < 1e-5
+    # Catmull-Rom reproduces a linear ramp away from the clamped edges
+    x = np.arange(50, dtype=np.float64)
+    r = np.add.outer(0.3 * x, -0.7 * x).astype(np.float32)
+    o = interpolate_phase(r, 8, 8)
+    X = np.arange(64) * (49 / 63.0)
+    ref = np.add.outer(0.3 * X, -0.7 * X)
+    assert np.abs(o[2:-2, 2:-2] - ref[2:-2, 2:-2]).max() < 1e-4
+    # and a cubic in the interior of a finer resample (the kernel's order)
+    assert interpolate_phase(rng.standard_normal((90, 90)).astype(np.float32), 8, 8).dtype == np.float32
+
+
+def test_oracle_interpolates_mismatched_phase():
+    """A phase of another size gives the centroids of its resampled array,
+    and OUTPUTPHASEARR receives the lit subapertures' resampled phase."""
+    from oracle.shwfs_oracle import OUTPUTPHASEARR, interpolate_phase
+    from dasp_gb300.screens import von_karman_screen
+    c = Case(nsubx=8, p=8, N=16)
+    inp = von_karman_screen(50, 4.2, 0.15, 30.0, 3, 640.0)
+    full = interpolate_phase(inp, 8, 8)
+    o1, o2 = c.oracle("f32"), c.oracle("f32")
+    out = np.full((64, 64), -7.0, np.float32)
+    o1.update(OUTPUTPHASEARR, out)
+    c1, _ = c.oracle_run(o1, phs=inp)
+    c2, _ = c.oracle_run(o2, phs=full)
+    np.testing.assert_array_equal(c1, c2)
+    lit = c.lit().reshape(8, 8)
+    for sy in range(8):
+        for sx in range(8):
+            blk = out[sy * 8:(sy + 1) * 8, sx * 8:(sx + 1) * 8]
+            if lit[sy, sx]:
+                np.testing.assert_array_equal(blk, full[sy * 8:(sy + 1) * 8, sx * 8:(sx + 1) * 8])
+            else:
+                assert (blk == -7.0).all()
