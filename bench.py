@@ -846,8 +846,9 @@ def main():
         "head_rule": "fastest tensor-core form whose noiseless centroid error vs the float64 oracle is <= 1e-3 px",
     }
     if ws == 1 and not args.no_cpu_baseline:
-        # CPU restatement of the path on a bounded sample, single thread
-        frames = 8
+        # CPU restatement of the path on a bounded sample (64 frames, about
+        # 10 s of CPU work on one core), single thread
+        frames = 64
         dt, nl = cpu_sample(frames, 1)
         line["cpu_baseline"] = {"value": nl * frames / dt, "unit": UNIT, "cores": 1, "kind": "port",
                                 "sample": "%d noisy frames of the same workload through the numpy/C restatement "
