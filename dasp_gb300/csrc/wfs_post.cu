@@ -172,8 +172,8 @@ __global__ void __launch_bounds__(kPostThreads, 4) wfs_post_kernel(const WfsArgs
 
 constexpr int kSlotThreads = 512;
 constexpr int kSlotCtasPerSM = 2;  // one copy of the Poisson tables per CTA
-constexpr int kSlotStages = 3;
-constexpr int kSlotMaxTS = 64;
+constexpr int kSlotStages = 2;
+constexpr int kSlotMaxTS = 96;
 
 // The common configuration (window CoG or image only; no brightest-pixel
 // selection, fit or optical binning) over tiles of TS consecutive
