@@ -1704,6 +1704,21 @@ shwfs_status shwfs_sample_noise(int kind, const float* lam, int64_t n, uint64_t 
   return SHWFS_OK;
 }
 
+shwfs_status shwfs_selftest_bounded_wait(int64_t max_cycles, int* timed_out, int* abort_raised) {
+  if (!timed_out || !abort_raised || max_cycles <= 0 || max_cycles > (int64_t)1 << 36)
+    return fail(SHWFS_ERR_INVALID, "bad self-test arguments");
+  DevBuf<int> out;
+  CK(out.alloc(3));
+  CK(cudaMemset(out.p, 0, 3 * sizeof(int)));
+  CK(launch_bounded_wait_selftest((long long)max_cycles, out.p, 0));
+  CK(cudaDeviceSynchronize());
+  int h[3];
+  CK(cudaMemcpy(h, out.p, sizeof(h), cudaMemcpyDeviceToHost));
+  *timed_out = h[0];
+  *abort_raised = h[1];
+  return SHWFS_OK;
+}
+
 shwfs_status shwfs_batch_free(shwfs_batch* b) {
   delete b;
   return SHWFS_OK;

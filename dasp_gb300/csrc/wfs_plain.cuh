@@ -766,6 +766,9 @@ cudaError_t launch_interp_phase(const float* in, long long inStride, int nin, fl
 // the p x p blocks of the lit subapertures of a W x W array, src -> dst
 cudaError_t launch_copy_lit_blocks(const float* src, float* dst, const int* lit, int nlit, int nsubx, int p,
                                    cudaStream_t stream);
+// one CTA waiting on an mbarrier nothing arrives on, up to max_cycles;
+// out[0..2] = gave up, abort flag raised, cycles waited / 2^20 (selftest.cu)
+cudaError_t launch_bounded_wait_selftest(long long max_cycles, int* out, cudaStream_t stream);
 cudaError_t launch_corr(const WfsArgs& a, CorrArgs c, int numSMs, cudaStream_t stream);
 
 // increment n device counters (graph replays of a batch)

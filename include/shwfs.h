@@ -269,6 +269,15 @@ shwfs_status shwfs_set_split_event(shwfs_handle* h, void* event);
 shwfs_status shwfs_sample_noise(int kind, const float* lam, int64_t n, uint64_t seed, uint64_t frame, float* out,
                                 void* stream);
 
+/* Self-test of the pipeline's bounded waits (no counterpart in the
+ * reference): a one-CTA kernel waits on an mbarrier that nothing arrives on,
+ * for at most max_cycles SM clocks.  *timed_out = 1 when the wait gave up
+ * and *abort_raised = 1 when it raised the CTA's abort flag, as every
+ * tensor-core pipeline wait does before the kernel drains and the handle
+ * reports SHWFS_ERR_STATE.  Returns after the kernel has finished; the
+ * context stays usable. */
+shwfs_status shwfs_selftest_bounded_wait(int64_t max_cycles, int* timed_out, int* abort_raised);
+
 /* ---- allocation-free image centroiding (no counterpart in the reference) ----
  *
  * For callers that cannot allocate GPU memory: a real-time control thread
