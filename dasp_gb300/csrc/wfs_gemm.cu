@@ -60,10 +60,9 @@ namespace shwfs {
 
 namespace {
 
-constexpr int kConsumers = 640;  // 8 epilogue + 12 field warps
+constexpr int kConsumers = 512;
 constexpr int kEpiWarps = 8;    // warps 0-7: D1/D2 epilogue
-constexpr int kFieldWarps = 12;  // warps 8-19: field build
-constexpr int kFieldPhases = kFieldWarps / 4;  // field threads per row
+constexpr int kFieldWarps = 8;  // warps 8-15: field build
 constexpr int kGemmThreads = kConsumers + 96;  // + GEMM1 issuer, GEMM2 producer, W2 loader
 constexpr int kTileSubaps = 128;
 constexpr uint32_t kTmemCols = 512;
@@ -371,8 +370,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     // ================= consumers =================
     // warps 0-7: epilogue (TMEM lane quarter warp & 3, column half h);
     // warps 8-15: field build (row r, pixel-group parity h)
-    // epilogue: column half h; field: pixel-group phase h (0 .. kFieldPhases-1)
-    const int r = tid & 127, h = warp < kEpiWarps ? (tid >> 7) & 1 : (tid - kEpiWarps * 32) >> 7;
+    const int r = tid & 127, h = (tid >> 7) & 1;
     const bool fieldRole = warp >= kEpiWarps;
     const bool vecPup = (pp & 3) == 0 && ((uintptr_t)a.pup & 15) == 0;
     const bool vecPhs = (p & 1) == 0 && (a.W & 1) == 0 && (a.phsFrameStride & 1) == 0 && ((uintptr_t)a.phs & 7) == 0;
@@ -479,7 +477,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         if (lt < reuse) {
           // zero K padding beyond 2*ppr once per buffer (none when 2*ppr is
           // a multiple of 16)
-          for (int k = 2 * ppr + h; k < g.K1; k += kFieldPhases) {
+          for (int k = 2 * ppr + h; k < g.K1; k += 2) {
             const uint32_t off = kmaj(r, k, ESZ, sboE);
             if constexpr (ESZ == 4) {
               *reinterpret_cast<uint32_t*>(Ehi + off) = 0u;
@@ -492,13 +490,13 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         const int sy = R.sub / a.nsubx, sx = R.sub - sy * a.nsubx;
         const float* ph = a.phs + (long long)R.frm * a.phsFrameStride + (long long)sy * p * a.W + sx * p;
         const float* pu = a.pup + (long long)R.sub * pp;
-        for (int g8 = h; g8 < ng8; g8 += 2 * kFieldPhases) {
+        for (int g8 = h; g8 < ng8; g8 += 4) {
           float phA[8], puA[8], phB[8], puB[8];
-          const bool two = g8 + kFieldPhases < ng8;
+          const bool two = g8 + 2 < ng8;
           load_group(R, ph, pu, g8, phA, puA);
-          if (two) load_group(R, ph, pu, g8 + kFieldPhases, phB, puB);
+          if (two) load_group(R, ph, pu, g8 + 2, phB, puB);
           emit_group(Ehi, Elo, R, g8, phA, puA);
-          if (two) emit_group(Ehi, Elo, R, g8 + kFieldPhases, phB, puB);
+          if (two) emit_group(Ehi, Elo, R, g8 + 2, phB, puB);
         }
         tc::fence_async_smem();
         __syncwarp();
