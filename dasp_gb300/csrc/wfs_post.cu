@@ -11,6 +11,8 @@
 // A separate launch rather than a stage of the tensor-core kernel: the noise
 // samplers are latency-bound scalar code that wants many resident warps,
 // while the tensor-core kernel holds one 608-thread CTA per SM.
+#include <type_traits>
+
 #include "gemm_form.h"
 #include "wfs_plain.cuh"
 
@@ -272,12 +274,24 @@ __global__ void __launch_bounds__(kSlotThreads, kSlotCtasPerSM)
     const int ns = min(TS, a.nsubaps - s0);
     float* dstF = a.bimg + (long long)f * a.bimgFrameStride + (long long)s0 * mm;
     // noise and threshold of pixel pix of slot s (pf: Poisson applies)
-    auto draw = [&](float v, int s, int pix, bool pf) {
+    // (bright: lambda >= 64, the rejection sampler; otherwise the tables,
+    // whose path the first loop compiles without the rejection loop)
+    auto draw = [&](float v, int s, int pix, bool pf, auto bright) {
       KeyedStream st(a.philoxKeys, fbase + f, s0 + s, pix, 0);
       float g = 0.f;
       if constexpr (RN) g = normal_counter(st);
       if constexpr (POIS) {
-        if (pf) v = poisson_counter_tab(st, v, *s_tab);
+        if (pf) {
+          if constexpr (decltype(bright)::value) {
+            v = poisson_counter_tab(st, v, *s_tab);
+          } else if (v > 0.f) {  // as poisson_counter_tab for 0 < lambda < 64
+            const float u3 = st.uniform();
+            const float u4 = st.uniform();
+            v = poisson_tab(*s_tab, u3, u4, v);
+          } else {
+            v = 0.f;
+          }
+        }
       }
       if constexpr (RN)
         v += rn * g + a.readBg;
@@ -309,8 +323,11 @@ __global__ void __launch_bounds__(kSlotThreads, kSlotCtasPerSM)
             s_brightv[slot] = v;
             continue;
           }
+          // queue full: drawn here
+          store(w, draw(v, s, w - s * mm, pf, std::true_type{}));
+          continue;
         }
-        v = draw(v, s, w - s * mm, pf);
+        v = draw(v, s, w - s * mm, pf, std::false_type{});
       }
       store(w, v);
     }
@@ -321,7 +338,7 @@ __global__ void __launch_bounds__(kSlotThreads, kSlotCtasPerSM)
         for (int b = tid; b < nb; b += blockDim.x) {
           const int w = s_bright[b];
           const int s = div_small(w, mm, inv_mm);
-          store(w, draw(s_brightv[b], s, w - s * mm, true));
+          store(w, draw(s_brightv[b], s, w - s * mm, true, std::true_type{}));
         }
       }
     }
