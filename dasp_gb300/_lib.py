@@ -37,7 +37,9 @@ EXPORTS = ("shwfs_initialise", "shwfs_run", "shwfs_run_slope", "shwfs_update", "
            "shwfs_batch_create", "shwfs_batch_run", "shwfs_batch_free", "shwfs_autotune",
            "shwfs_sample_noise", "shwfs_set_split_event", "shwfs_server_create", "shwfs_server_add_system",
            "shwfs_server_remove_system", "shwfs_server_submit", "shwfs_server_poll", "shwfs_server_get_stats",
-           "shwfs_server_clock", "shwfs_server_destroy", "shwfs_selftest_bounded_wait")
+           "shwfs_server_clock", "shwfs_server_destroy", "shwfs_selftest_bounded_wait",
+           "shwfs_screen_create", "shwfs_screen_add", "shwfs_screen_window", "shwfs_screen_read",
+           "shwfs_screen_free")
 
 NOALLOC_MAX_SUBAPS = 65536
 
@@ -151,6 +153,13 @@ def lib() -> ctypes.CDLL:
         L.shwfs_server_clock.restype = ctypes.c_double
         L.shwfs_sample_noise.argtypes = [ctypes.c_int, vp, ctypes.c_int64, ctypes.c_uint64, ctypes.c_uint64, vp, vp]
         L.shwfs_selftest_bounded_wait.argtypes = [ctypes.c_int64, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+        L.shwfs_screen_create.argtypes = [ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp, ctypes.c_uint64,
+                                          ctypes.POINTER(ctypes.c_void_p)]
+        L.shwfs_screen_add.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, vp, vp]
+        L.shwfs_screen_window.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp,
+                                          ctypes.c_int64, vp]
+        L.shwfs_screen_read.argtypes = [vp, vp]
+        L.shwfs_screen_free.argtypes = [vp]
         for name in EXPORTS:
             if name not in ("shwfs_last_error", "shwfs_version", "shwfs_server_clock"):
                 getattr(L, name).restype = ctypes.c_int

@@ -269,6 +269,31 @@ shwfs_status shwfs_set_split_event(shwfs_handle* h, void* event);
 shwfs_status shwfs_sample_noise(int kind, const float* lam, int64_t n, uint64_t seed, uint64_t frame, float* out,
                                 void* stream);
 
+/* ---- infinite phase screen on the device (science/infScrn.py) ----
+ *
+ * A screen of ny x nx float32 phase values kept in HBM as a circular buffer.
+ * shwfs_screen_add appends n columns (axis 0) or rows (axis 1) at the end,
+ * each A Z + coeff_turb B noise (+ step on the first one), Z the last two
+ * columns (rows) stacked oldest first, as addNewColumnOnEnd /
+ * addNewRowOnEnd (science/infScrn.py:747-791, 825-855); the oldest column
+ * (row) is dropped.  ay (ny x 2ny), by (ny x ny), ax (nx x 2nx), bx
+ * (nx x nx) are row-major float64 host arrays (either axis may be NULL if
+ * never extruded); init is the initial screen (ny x nx, host).  noise: NULL
+ * for the device's counter-based normals (seed, extrusion index), else n
+ * host vectors of ny (nx) float64 normals to inject.  shwfs_screen_window
+ * copies an h x w window at (y0, x0) of the current screen to a device
+ * array (row stride out_stride) -- a WFS's phase, without a host copy.
+ * With stream NULL the calls wait for the result. */
+typedef struct shwfs_screen shwfs_screen;
+shwfs_status shwfs_screen_create(int ny, int nx, const float* init, const double* ay, const double* by,
+                                 const double* ax, const double* bx, uint64_t seed, shwfs_screen** out);
+shwfs_status shwfs_screen_add(shwfs_screen* s, int axis, int n, double coeff_turb, double step, const double* noise,
+                              void* stream);
+shwfs_status shwfs_screen_window(shwfs_screen* s, int y0, int x0, int h, int w, float* out, int64_t out_stride,
+                                 void* stream);
+shwfs_status shwfs_screen_read(shwfs_screen* s, float* host_out);
+shwfs_status shwfs_screen_free(shwfs_screen* s);
+
 /* Self-test of the pipeline's bounded waits (no counterpart in the
  * reference): a one-CTA kernel waits on an mbarrier that nothing arrives on,
  * for at most max_cycles SM clocks.  *timed_out = 1 when the wait gave up
