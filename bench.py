@@ -587,6 +587,56 @@ def run_lgs_batch(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- reconstructor step
+
+def run_recon(args):
+    """The centroids' consumer: tomoRecon's decay + reconstructor MVM on
+    the device for an ELT-scale system (5,316 actuators x the 7,944 slopes
+    of the 74x74 sensor; R 169 MB, larger than L2, read once per step)."""
+    import torch
+    from dasp_gb300.recon import Reconstructor
+    torch.cuda.set_device(0)
+    nacts, ncents = 5316, 7944
+    rng = np.random.default_rng(2)
+    R = torch.from_numpy(rng.standard_normal((nacts, ncents), dtype=np.float32)).cuda()
+    rec = Reconstructor(R, 0.5, 0.99)
+    xs = [torch.from_numpy(rng.standard_normal(ncents, dtype=np.float32)).cuda() for _ in range(4)]
+    stream = torch.cuda.Stream()
+    for k in range(max(args.warmup, 3)):
+        rec.step(xs[k % 4], stream=stream)
+    stream.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(0) as clk:
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                ev[k][0].record(stream)
+                rec.step(xs[k % 4], stream=stream)
+                ev[k][1].record(stream)
+        stream.synchronize()
+    ms = float(np.median([a.elapsed_time(b) for a, b in ev]))
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            peaks = json.load(fh)
+    except (OSError, ValueError):
+        pass
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    bytes_step = 4.0 * nacts * ncents + 4.0 * ncents + 8.0 * nacts
+    gbs = bytes_step / (ms / 1e3) / 1e9
+    line = {
+        "metric": "reconstructor steps/s (5316 actuators x 7944 slopes, decay + MVM)", "value": 1e3 / ms,
+        "unit": "steps/s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded normal reconstructor and slopes",
+        "config": {"workload": "recon_mvm_5316x7944", "l2": "R (169 MB) larger than L2, read once per step"},
+        "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+                     "traffic": None, "kernel": "mvm_update_kernel",
+                     "algorithmic_bytes_per_step": bytes_step},
+        "clocks": clk.summary(), "gpu_launches": args.steps,
+    }
+    print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------------- our arm
 
 def main():
@@ -598,20 +648,21 @@ def main():
     ap.add_argument("--frames", type=int, default=FPSTEP, help="frames per step")
     ap.add_argument("--e2e-frames", type=int, default=400)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="ngs74", choices=["ngs74", "serving", "precision", "lgs_batch"],
+    ap.add_argument("--workload", default="ngs74", choices=["ngs74", "serving", "precision", "lgs_batch", "recon"],
                     help="ngs74: the headline 74x74 NGS sensor; serving: 64 AO systems through the serving loop; "
                          "precision: per-form centroid error sweep vs the float64 oracle; "
-                         "lgs_batch: 6 LGS + 3 NGS sensors in one CUDA graph")
+                         "lgs_batch: 6 LGS + 3 NGS sensors in one CUDA graph; recon: the reconstructor step")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--precision-frames", type=int, default=8)
     ap.add_argument("--serve-inflight", type=int, default=16)
     args = ap.parse_args()
     ws, rank, local = dist_env()
-    if args.workload in ("serving", "precision", "lgs_batch") and args.impl == "ours":
+    if args.workload in ("serving", "precision", "lgs_batch", "recon") and args.impl == "ours":
         if rank == 0:
             from dasp_gb300 import build
             build.build()
-            {"serving": run_serving, "precision": run_precision, "lgs_batch": run_lgs_batch}[args.workload](args)
+            {"serving": run_serving, "precision": run_precision, "lgs_batch": run_lgs_batch,
+             "recon": run_recon}[args.workload](args)
         return
 
     if args.impl == "reference":

@@ -39,7 +39,7 @@ EXPORTS = ("shwfs_initialise", "shwfs_run", "shwfs_run_slope", "shwfs_update", "
            "shwfs_server_remove_system", "shwfs_server_submit", "shwfs_server_poll", "shwfs_server_get_stats",
            "shwfs_server_clock", "shwfs_server_destroy", "shwfs_selftest_bounded_wait",
            "shwfs_screen_create", "shwfs_screen_add", "shwfs_screen_window", "shwfs_screen_read",
-           "shwfs_screen_free")
+           "shwfs_screen_free", "shwfs_mvm_update")
 
 NOALLOC_MAX_SUBAPS = 65536
 
@@ -160,6 +160,8 @@ def lib() -> ctypes.CDLL:
                                           ctypes.c_int64, vp]
         L.shwfs_screen_read.argtypes = [vp, vp]
         L.shwfs_screen_free.argtypes = [vp]
+        L.shwfs_mvm_update.argtypes = [ctypes.c_int, ctypes.c_int, vp, vp, vp, ctypes.c_float, vp, ctypes.c_float, vp,
+                                       vp]
         for name in EXPORTS:
             if name not in ("shwfs_last_error", "shwfs_version", "shwfs_server_clock"):
                 getattr(L, name).restype = ctypes.c_int

@@ -294,6 +294,15 @@ shwfs_status shwfs_screen_window(shwfs_screen* s, int y0, int x0, int h, int w, 
 shwfs_status shwfs_screen_read(shwfs_screen* s, float* host_out);
 shwfs_status shwfs_screen_free(shwfs_screen* s);
 
+/* ---- reconstructor step (science/tomoRecon.py:1077-1107, 1196-1223) ----
+ *
+ * act[i] = decay_i * act[i] - gain_i * sum_j R[i, j] x[j], R nacts x ncents
+ * row-major float32; gains/decay per actuator (device arrays) or, when NULL,
+ * the scalars gain/decay_scalar.  All arrays are device pointers; with
+ * stream NULL the call waits for the result. */
+shwfs_status shwfs_mvm_update(int nacts, int ncents, const float* R, const float* x, const float* gains, float gain,
+                              const float* decay, float decay_scalar, float* act, void* stream);
+
 /* Self-test of the pipeline's bounded waits (no counterpart in the
  * reference): a one-CTA kernel waits on an mbarrier that nothing arrives on,
  * for at most max_cycles SM clocks.  *timed_out = 1 when the wait gave up
