@@ -646,7 +646,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--frames", type=int, default=FPSTEP, help="frames per step")
-    ap.add_argument("--e2e-frames", type=int, default=400)
+    ap.add_argument("--e2e-frames", type=int, default=1000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="ngs74", choices=["ngs74", "serving", "precision", "lgs_batch", "recon"],
                     help="ngs74: the headline 74x74 NGS sensor; serving: 64 AO systems through the serving loop; "
@@ -802,6 +802,20 @@ def main():
     e2e_s = reduce_max(e2e_s, ws)
     e2e_value = ws * nlit * args.e2e_frames / e2e_s
     lat_ms = np.array(lat) * 1e3
+    # device-side latency of the same frames (run_async between two events on
+    # one stream: phase H2D from pinned memory, kernels, centroid/image D2H)
+    dev_lat = []
+    s_async = torch.cuda.Stream()
+    for k in range(min(args.e2e_frames, 1000)):
+        eng.set_io(phs=host_frames[k % 8])
+        ea = torch.cuda.Event(enable_timing=True)
+        eb = torch.cuda.Event(enable_timing=True)
+        ea.record(s_async)
+        eng.run_async(s_async)
+        eb.record(s_async)
+        s_async.synchronize()
+        dev_lat.append(ea.elapsed_time(eb))
+    dev_lat = np.array(dev_lat)
 
     F_alg, B_alg = algorithmic_per_subap()
     T_alg = tensor_flops_per_subap()
@@ -892,7 +906,12 @@ def main():
                         "cents/bimg out, one synchronous frame per step" % head,
                 "frames": args.e2e_frames},
         "latency_ms": {"p50": float(np.percentile(lat_ms, 50)), "p99": float(np.percentile(lat_ms, 99)),
-                       "mean": float(lat_ms.mean()), "path": "shwfs_run, host I/O"},
+                       "mean": float(lat_ms.mean()), "frames": len(lat_ms),
+                       "path": "run() entry to centroids on the host (sync, host I/O)"},
+        "latency_ms_device": {"p50": float(np.percentile(dev_lat, 50)) if len(dev_lat) else None,
+                              "p99": float(np.percentile(dev_lat, 99)) if len(dev_lat) else None,
+                              "frames": len(dev_lat),
+                              "path": "run_async between CUDA events: phase in, kernels, outputs back"},
         "clocks": clocks,
         "gpu_launches": (2 if head == "fp32" else 3) * args.steps,
         "centroid_err_px_vs_fp64": errs,
