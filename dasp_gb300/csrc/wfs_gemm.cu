@@ -507,16 +507,24 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       int d1b = 0;
       uint32_t d1r = 0, gA = 0;
       // binned image of tile lt (row P) from D2: normalise, sky -> bimg
-      auto read_D2 = [&](int lt, const Row& P) {
+      // per-row image scale and sky level, computed a tile before their D2
+      // read-out so the scattered loads are off the read-out's critical path
+      struct RowNorm {
+        float scale, skyv;
+      };
+      auto row_norm = [&](const Row& P) {
         const int i = P.sub;
-        const float totsig = a.totsig[i];
-        const float fr = a.frac[i];
-        const float isc = iscale ? iscale[i] : 1.f;
+        const float totsig = a.totsig[i], fr = a.frac[i];
+        float scale = totsig > 0.f ? (a.sigArr ? a.sigArr[i] / totsig : a.sig * fr / totsig) : 1.f;
+        if (iscale) scale = scale / iscale[i];  // undo the fp16 range scaling
+        return RowNorm{scale, a.sky * fr};
+      };
+      auto read_D2 = [&](int lt, const Row& P, const RowNorm& nv) {
+        const int i = P.sub;
         wait(&bars.d2full, lt & 1);
         tc::fence_after_sync();
-        float scale = totsig > 0.f ? (a.sigArr ? a.sigArr[i] / totsig : a.sig * fr / totsig) : 1.f;
-        if (iscale) scale = scale / isc;  // undo the fp16 range scaling
-        const float skyv = a.sky * fr;
+        const float scale = nv.scale;  // exactly 1 when there is nothing to scale
+        const float skyv = nv.skyv;
         float* out = a.bimg + (long long)P.frm * a.bimgFrameStride + (long long)i * mm;
         const float* skyA = a.skyArr ? a.skyArr + (long long)i * mm : nullptr;
         for (int cb = h * 32; cb < mm; cb += 64) {
@@ -529,7 +537,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
 #pragma unroll
           for (int e = 0; e < 32; e++) {
             x[e] = __uint_as_float(v[e]);
-            if (totsig > 0.f || iscale) x[e] *= scale;
+            x[e] *= scale;
             if (skyv > 0.f) x[e] += skyv;
             if (skyA && e < n) x[e] += skyA[cb + e];
           }
@@ -600,19 +608,24 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
 
       Row prev{false, 0, 0, 0};
       Row cur = row_of(0);
+      RowNorm prevN{1.f, 0.f};
+      RowNorm curN = row_norm(cur);
       float isc = (iscale && cur.live) ? iscale[cur.sub] : 1.f;
       for (int lt = 0; lt < myTiles; lt++) {
         const Row next = row_of(lt + 1);
         const float iscn = (iscale && next.live) ? iscale[next.sub] : 1.f;
+        const RowNorm nextN = row_norm(next);  // used two read-outs from now
         for (int oc = 0; oc < g.noc; oc++) {
-          if (oc == 0 && lt >= 1) read_D2(lt - 1, prev);
+          if (oc == 0 && lt >= 1) read_D2(lt - 1, prev, prevN);
           chunk(isc);
         }
         prev = cur;
+        prevN = curN;
         cur = next;
+        curN = nextN;
         isc = iscn;
       }
-      if (myTiles > 0) read_D2(myTiles - 1, prev);
+      if (myTiles > 0) read_D2(myTiles - 1, prev, prevN);
     }
   }
   if (!ok) atomicOr(err, 2);
