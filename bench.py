@@ -900,10 +900,15 @@ def main():
         "fp32_compute": {"achieved_tflops": form_report["fp32"]["fp32_tflops"], "peak_tflops": fp32_peak_tf,
                          "frac": form_report["fp32"]["fp32_frac"], "algorithmic_flops_per_subap_frame": F_alg,
                          "peak_basis": "SMs x 128 FP32 lanes x 2 x max SM clock", "form": "fp32"},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(W * W * 4),
-                "d2h_bytes_per_step": int(nsub * 2 * 4 + nsub * w["m"] * w["m"] * 4),
+        # zero-copy host I/O (the engine's default): the image-formation
+        # kernel reads the lit subapertures' phase from the pinned host array,
+        # the noise/centroid kernel writes every centroid and the lit
+        # subapertures' final images into the pinned host arrays
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(nlit * w["p"] * w["p"] * 4),
+                "d2h_bytes_per_step": int(nsub * 2 * 4 + nlit * w["m"] * w["m"] * 4),
                 "path": "centcmod.set_io + centcmod.run -> shwfs_run (%s form), pinned host numpy phase in, host "
-                        "cents/bimg out, one synchronous frame per step" % head,
+                        "cents/bimg out, one synchronous frame per step; zero-copy host I/O (kernels read the "
+                        "host phase and write the host outputs through their device aliases)" % head,
                 "frames": args.e2e_frames},
         "latency_ms": {"p50": float(np.percentile(lat_ms, 50)), "p99": float(np.percentile(lat_ms, 99)),
                        "mean": float(lat_ms.mean()), "frames": len(lat_ms),
@@ -913,7 +918,9 @@ def main():
                               "frames": len(dev_lat),
                               "path": "run_async between CUDA events: phase in, kernels, outputs back"},
         "clocks": clocks,
-        "gpu_launches": (2 if head == "fp32" else 3) * args.steps,
+        # per step: formation + noise/centroid kernels (tensor-core forms;
+        # the latter also zeroes the unlit centroids), or fused + unlit (FP32)
+        "gpu_launches": 2 * args.steps,
         "centroid_err_px_vs_fp64": errs,
         "head_rule": "fastest tensor-core form whose noiseless centroid error vs the float64 oracle is <= 1e-3 px",
     }

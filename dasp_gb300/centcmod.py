@@ -49,6 +49,9 @@ OUTPUTPHASEARR = 22
 TILESUBAPS = 101  # extension: subapertures per CTA tile (0 = default)
 FORM = 102  # extension: compute form (FORMS below)
 FORMS = {"fp32": 0, "bf16": 1, "bf16x3": 2, "fp16": 3, "tf32": 4}
+HOSTIO = 103  # extension: zero-copy host I/O switches (HOSTIO_* below)
+HOSTIO_OUTPUTS = 1  # kernels write cents / final images into the pinned host arrays
+HOSTIO_PHASE = 2  # image-formation kernels read the pinned host phase directly
 
 _INT_CODES = {CALSOURCE, ADDPOISSON, NCEN, NTHREADS, OPTICALBINNING, CORRELATIONCENTROIDING, INTEGSTEPS,
               NOISEMODE, TILESUBAPS, FORM}
@@ -266,6 +269,15 @@ class centcmod:
         code = {"counter": NOISE_COUNTER, "reference": NOISE_REFERENCE}[mode]
         self.update(NOISEMODE, code)
 
+    def set_host_io(self, outputs=True, phase=True):
+        """Zero-copy transfers of ``run`` with host (numpy) arrays: with
+        ``outputs`` the kernels write the centroids and final images straight
+        into the pinned host arrays while they run; with ``phase`` the
+        image-formation kernels read the host phase directly instead of after
+        a host-to-device copy.  Results are identical either way.  (Counter
+        noise without correlation centroiding; otherwise copies are used.)"""
+        self.update(HOSTIO, (HOSTIO_OUTPUTS if outputs else 0) | (HOSTIO_PHASE if phase else 0))
+
     def set_form(self, form):
         """Compute form: ``"fp32"`` (fused FP32 kernel, default), or GEMM-DFT
         on the tensor cores: ``"bf16"`` (one pass), ``"bf16x3"`` (split
@@ -303,18 +315,23 @@ class centcmod:
 
     def set_io(self, phs=None, cents=None, bimg=None):
         """Rebind the borrowed phase/output arrays (same shapes)."""
-        keep: list = []
+        keeps = {}
         args = []
         for x, n in ((phs, "phs"), (cents, "cents"), (bimg, "bimg")):
-            args.append(None if x is None else ctypes.byref(as_array(x, "f", n, keep)))
+            if x is not None:
+                keeps[n] = []
+            args.append(None if x is None else ctypes.byref(as_array(x, "f", n, keeps[n])))
         check(_lib.lib().shwfs_set_io(self.centstruct, *args), "set_io")
+        # the arrays now bound replace the previous ones of their slots
+        if not hasattr(self, "_io_keep"):
+            self._io_keep = {}
+        self._io_keep.update(keeps)
         if phs is not None:
             self.phs = phs
         if cents is not None:
             self.cents = cents
         if bimg is not None:
             self.bimg = bimg
-        self._keep.extend(keep)
 
     def set_split_event(self, event):
         """Timing aid: the engine records ``event`` (a created torch.cuda.Event

@@ -76,6 +76,10 @@ cudaError_t launch_gemm(const WfsArgs& a, const GemmGeom& g, const float* iscale
                         cudaStream_t stream);
 // noise, threshold and the post stages on the pre-noise images in bimg
 // (wfs_post.cu)
-cudaError_t launch_post(const WfsArgs& a, int numSMs, cudaStream_t stream);
+// done (optional) receives kPostDidUnlit when the launched kernel also
+// zeroed the centroids of the unlit subapertures, and kPostDidOut when it
+// also wrote the final images to a.bimgOut
+constexpr unsigned kPostDidUnlit = 1u, kPostDidOut = 2u;
+cudaError_t launch_post(const WfsArgs& a, int numSMs, cudaStream_t stream, unsigned* done = nullptr);
 
 }  // namespace shwfs

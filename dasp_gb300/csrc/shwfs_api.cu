@@ -129,6 +129,10 @@ struct shwfs_handle {
   int imageDims = 0, imageRows = 0, imageCols = 0;
   std::vector<int> subapLoc;
   float* bimgMapped = nullptr;        // device alias of a pinned host bimg
+  float* centsMapped = nullptr;       // ... of a pinned host cents
+  const float* phsMapped = nullptr;   // ... of a pinned host phase
+  int hostIO = SHWFS_HOSTIO_OUTPUTS | SHWFS_HOSTIO_PHASE;  // zero-copy switches
+  bool centsDirect = false, bimgDirect = false;  // this readout's kernels wrote the host outputs
   std::vector<float> bimgStage;       // fallback: full copy, then host scatter
   bool scatterPending = false;
   std::vector<void*> registered;  // host ranges pinned by the engine
@@ -212,13 +216,14 @@ shwfs_status bind_io(shwfs_handle* h, shwfs_array& slot, const shwfs_array& a, D
       h->registered.push_back((void*)a.data);
   }
   cudaGetLastError();  // a refused registration only costs copy speed
-  if (&slot == &h->bimg) {
-    h->bimgMapped = nullptr;
-    if (cudaPointerGetAttributes(&attr, a.data) == cudaSuccess && attr.type == cudaMemoryTypeHost &&
-        attr.devicePointer)
-      h->bimgMapped = (float*)attr.devicePointer;
-    cudaGetLastError();
-  }
+  // device alias of the pinned host array (zero-copy I/O), if it has one
+  float* alias = nullptr;
+  if (cudaPointerGetAttributes(&attr, a.data) == cudaSuccess && attr.type == cudaMemoryTypeHost && attr.devicePointer)
+    alias = (float*)attr.devicePointer;
+  cudaGetLastError();
+  if (&slot == &h->bimg) h->bimgMapped = alias;
+  if (&slot == &h->cents) h->centsMapped = alias;
+  if (&slot == &h->phs) h->phsMapped = alias;
   // outputs start from the caller's contents: entries the engine does not
   // write (unlit subapertures, non-readout frames) come back unchanged
   if (copy_initial) CK(cudaMemcpy(mirror.p, a.data, count * sizeof(float), cudaMemcpyHostToDevice));
@@ -767,8 +772,15 @@ shwfs_status prepare_readout(shwfs_handle* h) {
   return SHWFS_OK;
 }
 
+// bimgHost (optional): a second destination of the final images (the
+// device alias of the caller's pinned host array); *bimgHostDone tells
+// whether the launched kernels filled it (lit subapertures, and the unlit
+// ones with imageOnly)
 shwfs_status enqueue_readout(shwfs_handle* h, const float* phs, float* cents, float* bimg, int nframes,
-                             long long phsStride, cudaStream_t st) {
+                             long long phsStride, cudaStream_t st, float* bimgHost = nullptr,
+                             bool* bimgHostDone = nullptr) {
+  if (bimgHostDone) *bimgHostDone = false;
+  if (h->noiseMode == SHWFS_NOISE_REFERENCE || corr_active(h)) bimgHost = nullptr;
   if (h->interp && phs) {
     // resample the input frames to W x W first (interpolatePhase,
     // cmod/src/centmodule.c:1795-1804); the pipeline then reads d_interp
@@ -821,6 +833,8 @@ shwfs_status enqueue_readout(shwfs_handle* h, const float* phs, float* cents, fl
       CK(launch_unlit(a, h->d_unlit.p, (int)h->unlit.size(), st));
     }
   } else {
+    unsigned postDone = 0;
+    bool plainDirect = false;
     if (nlit && gemm_active(h)) {
       // tensor-core image formation into bimg, then noise + post stages
       WfsArgs a = make_args(h, phs, cents, bimg, nframes, phsStride, kForm);
@@ -831,14 +845,25 @@ shwfs_status enqueue_readout(shwfs_handle* h, const float* phs, float* cents, fl
       CK(launch_gemm(a, g, g.fmt == kFmtFP16 ? h->d_iscale.p : nullptr, h->numSMs, h->d_status.p, st));
       if (h->splitEvent) CK(cudaEventRecord(h->splitEvent, st));
       a.mode = kNoiseCounter | kPost;
-      CK(launch_post(a, h->numSMs, st));
+      a.bimgOut = bimgHost;
+      CK(launch_post(a, h->numSMs, st, &postDone));
     } else if (nlit) {
+      // the fused kernel writes each final image once: straight to the
+      // host array when there is one
+      plainDirect = bimgHost != nullptr;
+      if (plainDirect) bimg = bimgHost;
       WfsArgs a = make_args(h, phs, cents, bimg, nframes, phsStride, kForm | kNoiseCounter | kPost);
       CK(h->entry->launch(a, grid, h->smem, st));
     }
-    if (!h->unlit.empty()) {
+    if (!h->unlit.empty() && !(postDone & kPostDidUnlit)) {
       WfsArgs a = make_args(h, phs, cents, bimg, nframes, phsStride, 0);
       CK(launch_unlit(a, h->d_unlit.p, (int)h->unlit.size(), st));
+    }
+    if (bimgHostDone && bimgHost) {
+      if (plainDirect || !nlit)
+        *bimgHostDone = plainDirect || h->unlit.empty() || !h->imageOnly;
+      else
+        *bimgHostDone = (postDone & kPostDidOut) && (h->unlit.empty() || !h->imageOnly);
     }
   }
   return enqueue_corr(h, cents, bimg, 1, st);
@@ -872,10 +897,10 @@ shwfs_status publish_outputs(shwfs_handle* h, cudaStream_t st, bool* sync) {
     h->scatterPending = true;
     *sync = true;
   }
-  if (!h->cents.on_device && !h->imageOnly)
+  if (!h->cents.on_device && !h->imageOnly && !h->centsDirect)
     CK(cudaMemcpyAsync((void*)h->cents.data, h->d_cents.p, (size_t)h->nsubaps * 2 * sizeof(float),
                        cudaMemcpyDeviceToHost, st));
-  if (!h->bimg.on_device) {
+  if (!h->bimg.on_device && !h->bimgDirect) {
     const size_t nb = (size_t)h->nsubaps * h->nimg * h->nimg;
     if (h->imageOnly || h->unlit.empty()) {
       CK(cudaMemcpyAsync((void*)h->bimg.data, h->d_bimg.p, nb * sizeof(float), cudaMemcpyDeviceToHost, st));
@@ -942,6 +967,7 @@ shwfs_status run_impl(shwfs_handle* h, cudaStream_t st, bool sync, float* elapse
   if (slope && is_none(h->inputImage)) return fail(SHWFS_ERR_STATE, "centmodule - inputImage is NULL");
   if (!slope && is_none(h->phs)) return fail(SHWFS_ERR_STATE, "no phase array is bound (image-input handle)");
   const bool readout = slope || readout_frame(h);
+  h->centsDirect = h->bimgDirect = false;
   if (readout) {
     shwfs_status s;
     if (slope) {
@@ -949,13 +975,23 @@ shwfs_status run_impl(shwfs_handle* h, cudaStream_t st, bool sync, float* elapse
     } else {
       const size_t nph = (size_t)numel(h->phs);
       const float* phs = (const float*)h->phs.data;
+      // zero-copy host I/O (counter noise, no correlation): the kernels
+      // read / write the pinned host arrays through their device aliases
+      const bool zc = h->noiseMode != SHWFS_NOISE_REFERENCE && !corr_active(h);
       if (!h->phs.on_device) {
-        CK(cudaMemcpyAsync(h->d_phs.p, h->phs.data, nph * sizeof(float), cudaMemcpyHostToDevice, st));
-        phs = h->d_phs.p;
+        if (zc && !h->interp && (h->hostIO & SHWFS_HOSTIO_PHASE) && h->phsMapped) {
+          phs = h->phsMapped;
+        } else {
+          CK(cudaMemcpyAsync(h->d_phs.p, h->phs.data, nph * sizeof(float), cudaMemcpyHostToDevice, st));
+          phs = h->d_phs.p;
+        }
       }
-      float* cents = h->cents.on_device ? (float*)h->cents.data : h->d_cents.p;
+      const bool zcOut = zc && (h->hostIO & SHWFS_HOSTIO_OUTPUTS);
+      h->centsDirect = !h->cents.on_device && zcOut && h->centsMapped && !h->imageOnly;
+      float* cents = h->cents.on_device ? (float*)h->cents.data : (h->centsDirect ? h->centsMapped : h->d_cents.p);
       float* bimg = h->bimg.on_device ? (float*)h->bimg.data : h->d_bimg.p;
-      s = enqueue_readout(h, phs, cents, bimg, 1, 0, st);
+      float* bimgHost = !h->bimg.on_device && zcOut ? h->bimgMapped : nullptr;
+      s = enqueue_readout(h, phs, cents, bimg, 1, 0, st, bimgHost, &h->bimgDirect);
     }
     if (s) return s;
     if ((s = publish_outputs(h, st, &sync))) return s;
@@ -1482,6 +1518,12 @@ shwfs_status shwfs_update(shwfs_handle* h, int code, const shwfs_value* v) {
       if (v->ival < 0 || v->ival > 64) return fail(SHWFS_ERR_INVALID, "tile size must be in [0, 64]");
       h->tileOverride = (int)v->ival;
       return plan(h);
+    case SHWFS_HOSTIO:
+      if ((s = need(SHWFS_VAL_INT, "int"))) return s;
+      if (v->ival < 0 || v->ival > (SHWFS_HOSTIO_OUTPUTS | SHWFS_HOSTIO_PHASE))
+        return fail(SHWFS_ERR_INVALID, "unknown host I/O switches %lld", (long long)v->ival);
+      h->hostIO = (int)v->ival;
+      break;
     case SHWFS_NOISEMODE:
       if ((s = need(SHWFS_VAL_INT, "int"))) return s;
       if (v->ival != SHWFS_NOISE_COUNTER && v->ival != SHWFS_NOISE_REFERENCE)

@@ -85,6 +85,13 @@ struct WfsArgs {
   // 1: the post stages write bimg but no centroids (correlation
   // centroiding computes them afterwards from bimg)
   int skipCents;
+  // 1: the noise/centroid kernel also zeroes the centroids of the unlit
+  // subapertures (set by launch_post when it takes that work over)
+  int zeroUnlit;
+  // optional second destination of the final images (same layout as bimg),
+  // e.g. the device alias of a pinned host array; written by the
+  // noise/centroid kernel when launch_post reports it
+  float* bimgOut;
   int mode;
 };
 

@@ -11,6 +11,7 @@
 // A separate launch rather than a stage of the tensor-core kernel: the noise
 // samplers are latency-bound scalar code that wants many resident warps,
 // while the tensor-core kernel holds one 608-thread CTA per SM.
+#include <algorithm>
 #include <type_traits>
 
 #include "gemm_form.h"
@@ -299,12 +300,14 @@ __global__ void __launch_bounds__(kSlotThreads, kSlotCtasPerSM)
         v += a.readBg;
       return threshold_px(v, a.floorv, a.threshType);
     };
+    float* outF = a.bimgOut ? a.bimgOut + (long long)f * a.bimgFrameStride + (long long)s0 * mm : nullptr;
     auto store = [&](int w, float v) {
       if (a.pxlPower == 2.f)
         v = v * v;
       else if (a.pxlPower != 1.f && a.pxlPower != 0.f)
         v = powf(v, a.pxlPower);
       dstF[w] = v;
+      if (outF) outF[w] = v;
       imgs[w] = v;
     };
     for (int w = tid; w < ns * mm; w += blockDim.x) {
@@ -330,6 +333,15 @@ __global__ void __launch_bounds__(kSlotThreads, kSlotCtasPerSM)
         v = draw(v, s, w - s * mm, pf, std::false_type{});
       }
       store(w, v);
+    }
+    if (a.zeroUnlit) {
+      // unlit subapertures: centroids 0 (cmod/src/centmodule.c:1964-1981)
+      float* c = a.cents + (long long)f * a.centsFrameStride + 2LL * s0;
+      for (int s = tid; s < ns; s += blockDim.x)
+        if (s_flag[s] != 1) {
+          c[2 * s] = 0.f;
+          c[2 * s + 1] = 0.f;
+        }
     }
     if constexpr (POIS) {
       if (noise) {
@@ -387,8 +399,10 @@ __global__ void __launch_bounds__(kSlotThreads, kSlotCtasPerSM)
 
 }  // namespace
 
-cudaError_t launch_post(const WfsArgs& a0, int numSMs, cudaStream_t stream) {
+cudaError_t launch_post(const WfsArgs& a0, int numSMs, cudaStream_t stream, unsigned* done) {
   WfsArgs a = a0;
+  a.zeroUnlit = 0;
+  if (done) *done = 0;
   const int mm = a.m * a.m;
   const long long nwork = (long long)a.nlit * a.nframes;
   if (nwork == 0) return cudaSuccess;
@@ -409,7 +423,22 @@ cudaError_t launch_post(const WfsArgs& a0, int numSMs, cudaStream_t stream) {
     const int budget = (228 * 1024) / kSlotCtasPerSM - 1024 - 4 * kPostBright * 2 - 64 - tabB - cwB;
     int ts = budget / perSlot - 1;
     ts = ts < 1 ? 1 : (ts > kSlotMaxTS ? kSlotMaxTS : ts);
+    // small batches: tiles no larger than it takes to give every resident
+    // CTA one (latency), nor smaller than one pixel per thread
+    const long long slots = (long long)a.nsubaps * a.nframes;
+    const long long fill = (slots + (long long)numSMs * kSlotCtasPerSM - 1) / ((long long)numSMs * kSlotCtasPerSM);
+    const int minTs = (kSlotThreads + mm - 1) / mm;
+    if (fill < ts) ts = (int)std::max<long long>(fill, std::min(minTs, ts));
     a.TS = ts;
+    if (done) {
+      if (!a.imageOnly) {
+        a.zeroUnlit = 1;
+        *done |= kPostDidUnlit;
+      }
+      if (a.bimgOut) *done |= kPostDidOut;
+    } else {
+      a.bimgOut = nullptr;
+    }
     const int stageFloats = (ts * mm + 3 * ts + 3) / 4 * 4;
     const int smem = tabB + cwB + (kSlotStages * stageFloats + 2 * ts * a.ncen) * (int)sizeof(float);
     const bool rnOn = a.calsource == 0 && a.readNoise != 0.f;

@@ -69,7 +69,24 @@ enum {
    * the default for the geometry */
   SHWFS_TILESUBAPS = 101,
   /* extension: compute form, ival = SHWFS_FORM_* */
-  SHWFS_FORM = 102
+  SHWFS_FORM = 102,
+  /* extension: zero-copy host I/O of shwfs_run/shwfs_run_async, ival = an
+   * OR of SHWFS_HOSTIO_* (default: both) */
+  SHWFS_HOSTIO = 103
+};
+
+/* zero-copy host I/O switches (SHWFS_HOSTIO).  They apply to host arrays
+ * that are pinned (the engine pins borrowed host arrays when it can) with
+ * counter-based noise and no correlation centroiding; results are identical
+ * either way, only the transfers change. */
+enum {
+  /* the kernels write the centroids and the final images of the lit
+   * subapertures straight into the caller's host arrays, during the kernels,
+   * instead of device copies followed by host copies */
+  SHWFS_HOSTIO_OUTPUTS = 1,
+  /* the image-formation kernels read the phase from the caller's host array
+   * instead of a host-to-device copy ahead of them */
+  SHWFS_HOSTIO_PHASE = 2
 };
 
 /* compute forms */
