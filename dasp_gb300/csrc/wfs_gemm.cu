@@ -50,6 +50,7 @@
 #include <string.h>
 
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 #include "gemm_form.h"
@@ -146,6 +147,7 @@ struct Bars {
   uint64_t d1full[3], d1free[3];  // per D1 buffer (two or three)
   uint64_t a2full[2], a2free[2];  // per GEMM2 operand buffer
   uint64_t d2full, d2free;
+  uint64_t ehelp;  // the epilogue warps' share of the first tile's field
 };
 
 template <int FMT, int PASSES>
@@ -200,6 +202,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     }
     tc::mbar_init(&bars.d2full, 1);
     tc::mbar_init(&bars.d2free, kEpiWarps);
+    tc::mbar_init(&bars.ehelp, kEpiWarps);
     tc::fence_mbar_init();
   }
   tc::fence_before_sync();
@@ -214,6 +217,9 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   const long long nwork = (long long)a.nlit * a.nframes;
   const long long ntiles = (nwork + kTileSubaps - 1) / kTileSubaps;
   const int myTiles = blockIdx.x < ntiles ? (int)((ntiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
+  // small batches (at most two tiles per CTA): the epilogue warps build half
+  // of the first tile's field, which their first D1 chunk waits for anyway
+  const bool help = myTiles > 0 && myTiles <= 2;
 
   if (warp == kConsumers / 32) {
     // ================= GEMM1 producer (MMA issue only) =================
@@ -241,6 +247,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         // field buffer eb; its uses alternate when double buffered
         const int eb = g.dbE ? (lt & 1) : 0;
         wait(&bars.efull[eb], (uint32_t)((g.dbE ? (lt >> 1) : lt) & 1));
+        if (lt == 0 && help) wait(&bars.ehelp, 0);
         tc::fence_after_sync();
         const uint64_t dEh = dEh0 + (eb ? dEstep : 0);
         const uint64_t dEl = dEl0 + (eb ? dEstep : 0);
@@ -394,87 +401,109 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       return o;
     };
 
-    if (fieldRole) {
-      // ---- field build: E = pup*exp(i(phs - tilt)) of this row, pixel
-      // groups g8 = h, h+2, ... (8 pixels each), Re at K = pix, Im at
-      // K = ppr + pix; two groups' loads are in flight before either is used
-      auto load_group = [&](const Row& R, const float* ph, const float* pu, int g8, float (&phv)[8],
-                            float (&puv)[8]) {
-        const int pix0 = g8 * 8;
-        if (R.live && g.pupT) {
-          // grouped copy: lanes (consecutive lit subapertures) read
-          // consecutive 32-byte entries; zero past the last pixel
-          const float* pt = g.pupT + ((long long)g8 * a.nlit + R.li) * 8;
-          const float4 u0 = *reinterpret_cast<const float4*>(pt);
-          const float4 u1 = *reinterpret_cast<const float4*>(pt + 4);
-          puv[0] = u0.x; puv[1] = u0.y; puv[2] = u0.z; puv[3] = u0.w;
-          puv[4] = u1.x; puv[5] = u1.y; puv[6] = u1.z; puv[7] = u1.w;
-        } else if (R.live && vecPup && pix0 + 8 <= pp) {
-          const float4 u0 = *reinterpret_cast<const float4*>(pu + pix0);
-          const float4 u1 = *reinterpret_cast<const float4*>(pu + pix0 + 4);
-          puv[0] = u0.x; puv[1] = u0.y; puv[2] = u0.z; puv[3] = u0.w;
-          puv[4] = u1.x; puv[5] = u1.y; puv[6] = u1.z; puv[7] = u1.w;
-        } else {
+    // ---- field build: E = pup*exp(i(phs - tilt)) of this row in pixel
+    // groups g8 of 8 pixels, Re at K = pix, Im at K = ppr + pix
+    auto load_group = [&](const Row& R, const float* ph, const float* pu, int g8, float (&phv)[8],
+                          float (&puv)[8]) {
+      const int pix0 = g8 * 8;
+      if (R.live && g.pupT) {
+        // grouped copy: lanes (consecutive lit subapertures) read
+        // consecutive 32-byte entries; zero past the last pixel
+        const float* pt = g.pupT + ((long long)g8 * a.nlit + R.li) * 8;
+        const float4 u0 = *reinterpret_cast<const float4*>(pt);
+        const float4 u1 = *reinterpret_cast<const float4*>(pt + 4);
+        puv[0] = u0.x; puv[1] = u0.y; puv[2] = u0.z; puv[3] = u0.w;
+        puv[4] = u1.x; puv[5] = u1.y; puv[6] = u1.z; puv[7] = u1.w;
+      } else if (R.live && vecPup && pix0 + 8 <= pp) {
+        const float4 u0 = *reinterpret_cast<const float4*>(pu + pix0);
+        const float4 u1 = *reinterpret_cast<const float4*>(pu + pix0 + 4);
+        puv[0] = u0.x; puv[1] = u0.y; puv[2] = u0.z; puv[3] = u0.w;
+        puv[4] = u1.x; puv[5] = u1.y; puv[6] = u1.z; puv[7] = u1.w;
+      } else {
 #pragma unroll
-          for (int e = 0; e < 8; e++) puv[e] = (R.live && pix0 + e < pp) ? pu[pix0 + e] : 0.f;
-        }
-        if (R.live && vecPhs) {
+        for (int e = 0; e < 8; e++) puv[e] = (R.live && pix0 + e < pp) ? pu[pix0 + e] : 0.f;
+      }
+      if (R.live && vecPhs) {
 #pragma unroll
-          for (int e = 0; e < 8; e += 2) {
-            const int pix = pix0 + e;
-            if (pix < pp) {
-              const int ii = pix / p, jj = pix - ii * p;  // jj even: the pair stays in the row
-              const float2 v2 = *reinterpret_cast<const float2*>(ph + (long long)ii * a.W + jj);
-              phv[e] = v2.x;
-              phv[e + 1] = v2.y;
-            } else {
-              phv[e] = phv[e + 1] = 0.f;
-            }
-          }
-        } else {
-#pragma unroll
-          for (int e = 0; e < 8; e++) {
-            const int pix = pix0 + e;
-            const int ii = pix / p, jj = pix - ii * p;
-            phv[e] = (R.live && pix < pp) ? ph[(long long)ii * a.W + jj] : 0.f;
+        for (int e = 0; e < 8; e += 2) {
+          const int pix = pix0 + e;
+          if (pix < pp) {
+            const int ii = pix / p, jj = pix - ii * p;  // jj even: the pair stays in the row
+            const float2 v2 = *reinterpret_cast<const float2*>(ph + (long long)ii * a.W + jj);
+            phv[e] = v2.x;
+            phv[e + 1] = v2.y;
+          } else {
+            phv[e] = phv[e + 1] = 0.f;
           }
         }
-      };
-      auto emit_group = [&](uint8_t* Ehi, uint8_t* Elo, const Row& R, int g8, const float (&phv)[8],
-                            const float (&puv)[8]) {
-        const int pix0 = g8 * 8;
-        float er[8], ei[8];
+      } else {
 #pragma unroll
         for (int e = 0; e < 8; e++) {
           const int pix = pix0 + e;
-          er[e] = 0.f;
-          ei[e] = 0.f;
-          if (R.live && pix < pp) {
-            const float t = phv[e] - s_tilt[pix];
-            float sn, cs;
-            if constexpr (SPLIT) {
-              sincosf(t, &sn, &cs);
-            } else {
-              sincos_reduced(t, &sn, &cs);
-            }
-            er[e] = puv[e] * cs;
-            ei[e] = puv[e] * sn;
-          }
+          const int ii = pix / p, jj = pix - ii * p;
+          phv[e] = (R.live && pix < pp) ? ph[(long long)ii * a.W + jj] : 0.f;
         }
-        store8<FMT, SPLIT>(Ehi, Elo, kmaj(r, pix0, ESZ, sboE), er);
-        store8<FMT, SPLIT>(Ehi, Elo, kmaj(r, ppr + pix0, ESZ, sboE), ei);
-      };
-      const int ng8 = ppr / 8;
+      }
+    };
+    auto emit_group = [&](uint8_t* Ehi, uint8_t* Elo, const Row& R, int g8, const float (&phv)[8],
+                          const float (&puv)[8]) {
+      const int pix0 = g8 * 8;
+      float er[8], ei[8];
+#pragma unroll
+      for (int e = 0; e < 8; e++) {
+        const int pix = pix0 + e;
+        er[e] = 0.f;
+        ei[e] = 0.f;
+        if (R.live && pix < pp) {
+          const float t = phv[e] - s_tilt[pix];
+          float sn, cs;
+          if constexpr (SPLIT) {
+            sincosf(t, &sn, &cs);
+          } else {
+            sincos_reduced(t, &sn, &cs);
+          }
+          er[e] = puv[e] * cs;
+          ei[e] = puv[e] * sn;
+        }
+      }
+      store8<FMT, SPLIT>(Ehi, Elo, kmaj(r, pix0, ESZ, sboE), er);
+      store8<FMT, SPLIT>(Ehi, Elo, kmaj(r, ppr + pix0, ESZ, sboE), ei);
+    };
+    const int ng8 = ppr / 8;
+    // the field of row R into (Ehi, Elo): this thread's pixel groups of
+    // parity h in [g0, g1) (two groups' loads in flight)
+    auto build_field = [&](const Row& R, uint8_t* Ehi, uint8_t* Elo, int g0, int g1) {
+      const int sy = R.sub / a.nsubx, sx = R.sub - sy * a.nsubx;
+      const float* ph = a.phs + (long long)R.frm * a.phsFrameStride + (long long)sy * p * a.W + sx * p;
+      const float* pu = a.pup + (long long)R.sub * pp;
+      for (int g8 = g0 + h; g8 < g1; g8 += 4) {
+        float phA[8], puA[8], phB[8], puB[8];
+        const bool two = g8 + 2 < g1;
+        load_group(R, ph, pu, g8, phA, puA);
+        if (two) load_group(R, ph, pu, g8 + 2, phB, puB);
+        emit_group(Ehi, Elo, R, g8, phA, puA);
+        if (two) emit_group(Ehi, Elo, R, g8 + 2, phB, puB);
+      }
+    };
+    // with help the first tile's groups split at gMid (even): the field
+    // warps take [0, gMid), the epilogue warps [gMid, ng8)
+    const int gMid = (ng8 / 2) & ~1;
+
+    {
+      // ---- field build (warps 8-15): row r, pixel groups of parity h.
+      // With help the epilogue warps run the first pass of this loop too
+      // (one copy of the field code for both roles), then leave it.
       Row next = row_of(0);
-      for (int lt = 0; lt < myTiles; lt++) {
+      const int fieldTiles = fieldRole ? myTiles : (help ? 1 : 0);
+      for (int lt = 0; lt < fieldTiles; lt++) {
         const Row R = next;
-        next = row_of(lt + 1);  // its index loads overlap this tile
+        if (fieldRole) next = row_of(lt + 1);  // its index loads overlap this tile
         const int eb = g.dbE ? (lt & 1) : 0;
         uint8_t* Ehi = A1hi + (size_t)eb * L.a1Half * (SPLIT ? 2 : 1);
         uint8_t* Elo = Ehi + L.a1Half;
         const int reuse = g.dbE ? 2 : 1;  // tiles between two uses of a buffer
         if (lt >= reuse) wait(&bars.efree[eb], (uint32_t)(((lt - reuse) / reuse) & 1));
-        if (lt < reuse) {
+        if (lt < reuse && fieldRole) {
           // zero K padding beyond 2*ppr once per buffer (none when 2*ppr is
           // a multiple of 16)
           for (int k = 2 * ppr + h; k < g.K1; k += 2) {
@@ -487,22 +516,14 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
             }
           }
         }
-        const int sy = R.sub / a.nsubx, sx = R.sub - sy * a.nsubx;
-        const float* ph = a.phs + (long long)R.frm * a.phsFrameStride + (long long)sy * p * a.W + sx * p;
-        const float* pu = a.pup + (long long)R.sub * pp;
-        for (int g8 = h; g8 < ng8; g8 += 4) {
-          float phA[8], puA[8], phB[8], puB[8];
-          const bool two = g8 + 2 < ng8;
-          load_group(R, ph, pu, g8, phA, puA);
-          if (two) load_group(R, ph, pu, g8 + 2, phB, puB);
-          emit_group(Ehi, Elo, R, g8, phA, puA);
-          if (two) emit_group(Ehi, Elo, R, g8 + 2, phB, puB);
-        }
+        const bool split = lt == 0 && help;
+        build_field(R, Ehi, Elo, split && !fieldRole ? gMid : 0, split && fieldRole ? gMid : ng8);
         tc::fence_async_smem();
         __syncwarp();
-        if (lane == 0) tc::mbar_arrive(&bars.efull[eb]);
+        if (lane == 0) tc::mbar_arrive(fieldRole ? &bars.efull[eb] : &bars.ehelp);
       }
-    } else {
+    }
+    if (!fieldRole) {
       // ---- epilogue ----
       int d1b = 0;
       uint32_t d1r = 0, gA = 0;
