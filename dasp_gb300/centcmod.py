@@ -318,11 +318,17 @@ class centcmod:
         keeps = {}
         args = []
         for x, n in ((phs, "phs"), (cents, "cents"), (bimg, "bimg")):
-            if x is not None:
-                keeps[n] = []
-            args.append(None if x is None else ctypes.byref(as_array(x, "f", n, keeps[n])))
+            if x is None:
+                args.append(None)
+                continue
+            keep: list = []
+            desc = as_array(x, "f", n, keep)
+            keeps[int(desc.data)] = keep
+            args.append(ctypes.byref(desc))
         check(_lib.lib().shwfs_set_io(self.centstruct, *args), "set_io")
-        # the arrays now bound replace the previous ones of their slots
+        # host arrays stay pinned (registered in place) until the handle is
+        # freed, so every distinct array bound here stays referenced until
+        # then; rebinding the same few buffers costs nothing
         if not hasattr(self, "_io_keep"):
             self._io_keep = {}
         self._io_keep.update(keeps)

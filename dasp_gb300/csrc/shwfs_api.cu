@@ -216,9 +216,16 @@ shwfs_status bind_io(shwfs_handle* h, shwfs_array& slot, const shwfs_array& a, D
       h->registered.push_back((void*)a.data);
   }
   cudaGetLastError();  // a refused registration only costs copy speed
-  // device alias of the pinned host array (zero-copy I/O), if it has one
+  // device alias of the pinned host array (zero-copy I/O), only when the
+  // whole range is pinned and maps contiguously (a registration refused
+  // because a neighbour already pinned some of its pages leaves it partial)
   float* alias = nullptr;
-  if (cudaPointerGetAttributes(&attr, a.data) == cudaSuccess && attr.type == cudaMemoryTypeHost && attr.devicePointer)
+  cudaPointerAttributes last;
+  const char* lastByte = (const char*)a.data + count * sizeof(float) - 1;
+  if (cudaPointerGetAttributes(&attr, a.data) == cudaSuccess && attr.type == cudaMemoryTypeHost &&
+      attr.devicePointer && cudaPointerGetAttributes(&last, lastByte) == cudaSuccess &&
+      last.type == cudaMemoryTypeHost && last.devicePointer &&
+      (const char*)last.devicePointer - (const char*)attr.devicePointer == (ptrdiff_t)(count * sizeof(float) - 1))
     alias = (float*)attr.devicePointer;
   cudaGetLastError();
   if (&slot == &h->bimg) h->bimgMapped = alias;

@@ -217,9 +217,9 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   const long long nwork = (long long)a.nlit * a.nframes;
   const long long ntiles = (nwork + kTileSubaps - 1) / kTileSubaps;
   const int myTiles = blockIdx.x < ntiles ? (int)((ntiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
-  // small batches (at most two tiles per CTA): the epilogue warps build half
-  // of the first tile's field, which their first D1 chunk waits for anyway
-  const bool help = myTiles > 0 && myTiles <= 2;
+  // the epilogue warps build half of the first tile's field, which their
+  // first D1 chunk waits for anyway (the field warps go on to the next tile)
+  const bool help = myTiles > 0;
 
   if (warp == kConsumers / 32) {
     // ================= GEMM1 producer (MMA issue only) =================

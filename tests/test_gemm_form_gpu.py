@@ -103,6 +103,40 @@ def test_batch_equals_single_frames_bf16x3():
     eng.free()
 
 
+@pytest.mark.parametrize("form", ["fp16", "bf16x3"])
+def test_many_tiles_per_cta_batch_equals_single_frames(form):
+    """A 24-frame batch of the 74x74 sensor gives every CTA several
+    128-subaperture tiles (the steady-state pipeline: double-buffered field,
+    D1 buffer rounds, the epilogue warps' share of the first field); each
+    frame must equal that frame run alone, noise included (two engines of
+    the same seed: frame f draws from the streams of frame f either way)."""
+    torch = pytest.importorskip("torch")
+    kw = dict(nsubx=74, p=10, N=20, C=20, m=10, obs=0.28, Dtel=39.0, r0=0.157, L0=25.0, wavelength=589.0,
+              psf="gauss", sig=500.0, skybrightness=10.0, noiseFloor=6.0, readnoise=3.0, addPoisson=1)
+    F = 24
+    c = Case(**kw)
+    phases = np.stack([c.new_phase(300 + s) for s in range(F)])
+    eng = c.engine()
+    eng.set_form(form)
+    singles = []
+    for f in range(F):
+        c.phs[...] = phases[f]
+        eng.run(0)
+        singles.append((c.cents.copy(), c.bimg.copy()))
+    eng.free()
+    c2 = Case(**kw)
+    eng2 = c2.engine()
+    eng2.set_form(form)
+    dc = torch.zeros((F, c.nsubaps * 2), device="cuda")
+    db = torch.zeros((F, c.nsubaps, c.m, c.m), device="cuda")
+    eng2.run_batch(torch.from_numpy(phases).cuda(), dc, db)
+    torch.cuda.synchronize()
+    for f in range(F):
+        np.testing.assert_array_equal(dc[f].cpu().numpy(), singles[f][0])
+        np.testing.assert_array_equal(db[f].cpu().numpy().reshape(c.bimg.shape), singles[f][1])
+    eng2.free()
+
+
 def test_counter_noise_matches_fp32_form_statistics():
     c = Case(nsubx=8, p=8, N=16, sig=2e3, addPoisson=1, readnoise=2.0, noiseFloor=-1e9, threshType=1, seed=9)
     quiet = Case(nsubx=8, p=8, N=16, sig=2e3, noiseFloor=-1e9, threshType=1)
