@@ -208,6 +208,10 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
+  // the noise/centroid kernel queued behind this one (programmatic launch)
+  // may start its CTAs on SMs this grid leaves free; it reads nothing of
+  // ours before griddepcontrol.wait, which waits for this whole grid
+  if (tid == 0) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   const uint32_t tmem = s_tmem;
   bool ok = true;
   auto wait = [&](uint64_t* bar, uint32_t parity) {

@@ -211,6 +211,10 @@ __global__ void __launch_bounds__(kSlotThreads, kSlotCtasPerSM)
   }
   if (cw2d)
     for (int k = tid; k < mm; k += blockDim.x) s_cw[k] = a.centWeight[k];
+  // launched programmatically behind the image-formation kernel: everything
+  // above reads constants only; bimg is read after that grid has completed
+  // and its writes are visible (a no-op for an ordinary launch)
+  asm volatile("griddepcontrol.wait;" ::: "memory");
 
   const int tpf = (a.nsubaps + TS - 1) / TS;  // tiles per frame
   const long long ntiles = (long long)tpf * a.nframes;
@@ -454,8 +458,21 @@ cudaError_t launch_post(const WfsArgs& a0, int numSMs, cudaStream_t stream, unsi
     const long long ntiles = (long long)((a.nsubaps + ts - 1) / ts) * a.nframes;
     const long long cap = (long long)numSMs * ctas;
     const int grid = (int)(ntiles < cap ? ntiles : cap);
-    kern<<<grid, kSlotThreads, smem, stream>>>(a, pois ? tab : nullptr);
-    return cudaGetLastError();
+    // programmatic launch: CTAs may become resident while the previous
+    // kernel of the stream (the image formation) still runs and wait for it
+    // in griddepcontrol.wait after loading their tables
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kSlotThreads);
+    cfg.dynamicSmemBytes = (size_t)smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const PoisTab* tabArg = pois ? tab : nullptr;
+    return cudaLaunchKernelEx(&cfg, kern, a, tabArg);
   }
   const int smem = (a.TS * mm + (a.centWeightDim == 2 ? mm : 0)) * (int)sizeof(float) +
                    (pois ? (int)sizeof(PoisTab) : 0);
