@@ -184,8 +184,12 @@ struct shwfs_handle {
   const unsigned long long* graphCtr = nullptr;  // set while a batch captures
   DevBuf<unsigned long long> d_frameCtr;
 
+  int* h_status = nullptr;      // pinned host copy of d_status, read after a sync
+  int* h_statusDev = nullptr;   // its device alias (written by the noise/centroid kernel)
+
   ~shwfs_handle() {
     for (void* p : registered) cudaHostUnregister(p);
+    if (h_status) cudaFreeHost(h_status);
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -853,6 +857,8 @@ shwfs_status enqueue_readout(shwfs_handle* h, const float* phs, float* cents, fl
       if (h->splitEvent) CK(cudaEventRecord(h->splitEvent, st));
       a.mode = kNoiseCounter | kPost;
       a.bimgOut = bimgHost;
+      a.statusIn = h->d_status.p;
+      a.statusOut = h->h_statusDev;
       CK(launch_post(a, h->numSMs, st, &postDone));
     } else if (nlit) {
       // the fused kernel writes each final image once: straight to the
@@ -1009,6 +1015,12 @@ shwfs_status run_impl(shwfs_handle* h, cudaStream_t st, bool sync, float* elapse
     h->curInteg++;
     if (h->curInteg >= h->nintegrations + h->nlatency) h->curInteg = 0;
   }
+  // the kernels' status word comes back in stream order with the outputs:
+  // the tensor-core forms' noise/centroid kernel writes it to the pinned
+  // host word, the reference-stream path copies it
+  const bool checkStatus = sync && readout && (h->noiseMode == SHWFS_NOISE_REFERENCE || gemm_active(h));
+  if (checkStatus && h->noiseMode == SHWFS_NOISE_REFERENCE)
+    CK(cudaMemcpyAsync(h->h_status, h->d_status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   if (sync) {
     CK(cudaStreamSynchronize(st));
     if (h->scatterPending) {
@@ -1037,9 +1049,8 @@ shwfs_status run_impl(shwfs_handle* h, cudaStream_t st, bool sync, float* elapse
       }
       h->scatterPending = false;
     }
-    if ((h->noiseMode == SHWFS_NOISE_REFERENCE || gemm_active(h)) && readout) {
-      int status = 0;
-      CK(cudaMemcpy(&status, h->d_status.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (checkStatus) {
+      const int status = *(volatile int*)h->h_status;
       if (status & 1) return fail(SHWFS_ERR_STATE, "reference-stream Poisson sampler hit its iteration limit");
       if (status & 2) return fail(SHWFS_ERR_STATE, "tensor-core pipeline wait timed out (results invalid)");
     }
@@ -1248,6 +1259,9 @@ shwfs_status shwfs_initialise(const shwfs_init* in, shwfs_handle** out) {
   CK(h->d_status.alloc(1));
   if (h->interp) CK(h->d_interp.alloc((size_t)h->W * h->W));
   CK(cudaMemset(h->d_status.p, 0, sizeof(int)));
+  CK(cudaHostAlloc((void**)&h->h_status, sizeof(int), cudaHostAllocMapped));
+  *h->h_status = 0;
+  CK(cudaHostGetDevicePointer((void**)&h->h_statusDev, h->h_status, 0));
 
   // tiltfn (cmod/src/centmodule.c:3074-3081)
   std::vector<float> tilt((size_t)p * p);
@@ -1732,11 +1746,12 @@ shwfs_status shwfs_batch_run(shwfs_batch* b, void* stream) {
     b->ctrFrames[i] = b->hs[i]->framesRead;
   }
   if (!stream) {
+    // the tensor-core forms' noise/centroid kernels wrote each status word
+    // to its pinned host copy
     CK(cudaStreamSynchronize(st));
     for (shwfs_handle* h : b->hs) {
       if (!gemm_active(h)) continue;
-      int status = 0;
-      CK(cudaMemcpy(&status, h->d_status.p, sizeof(int), cudaMemcpyDeviceToHost));
+      const int status = *(volatile int*)h->h_status;
       if (status & 2) return fail(SHWFS_ERR_STATE, "tensor-core pipeline wait timed out (results invalid)");
     }
   }

@@ -92,6 +92,11 @@ struct WfsArgs {
   // e.g. the device alias of a pinned host array; written by the
   // noise/centroid kernel when launch_post reports it
   float* bimgOut;
+  // optional: the noise/centroid kernel copies the pipeline status word
+  // (statusIn, device) to statusOut (the device alias of a pinned host
+  // word) once the image-formation kernel has completed
+  const int* statusIn;
+  int* statusOut;
   int mode;
 };
 

@@ -34,6 +34,8 @@ __global__ void __launch_bounds__(kPostThreads, 4) wfs_post_kernel(const WfsArgs
   __shared__ int s_bright[kPostBright];
   __shared__ float s_brightv[kPostBright];
   const int tid = threadIdx.x;
+  // the image-formation kernel before this one has completed (stream order)
+  if (a.statusOut && blockIdx.x == 0 && tid == 0) *(volatile int*)a.statusOut = *(const volatile int*)a.statusIn;
   const int mm = a.m * a.m;
   const bool cw2d = a.centWeightDim == 2;
   const bool useTab = tab != nullptr;
@@ -215,6 +217,7 @@ __global__ void __launch_bounds__(kSlotThreads, kSlotCtasPerSM)
   // above reads constants only; bimg is read after that grid has completed
   // and its writes are visible (a no-op for an ordinary launch)
   asm volatile("griddepcontrol.wait;" ::: "memory");
+  if (a.statusOut && blockIdx.x == 0 && tid == 0) *(volatile int*)a.statusOut = *(const volatile int*)a.statusIn;
 
   const int tpf = (a.nsubaps + TS - 1) / TS;  // tiles per frame
   const long long ntiles = (long long)tpf * a.nframes;
