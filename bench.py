@@ -637,6 +637,78 @@ def run_recon(args):
     print(json.dumps(line), flush=True)
 
 
+def run_corr(args):
+    """Correlation centroiding on the 74x74 sensor (noisy, Gaussian spot
+    PSF): mode 1 (FFT correlation with a 20x20 pattern made by
+    transform_psf from a reference spot, as util/centroid.py does) and mode
+    5 (brute-force correlation with the spot itself), FP16 and FP32 forms.
+    Correlation runs one frame per call: each frame goes through
+    centcmod.set_io + run_async with host numpy phase/cents/bimg (copies;
+    the correlation images are not bound), timed between CUDA events on the
+    launch stream."""
+    import torch
+    from dasp_gb300.centcmod import centcmod
+    from dasp_gb300.correlation import transform_psf
+    from dasp_gb300.screens import gaussian_psf
+    torch.cuda.set_device(0)
+    w = WORKLOAD
+    pup = make_pupil()
+    nsx, m = w["nsubx"], w["m"]
+    nsub = nsx * nsx
+    screens = make_screens(4)
+    frames = [np.ascontiguousarray(f) for f in make_frames(screens, 8, 21)]
+    cs = 2 * m
+    y, x = np.mgrid[0:cs, 0:cs] - (cs - 1) / 2.0
+    spot = (50.0 * np.exp(-(x * x + y * y) / (2 * 1.5 ** 2))).astype(np.float32)
+    spots = np.ascontiguousarray(np.broadcast_to(spot, (nsx, nsx, cs, cs)))
+    psf = gaussian_psf(w["C"], w["psf_fwhm"])
+    nframes = max(args.steps * 10, 100)
+    results = {}
+    with ClockSampler(0) as clk:
+        for mode in (1, 5):
+            pattern = transform_psf(spots) if mode == 1 else spots.copy()
+            for form in ("fp16", "fp32"):
+                hc = np.zeros(nsub * 2, np.float32)
+                hb = np.zeros((nsx, nsx, m, m), np.float32)
+                e = centcmod(8, nsx, w["ncen"], w["N"], w["C"], m, w["p"], w["readnoise"], w["readbg"],
+                             w["addPoisson"], w["floor"], w["sig"], w["sky"], 0, 1.0, 1, 0, 1234, frames[0], pup,
+                             psf, hc, hb, 0.5, 0, None, mode, 0.0, pattern, None, w["threshType"], 0, 0, 1, 0, None)
+                e.set_form(form)
+                st = torch.cuda.Stream()
+                for k in range(max(args.warmup, 3)):
+                    e.set_io(phs=frames[k % 8])
+                    e.run_async(st)
+                st.synchronize()
+                lat = []
+                for k in range(nframes):
+                    e.set_io(phs=frames[k % 8])
+                    ea = torch.cuda.Event(enable_timing=True)
+                    eb = torch.cuda.Event(enable_timing=True)
+                    ea.record(st)
+                    e.run_async(st)
+                    eb.record(st)
+                    st.synchronize()
+                    lat.append(ea.elapsed_time(eb))
+                nlit = e.info()["nlit"]
+                p50 = float(np.percentile(lat, 50))
+                results["mode%d_%s" % (mode, form)] = {
+                    "ms_p50": p50, "ms_p99": float(np.percentile(lat, 99)),
+                    "subap_frames_per_s": nlit / (p50 / 1e3), "form_active": e.info()["form_active"]}
+                e.free()
+    head = results["mode1_fp16"]
+    line = {
+        "metric": "correlation-centroiding subap-frames/s (74x74 NGS, mode 1 FFT correlation, one frame per call)",
+        "value": head["subap_frames_per_s"], "unit": "subap-frames/s", "n_gpus": 1, "steps": nframes,
+        "warmup": max(args.warmup, 3), "ms_per_step": head["ms_p50"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp16 (per-subap scaled, f32 accumulate); correlation f32",
+        "data": "synthetic: seeded von Karman phase screens; Gaussian reference spot (sigma 1.5 px, 20x20)",
+        "config": {"workload": "elt74x74_ngs_correlation", "corrsize": cs, "modes": [1, 5],
+                   "io": "host numpy phase/cents/bimg, copies (correlation keeps the copying path)"},
+        "results": results, "clocks": clk.summary(), "gpu_launches": None,
+    }
+    print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------------- our arm
 
 def main():
@@ -648,21 +720,23 @@ def main():
     ap.add_argument("--frames", type=int, default=FPSTEP, help="frames per step")
     ap.add_argument("--e2e-frames", type=int, default=1000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="ngs74", choices=["ngs74", "serving", "precision", "lgs_batch", "recon"],
+    ap.add_argument("--workload", default="ngs74",
+                    choices=["ngs74", "serving", "precision", "lgs_batch", "recon", "corr"],
                     help="ngs74: the headline 74x74 NGS sensor; serving: 64 AO systems through the serving loop; "
                          "precision: per-form centroid error sweep vs the float64 oracle; "
-                         "lgs_batch: 6 LGS + 3 NGS sensors in one CUDA graph; recon: the reconstructor step")
+                         "lgs_batch: 6 LGS + 3 NGS sensors in one CUDA graph; recon: the reconstructor step; "
+                         "corr: correlation centroiding (modes 1 and 5) on the 74x74 sensor")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--precision-frames", type=int, default=8)
     ap.add_argument("--serve-inflight", type=int, default=16)
     args = ap.parse_args()
     ws, rank, local = dist_env()
-    if args.workload in ("serving", "precision", "lgs_batch", "recon") and args.impl == "ours":
+    if args.workload in ("serving", "precision", "lgs_batch", "recon", "corr") and args.impl == "ours":
         if rank == 0:
             from dasp_gb300 import build
             build.build()
             {"serving": run_serving, "precision": run_precision, "lgs_batch": run_lgs_batch,
-             "recon": run_recon}[args.workload](args)
+             "recon": run_recon, "corr": run_corr}[args.workload](args)
         return
 
     if args.impl == "reference":

@@ -49,6 +49,7 @@ __global__ void __launch_bounds__(kCorrThreads) wfs_corr_kernel(const WfsArgs a,
   float* s_cw = smem_corr;
   float* imgs = s_cw + (cw2d ? cc : 0);
   float* corr = imgs + c.TS * mm;
+  float* Ks = corr + c.TS * cc;  // the tile's patterns (or hc2r(pattern) for mode 1)
   if (cw2d)
     for (int k = tid; k < cc; k += blockDim.x) s_cw[k] = a.centWeight[k];
   WfsArgs ac = a;  // the centroid stage sees corrsize x corrsize images
@@ -69,22 +70,32 @@ __global__ void __launch_bounds__(kCorrThreads) wfs_corr_kernel(const WfsArgs a,
       const int s = w / mm, pix = w - s * mm;
       imgs[w] = a.bimg[(long long)s_frame[s] * a.bimgFrameStride + (long long)s_subap[s] * mm + pix];
     }
+    for (int w = tid; w < ns * cc; w += blockDim.x) {
+      const int s = w / cc, o = w - s * cc;
+      Ks[w] = c.K[(long long)s_subap[s] * cc + o];
+    }
     __syncthreads();
     // ---- correlation images ----
     for (int w = tid; w < ns * cc; w += blockDim.x) {
       const int s = w / cc, o = w - s * cc, y = o / cs, x = o - y * cs;
       const float* img = imgs + s * mm;
-      const float* K = c.K + (long long)s_subap[s] * cc;
+      const float* K = Ks + s * cc;
       float v = 0.f;
       if (c.mode == 1) {
+        // circular indices (y - p - off) mod cs and (x - q - off) mod cs: both
+        // differences lie in [-cs, cs), so one conditional wrap each
         const int off = (cs - m) / 2;
+        int kx0 = x - off;
+        if (kx0 < 0) kx0 += cs;
         for (int p = 0; p < m; p++) {
           int ky = y - p - off;
-          ky = ((ky % cs) + cs) % cs;
+          if (ky < 0) ky += cs;
+          const float* Krow = K + ky * cs;
+          const float* irow = img + p * m;
+          int kx = kx0;
           for (int q = 0; q < m; q++) {
-            int kx = x - q - off;
-            kx = ((kx % cs) + cs) % cs;
-            v += img[p * m + q] * K[ky * cs + kx];
+            v += irow[q] * Krow[kx];
+            kx = kx == 0 ? cs - 1 : kx - 1;
           }
         }
       } else if (c.mode == 3) {
@@ -175,9 +186,10 @@ cudaError_t launch_corr(const WfsArgs& a, CorrArgs c, int numSMs, cudaStream_t s
   const long long nwork = (long long)a.nlit * a.nframes;
   if (nwork == 0) return cudaSuccess;
   const int mm = a.m * a.m, cc = c.cs * c.cs;
-  int ts = 8192 / (mm + cc);
+  // per subaperture: image, correlation image, pattern
+  int ts = 12288 / (mm + 2 * cc);
   c.TS = ts < 1 ? 1 : (ts > kCorrMaxTS ? kCorrMaxTS : ts);
-  const int smem = (c.TS * (mm + cc) + (a.centWeightDim == 2 ? cc : 0)) * (int)sizeof(float);
+  const int smem = (c.TS * (mm + 2 * cc) + (a.centWeightDim == 2 ? cc : 0)) * (int)sizeof(float);
   cudaError_t e = cudaFuncSetAttribute(wfs_corr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   const long long ntiles = (nwork + c.TS - 1) / c.TS;

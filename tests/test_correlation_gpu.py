@@ -94,3 +94,27 @@ def test_correlation_update_codes():
     eng.run(0)
     np.testing.assert_allclose(c.cents, plain, atol=1e-6)
     eng.free()
+
+
+@pytest.mark.parametrize("cs", [8, 12])
+def test_mode1_pattern_from_transform_psf(cs):
+    """util/centroid.py builds mode 1's pattern from the user's reference
+    spot with transformPSF (util/correlation.py:20-51); the engine on the
+    pattern dasp_gb300.correlation.transform_psf makes matches the oracle,
+    and its correlation peak sits where a cross-correlation puts it."""
+    from dasp_gb300.correlation import transform_psf
+    c = Case(nsubx=8, p=8, N=16, C=16, m=8, ncen=6, sig=2e3, correlationCentroiding=1, phase_seed=4)
+    c.params["corrPattern"] = transform_psf(_reference_spots(c, cs) * 50.0)
+    corrimg = np.zeros((c.nsubx, c.nsubx, cs, cs), np.float32)
+    c.params["corrimg"] = corrimg
+    eng = c.engine()
+    eng.run(0)
+    orc = c.oracle("f64")
+    oc, _ = c.oracle_run(orc)
+    lit = c.lit()
+    ec = np.abs(c.cents.reshape(-1, 2)[lit] - oc.reshape(-1, 2)[lit]).max()
+    ci = corrimg.reshape(c.nsubaps, -1)[lit]
+    oi = orc.corrimg.reshape(c.nsubaps, -1)[lit]
+    assert np.abs(ci - oi).max() / max(np.abs(oi).max(), 1e-30) < 1e-4
+    assert ec < 1e-3, "centroid error %g px" % ec
+    eng.free()
