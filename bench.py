@@ -709,6 +709,72 @@ def run_corr(args):
     print(json.dumps(line), flush=True)
 
 
+def run_slope(args):
+    """Image input (centroidsFromImage through runSlope, the real-camera
+    path): the 74x74 sensor's 740x740 detector frame -- the noisy images of a
+    phase-mode frame laid out as the detector sees them -- centroided one
+    frame per call from a pinned host numpy array into host cents/bimg,
+    with zero-copy host I/O (default) and with copies.  Latency from the
+    call's entry to the centroids on the host."""
+    import time
+    import torch
+    torch.cuda.set_device(0)
+    w = WORKLOAD
+    pup = make_pupil()
+    nsx, m = w["nsubx"], w["m"]
+    nsub = nsx * nsx
+    screens = make_screens(2)
+    # detector frame: one noisy phase-mode frame's images, tiled
+    hc = np.zeros(nsub * 2, np.float32)
+    hb = np.zeros((nsx, nsx, m, m), np.float32)
+    ph = np.ascontiguousarray(make_frames(screens, 1, 3)[0])
+    e0 = make_engine(pup, ph, hc, hb)
+    e0.run(0)
+    det = np.ascontiguousarray(hb.transpose(0, 2, 1, 3).reshape(nsx * m, nsx * m))
+    e0.free()
+    results = {}
+    with ClockSampler(0) as clk:
+        for name, outputs, inp in (("zero_copy", True, True), ("copies", False, False)):
+            img = det.copy()
+            c2 = np.zeros(nsub * 2, np.float32)
+            b2 = np.zeros((nsx, nsx, m, m), np.float32)
+            from dasp_gb300.centcmod import centcmod
+            from dasp_gb300.screens import gaussian_psf
+            e = centcmod(8, nsx, w["ncen"], w["N"], w["C"], m, w["p"], w["readnoise"], w["readbg"],
+                         w["addPoisson"], w["floor"], w["sig"], w["sky"], 0, 1.0, 1, 0, 1234, ph, pup,
+                         gaussian_psf(w["C"], w["psf_fwhm"]), c2, b2, 0.5, 0, None, 0, 0.0, None, None,
+                         w["threshType"], 0, 0, 1, 0, None, img)
+            e.set_host_io(outputs=outputs, phase=inp)
+            for k in range(max(args.warmup, 3)):
+                e.runSlope(0)
+            lat = []
+            n = max(args.e2e_frames, 100)
+            t0 = time.perf_counter()
+            for k in range(n):
+                t1 = time.perf_counter()
+                e.runSlope(0)
+                lat.append((time.perf_counter() - t1) * 1e3)
+            wall = time.perf_counter() - t0
+            nlit = e.info()["nlit"]
+            results[name] = {"latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+                             "subap_frames_per_s": nlit * n / wall, "host_io_direct": e.info()["host_io_direct"]}
+            e.free()
+    head = results["zero_copy"]
+    line = {
+        "metric": "image-input centroiding subap-frames/s (74x74 NGS, 740x740 detector frame, runSlope, one "
+                  "frame per call, host arrays)",
+        "value": head["subap_frames_per_s"], "unit": "subap-frames/s", "n_gpus": 1, "steps": max(args.e2e_frames, 100),
+        "warmup": max(args.warmup, 3), "ms_per_step": head["latency_ms"]["p50"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: the noisy images of a seeded von Karman phase frame, tiled as a 740x740 detector frame",
+        "config": {"workload": "elt74x74_ngs_image_input", "detector": [nsx * m, nsx * m],
+                   "e2e": {"h2d_bytes_per_step": int(nsx * m * nsx * m * 4),
+                           "d2h_bytes_per_step": int(nsub * 2 * 4 + nsub * m * m * 4)}},
+        "results": results, "clocks": clk.summary(), "gpu_launches": None,
+    }
+    print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------------- our arm
 
 def main():
@@ -721,22 +787,23 @@ def main():
     ap.add_argument("--e2e-frames", type=int, default=1000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="ngs74",
-                    choices=["ngs74", "serving", "precision", "lgs_batch", "recon", "corr"],
+                    choices=["ngs74", "serving", "precision", "lgs_batch", "recon", "corr", "slope"],
                     help="ngs74: the headline 74x74 NGS sensor; serving: 64 AO systems through the serving loop; "
                          "precision: per-form centroid error sweep vs the float64 oracle; "
                          "lgs_batch: 6 LGS + 3 NGS sensors in one CUDA graph; recon: the reconstructor step; "
-                         "corr: correlation centroiding (modes 1 and 5) on the 74x74 sensor")
+                         "corr: correlation centroiding (modes 1 and 5) on the 74x74 sensor; "
+                         "slope: image input (runSlope) from a 740x740 detector frame")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--precision-frames", type=int, default=8)
     ap.add_argument("--serve-inflight", type=int, default=16)
     args = ap.parse_args()
     ws, rank, local = dist_env()
-    if args.workload in ("serving", "precision", "lgs_batch", "recon", "corr") and args.impl == "ours":
+    if args.workload in ("serving", "precision", "lgs_batch", "recon", "corr", "slope") and args.impl == "ours":
         if rank == 0:
             from dasp_gb300 import build
             build.build()
             {"serving": run_serving, "precision": run_precision, "lgs_batch": run_lgs_batch,
-             "recon": run_recon, "corr": run_corr}[args.workload](args)
+             "recon": run_recon, "corr": run_corr, "slope": run_slope}[args.workload](args)
         return
 
     if args.impl == "reference":

@@ -131,8 +131,10 @@ struct shwfs_handle {
   float* bimgMapped = nullptr;        // device alias of a pinned host bimg
   float* centsMapped = nullptr;       // ... of a pinned host cents
   const float* phsMapped = nullptr;   // ... of a pinned host phase
+  const float* imageMapped = nullptr; // ... of a pinned host detector image (runSlope)
   int hostIO = SHWFS_HOSTIO_OUTPUTS | SHWFS_HOSTIO_PHASE;  // zero-copy switches
   bool centsDirect = false, bimgDirect = false;  // this readout's kernels wrote the host outputs
+  bool inDirect = false;                         // ... read the host input
   std::vector<float> bimgStage;       // fallback: full copy, then host scatter
   bool scatterPending = false;
   std::vector<void*> registered;  // host ranges pinned by the engine
@@ -235,6 +237,7 @@ shwfs_status bind_io(shwfs_handle* h, shwfs_array& slot, const shwfs_array& a, D
   if (&slot == &h->bimg) h->bimgMapped = alias;
   if (&slot == &h->cents) h->centsMapped = alias;
   if (&slot == &h->phs) h->phsMapped = alias;
+  if (&slot == &h->inputImage) h->imageMapped = alias;
   // outputs start from the caller's contents: entries the engine does not
   // write (unlit subapertures, non-readout frames) come back unchanged
   if (copy_initial) CK(cudaMemcpy(mirror.p, a.data, count * sizeof(float), cudaMemcpyHostToDevice));
@@ -939,14 +942,26 @@ shwfs_status publish_outputs(shwfs_handle* h, cudaStream_t st, bool* sync) {
 // queue one image-input frame (centroidsFromImage)
 shwfs_status enqueue_slope(shwfs_handle* h, cudaStream_t st) {
   if (shwfs_status s = prepare_readout(h)) return s;
+  // zero-copy host I/O as for phase frames (counter noise, no correlation):
+  // the image kernel reads the pinned detector frame and, with the unlit
+  // kernel, writes the centroids and images into the pinned host arrays
+  const bool zc = h->noiseMode != SHWFS_NOISE_REFERENCE && !corr_active(h);
+  const bool zcOut = zc && (h->hostIO & SHWFS_HOSTIO_OUTPUTS);
   const float* img = (const float*)h->inputImage.data;
   if (!h->inputImage.on_device) {
-    CK(cudaMemcpyAsync(h->d_image.p, h->inputImage.data, (size_t)numel(h->inputImage) * sizeof(float),
-                       cudaMemcpyHostToDevice, st));
-    img = h->d_image.p;
+    if (zc && (h->hostIO & SHWFS_HOSTIO_PHASE) && h->imageMapped) {
+      img = h->imageMapped;
+      h->inDirect = true;
+    } else {
+      CK(cudaMemcpyAsync(h->d_image.p, h->inputImage.data, (size_t)numel(h->inputImage) * sizeof(float),
+                         cudaMemcpyHostToDevice, st));
+      img = h->d_image.p;
+    }
   }
-  float* cents = h->cents.on_device ? (float*)h->cents.data : h->d_cents.p;
-  float* bimg = h->bimg.on_device ? (float*)h->bimg.data : h->d_bimg.p;
+  h->centsDirect = !h->cents.on_device && zcOut && h->centsMapped && !h->imageOnly;
+  h->bimgDirect = !h->bimg.on_device && zcOut && h->bimgMapped;
+  float* cents = h->cents.on_device ? (float*)h->cents.data : (h->centsDirect ? h->centsMapped : h->d_cents.p);
+  float* bimg = h->bimg.on_device ? (float*)h->bimg.data : (h->bimgDirect ? h->bimgMapped : h->d_bimg.p);
   const int mm = h->nimg * h->nimg;
   if (!h->lit.empty()) {
     WfsArgs a = make_args(h, nullptr, cents, bimg, 1, 0, kPost);
@@ -987,7 +1002,7 @@ shwfs_status run_impl(shwfs_handle* h, cudaStream_t st, bool sync, float* elapse
   if (slope && is_none(h->inputImage)) return fail(SHWFS_ERR_STATE, "centmodule - inputImage is NULL");
   if (!slope && is_none(h->phs)) return fail(SHWFS_ERR_STATE, "no phase array is bound (image-input handle)");
   const bool readout = slope || readout_frame(h);
-  h->centsDirect = h->bimgDirect = false;
+  h->centsDirect = h->bimgDirect = h->inDirect = false;
   if (readout) {
     shwfs_status s;
     if (slope) {
@@ -1001,6 +1016,7 @@ shwfs_status run_impl(shwfs_handle* h, cudaStream_t st, bool sync, float* elapse
       if (!h->phs.on_device) {
         if (zc && !h->interp && (h->hostIO & SHWFS_HOSTIO_PHASE) && h->phsMapped) {
           phs = h->phsMapped;
+          h->inDirect = true;
         } else {
           CK(cudaMemcpyAsync(h->d_phs.p, h->phs.data, nph * sizeof(float), cudaMemcpyHostToDevice, st));
           phs = h->d_phs.p;
@@ -1591,6 +1607,7 @@ shwfs_status shwfs_get_info(const shwfs_handle* h, shwfs_info* info) {
   info->frames_read = h->framesRead;
   info->form = h->form;
   info->form_active = gemm_active(h) ? h->form : SHWFS_FORM_FP32;
+  info->host_io_direct = (h->centsDirect ? 1 : 0) | (h->bimgDirect ? 2 : 0) | (h->inDirect ? 4 : 0);
   return SHWFS_OK;
 }
 

@@ -199,6 +199,10 @@ typedef struct shwfs_info {
   int form_active;      /* form the next readout will use (GEMM forms fall back to
                            FP32 for 4-D PSFs, phase+amplitude, optical binning,
                            reference-stream noise or sizes beyond the GEMM kernel) */
+  int host_io_direct;   /* zero-copy host I/O of the last readout: 1 centroids and
+                           2 images written into the host arrays by the kernels,
+                           4 input (phase or detector image) read from the host
+                           array by the kernels */
 } shwfs_info;
 
 typedef struct shwfs_handle shwfs_handle;
