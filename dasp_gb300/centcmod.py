@@ -315,22 +315,31 @@ class centcmod:
 
     def set_io(self, phs=None, cents=None, bimg=None):
         """Rebind the borrowed phase/output arrays (same shapes)."""
+        if not hasattr(self, "_io_keep"):
+            self._io_keep = {}
+            self._io_desc = {}
         keeps = {}
         args = []
         for x, n in ((phs, "phs"), (cents, "cents"), (bimg, "bimg")):
             if x is None:
                 args.append(None)
                 continue
+            # an array bound before is still referenced here, so its buffer
+            # and descriptor are unchanged: reuse the descriptor
+            hit = self._io_desc.get((n, id(x)))
+            if hit is not None and hit[0] is x:
+                args.append(ctypes.byref(hit[1]))
+                continue
             keep: list = []
             desc = as_array(x, "f", n, keep)
             keeps[int(desc.data)] = keep
+            if isinstance(x, np.ndarray):
+                self._io_desc[(n, id(x))] = (x, desc)
             args.append(ctypes.byref(desc))
         check(_lib.lib().shwfs_set_io(self.centstruct, *args), "set_io")
         # host arrays stay pinned (registered in place) until the handle is
         # freed, so every distinct array bound here stays referenced until
         # then; rebinding the same few buffers costs nothing
-        if not hasattr(self, "_io_keep"):
-            self._io_keep = {}
         self._io_keep.update(keeps)
         if phs is not None:
             self.phs = phs

@@ -138,6 +138,15 @@ struct shwfs_handle {
   std::vector<float> bimgStage;       // fallback: full copy, then host scatter
   bool scatterPending = false;
   std::vector<void*> registered;  // host ranges pinned by the engine
+  // host arrays bound before: (data, bytes) -> device alias or null.  Their
+  // pinning lasts until the handle is freed, so rebinding one of them (a
+  // few buffers in turn, every frame) needs no driver query.
+  struct BoundHost {
+    const void* data;
+    size_t bytes;
+    float* alias;
+  };
+  std::vector<BoundHost> boundHost;
 
   // device state
   int device = 0;
@@ -203,6 +212,8 @@ shwfs_status check_f32(const shwfs_array& a, const char* name) {
   return SHWFS_OK;
 }
 
+float* pin_host(shwfs_handle* h, const void* data, size_t bytes);
+
 // bind a borrowed array; host pages are pinned in place (once) so the
 // per-frame copies are asynchronous DMA
 shwfs_status bind_io(shwfs_handle* h, shwfs_array& slot, const shwfs_array& a, DevBuf<float>& mirror, size_t count,
@@ -216,24 +227,16 @@ shwfs_status bind_io(shwfs_handle* h, shwfs_array& slot, const shwfs_array& a, D
     cudaError_t e = mirror.alloc(count);
     if (e != cudaSuccess) return fail(SHWFS_ERR_NOMEM, "device mirror allocation failed: %s", cudaGetErrorString(e));
   }
-  cudaPointerAttributes attr;
-  if (cudaPointerGetAttributes(&attr, a.data) == cudaSuccess && attr.type == cudaMemoryTypeUnregistered) {
-    if (cudaHostRegister((void*)a.data, count * sizeof(float), cudaHostRegisterDefault) == cudaSuccess)
-      h->registered.push_back((void*)a.data);
-  }
-  cudaGetLastError();  // a refused registration only costs copy speed
-  // device alias of the pinned host array (zero-copy I/O), only when the
-  // whole range is pinned and maps contiguously (a registration refused
-  // because a neighbour already pinned some of its pages leaves it partial)
+  const size_t bytes = count * sizeof(float);
   float* alias = nullptr;
-  cudaPointerAttributes last;
-  const char* lastByte = (const char*)a.data + count * sizeof(float) - 1;
-  if (cudaPointerGetAttributes(&attr, a.data) == cudaSuccess && attr.type == cudaMemoryTypeHost &&
-      attr.devicePointer && cudaPointerGetAttributes(&last, lastByte) == cudaSuccess &&
-      last.type == cudaMemoryTypeHost && last.devicePointer &&
-      (const char*)last.devicePointer - (const char*)attr.devicePointer == (ptrdiff_t)(count * sizeof(float) - 1))
-    alias = (float*)attr.devicePointer;
-  cudaGetLastError();
+  bool known = false;
+  for (const auto& b : h->boundHost)
+    if (b.data == a.data && b.bytes == bytes) {
+      alias = b.alias;
+      known = true;
+      break;
+    }
+  if (!known) alias = pin_host(h, a.data, bytes);
   if (&slot == &h->bimg) h->bimgMapped = alias;
   if (&slot == &h->cents) h->centsMapped = alias;
   if (&slot == &h->phs) h->phsMapped = alias;
@@ -242,6 +245,31 @@ shwfs_status bind_io(shwfs_handle* h, shwfs_array& slot, const shwfs_array& a, D
   // write (unlit subapertures, non-readout frames) come back unchanged
   if (copy_initial) CK(cudaMemcpy(mirror.p, a.data, count * sizeof(float), cudaMemcpyHostToDevice));
   return SHWFS_OK;
+}
+
+// pin a borrowed host range in place (once) so that per-frame copies are
+// asynchronous DMA, and return its device alias for zero-copy I/O, or null
+float* pin_host(shwfs_handle* h, const void* data, size_t bytes) {
+  cudaPointerAttributes attr;
+  if (cudaPointerGetAttributes(&attr, data) == cudaSuccess && attr.type == cudaMemoryTypeUnregistered) {
+    if (cudaHostRegister((void*)data, bytes, cudaHostRegisterDefault) == cudaSuccess)
+      h->registered.push_back((void*)data);
+  }
+  cudaGetLastError();  // a refused registration only costs copy speed
+  // device alias, only when the whole range is pinned and maps contiguously
+  // (a registration refused because a neighbour already pinned some of its
+  // pages leaves it partial)
+  float* alias = nullptr;
+  cudaPointerAttributes last;
+  const char* lastByte = (const char*)data + bytes - 1;
+  if (cudaPointerGetAttributes(&attr, data) == cudaSuccess && attr.type == cudaMemoryTypeHost &&
+      attr.devicePointer && cudaPointerGetAttributes(&last, lastByte) == cudaSuccess &&
+      last.type == cudaMemoryTypeHost && last.devicePointer &&
+      (const char*)last.devicePointer - (const char*)attr.devicePointer == (ptrdiff_t)(bytes - 1))
+    alias = (float*)attr.devicePointer;
+  cudaGetLastError();
+  if (h->boundHost.size() < 64) h->boundHost.push_back({data, bytes, alias});
+  return alias;
 }
 
 // updateTotSigArr (cmod/src/centmodule.c:2403-2427): float accumulation in
