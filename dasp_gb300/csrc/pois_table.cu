@@ -5,7 +5,10 @@
 #include <string.h>
 
 #include <cmath>
+#include <map>
 #include <mutex>
+#include <tuple>
+#include <utility>
 #include <set>
 #include <vector>
 
@@ -69,7 +72,11 @@ bool build_host_table(PoisTab* t) {
 }
 
 std::mutex g_mu;
-std::set<int> g_ready;
+std::map<int, const PoisTab*> g_ready;  // device -> table address
+
+std::mutex g_launch_mu;
+std::map<std::pair<int, const void*>, int> g_smemAttr;           // (device, kernel) -> its dynamic smem limit
+std::map<std::tuple<int, const void*, int, int>, int> g_occupancy;  // (device, kernel, smem, threads) -> CTAs/SM
 
 }  // namespace
 
@@ -78,7 +85,8 @@ cudaError_t pois_table_device(const PoisTab** out) {
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_ready.count(dev)) {
+  auto it = g_ready.find(dev);
+  if (it == g_ready.end()) {
     static PoisTab host;
     static bool built = false;
     if (!built) {
@@ -87,12 +95,39 @@ cudaError_t pois_table_device(const PoisTab** out) {
     }
     e = cudaMemcpyToSymbol(g_poistab, &host, sizeof(host));
     if (e != cudaSuccess) return e;
-    g_ready.insert(dev);
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_poistab);
+    if (e != cudaSuccess) return e;
+    it = g_ready.emplace(dev, static_cast<const PoisTab*>(p)).first;
   }
-  void* p = nullptr;
-  e = cudaGetSymbolAddress(&p, g_poistab);
+  *out = it->second;
+  return cudaSuccess;
+}
+
+cudaError_t kernel_smem_setup(const void* kern, int smem, int threads, int* ctasPerSM) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  *out = static_cast<const PoisTab*>(p);
+  std::lock_guard<std::mutex> lk(g_launch_mu);
+  // the limit is a property of the kernel: only ever raised, so a launch
+  // with less shared memory than an earlier one never lowers it under a
+  // later, larger launch
+  auto at = g_smemAttr.find(std::make_pair(dev, kern));
+  if (at == g_smemAttr.end() || at->second < smem) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    g_smemAttr[std::make_pair(dev, kern)] = smem;
+  }
+  if (!ctasPerSM) return cudaSuccess;
+  const auto key = std::make_tuple(dev, kern, smem, threads);
+  auto it = g_occupancy.find(key);
+  if (it == g_occupancy.end()) {
+    int ctas = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctas, kern, threads, (size_t)smem);
+    if (e != cudaSuccess) return e;
+    it = g_occupancy.emplace(key, ctas).first;
+  }
+  *ctasPerSM = it->second;
   return cudaSuccess;
 }
 

@@ -390,6 +390,12 @@ __device__ __forceinline__ float poisson_counter(Stream& st, float lam) {
 // (pois_table.cu)
 cudaError_t pois_table_device(const PoisTab** out);
 
+// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) and the occupancy query of
+// a kernel, done once per (device, kernel, shared memory, threads) and then
+// cached: host round trips that each frame would otherwise repeat
+// (ctasPerSM may be NULL)
+cudaError_t kernel_smem_setup(const void* kern, int smem, int threads, int* ctasPerSM);
+
 // Poisson(lam) from the pixel's stream: below lambda 64 the tabulated
 // sampler (two uniforms, poisson_tab), above PTRS (poisson_counter).  (Summing
 // tabulated Poisson(63) parts for larger lambda is exact too, but measured

@@ -190,7 +190,7 @@ cudaError_t launch_corr(const WfsArgs& a, CorrArgs c, int numSMs, cudaStream_t s
   int ts = 12288 / (mm + 2 * cc);
   c.TS = ts < 1 ? 1 : (ts > kCorrMaxTS ? kCorrMaxTS : ts);
   const int smem = (c.TS * (mm + 2 * cc) + (a.centWeightDim == 2 ? cc : 0)) * (int)sizeof(float);
-  cudaError_t e = cudaFuncSetAttribute(wfs_corr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaError_t e = kernel_smem_setup((const void*)wfs_corr_kernel, smem, kCorrThreads, nullptr);
   if (e != cudaSuccess) return e;
   const long long ntiles = (nwork + c.TS - 1) / c.TS;
   const long long cap = (long long)numSMs * 4;

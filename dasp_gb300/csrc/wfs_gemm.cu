@@ -721,8 +721,7 @@ cudaError_t launch_one(const WfsArgs& a, const GemmGeom& g, const float* iscale,
   const long long nwork = (long long)a.nlit * a.nframes;
   const long long ntiles = (nwork + kTileSubaps - 1) / kTileSubaps;
   const int grid = (int)(ntiles < numSMs ? (ntiles > 0 ? ntiles : 1) : numSMs);
-  cudaError_t e = cudaFuncSetAttribute(wfs_gemm_kernel<FMT, PASSES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       smem);
+  cudaError_t e = kernel_smem_setup((const void*)wfs_gemm_kernel<FMT, PASSES>, smem, kGemmThreads, nullptr);
   if (e != cudaSuccess) return e;
   wfs_gemm_kernel<FMT, PASSES><<<grid, kGemmThreads, smem, stream>>>(a, g, iscale, err);
   return cudaGetLastError();

@@ -89,7 +89,7 @@ cudaError_t launch_image(const WfsArgs& a, const float* img, int dims, int npxlx
                          cudaStream_t stream) {
   const int mm = a.m * a.m;
   const int smem = ((((a.centWeightDim == 2 ? mm : 0) + 3) & ~3) + a.TS * ((mm + 3) & ~3)) * 4;
-  cudaError_t e = cudaFuncSetAttribute(wfs_image_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaError_t e = kernel_smem_setup((const void*)wfs_image_kernel, smem, kThreads, nullptr);
   if (e != cudaSuccess) return e;
   const int ntiles = (a.nlit + a.TS - 1) / a.TS;
   const int grid = ntiles < numSMs * 8 ? (ntiles > 0 ? ntiles : 1) : numSMs * 8;

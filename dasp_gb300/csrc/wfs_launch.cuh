@@ -55,7 +55,7 @@ __global__ void psf_spectrum_kernel(const float* psf, int npsf, float2* out) {
 
 template <int N, int P>
 cudaError_t plain_launch(const WfsArgs& a, int grid, int smem, cudaStream_t stream) {
-  cudaError_t e = cudaFuncSetAttribute(wfs_plain_kernel<N, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaError_t e = kernel_smem_setup((const void*)wfs_plain_kernel<N, P>, smem, kThreads, nullptr);
   if (e != cudaSuccess) return e;
   wfs_plain_kernel<N, P><<<grid, kThreads, smem, stream>>>(a);
   return cudaGetLastError();
@@ -63,9 +63,7 @@ cudaError_t plain_launch(const WfsArgs& a, int grid, int smem, cudaStream_t stre
 
 template <int N, int P>
 cudaError_t plain_occupancy(int* ctas, int smem) {
-  cudaError_t e = cudaFuncSetAttribute(wfs_plain_kernel<N, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas, wfs_plain_kernel<N, P>, kThreads, smem);
+  return kernel_smem_setup((const void*)wfs_plain_kernel<N, P>, smem, kThreads, ctas);
 }
 
 template <int P>

@@ -452,10 +452,8 @@ cudaError_t launch_post(const WfsArgs& a0, int numSMs, cudaStream_t stream, unsi
     auto kern = pois ? (rnOn ? wfs_post_slots_kernel<true, true> : wfs_post_slots_kernel<false, true>)
                      : (rnOn ? wfs_post_slots_kernel<true, false> : wfs_post_slots_kernel<false, false>);
     if (a.calsource != 0) a.readNoise = 0.f;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
     int ctas = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctas, kern, kSlotThreads, smem);
+    cudaError_t e = kernel_smem_setup((const void*)kern, smem, kSlotThreads, &ctas);
     if (e != cudaSuccess) return e;
     if (ctas < 1) return cudaErrorInvalidConfiguration;
     const long long ntiles = (long long)((a.nsubaps + ts - 1) / ts) * a.nframes;
@@ -479,10 +477,8 @@ cudaError_t launch_post(const WfsArgs& a0, int numSMs, cudaStream_t stream, unsi
   }
   const int smem = (a.TS * mm + (a.centWeightDim == 2 ? mm : 0)) * (int)sizeof(float) +
                    (pois ? (int)sizeof(PoisTab) : 0);
-  cudaError_t e = cudaFuncSetAttribute(wfs_post_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e != cudaSuccess) return e;
   int ctas = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctas, wfs_post_kernel, kPostThreads, smem);
+  cudaError_t e = kernel_smem_setup((const void*)wfs_post_kernel, smem, kPostThreads, &ctas);
   if (e != cudaSuccess) return e;
   if (ctas < 1) return cudaErrorInvalidConfiguration;
   const long long ntiles = (nwork + a.TS - 1) / a.TS;
