@@ -1611,7 +1611,10 @@ shwfs_status shwfs_update(shwfs_handle* h, int code, const shwfs_value* v) {
 shwfs_status shwfs_free(shwfs_handle* h) {
   if (!h) return SHWFS_OK;
   cudaSetDevice(h->device);
-  if (h->stream) cudaStreamSynchronize(h->stream);
+  // work of this handle may be queued on the caller's streams (run_async,
+  // run_batch, batch graphs) and write into its pinned host words and
+  // aliases: let the device drain before they are freed and unregistered
+  cudaDeviceSynchronize();
   delete h;
   return SHWFS_OK;
 }
