@@ -48,6 +48,28 @@ def test_update_codes_match_reference_module():
     assert (cc.CALSOURCE, cc.REFCENTS, cc.OUTPUTPHASEARR) == (1, 18, 22)
 
 
+def test_extension_codes_match_header():
+    """The update codes and switches with no reference counterpart (noise
+    mode, tile size, compute form, zero-copy host I/O) agree between the C
+    header and the Python layer."""
+    import dasp_gb300.centcmod as cc
+    src = open(HEADER).read()
+
+    def code(name):
+        m = re.search(r"\b%s\s*=\s*(\d+)" % name, src)
+        assert m, name
+        return int(m.group(1))
+
+    assert code("SHWFS_NOISEMODE") == cc.NOISEMODE
+    assert code("SHWFS_TILESUBAPS") == cc.TILESUBAPS
+    assert code("SHWFS_FORM") == cc.FORM
+    assert code("SHWFS_HOSTIO") == cc.HOSTIO
+    assert code("SHWFS_HOSTIO_OUTPUTS") == cc.HOSTIO_OUTPUTS
+    assert code("SHWFS_HOSTIO_PHASE") == cc.HOSTIO_PHASE
+    for name, v in cc.FORMS.items():
+        assert code("SHWFS_FORM_%s" % name.upper()) == v
+
+
 def _c_struct_sizes():
     """sizeof the header's structs, from a tiny C program compiled here."""
     import subprocess
