@@ -39,7 +39,7 @@ EXPORTS = ("shwfs_initialise", "shwfs_run", "shwfs_run_slope", "shwfs_update", "
            "shwfs_server_remove_system", "shwfs_server_submit", "shwfs_server_poll", "shwfs_server_get_stats",
            "shwfs_server_clock", "shwfs_server_destroy", "shwfs_selftest_bounded_wait",
            "shwfs_screen_create", "shwfs_screen_add", "shwfs_screen_window", "shwfs_screen_read",
-           "shwfs_screen_free", "shwfs_mvm_update")
+           "shwfs_screen_free", "shwfs_mvm_update", "shwfs_test_correlation")
 
 NOALLOC_MAX_SUBAPS = 65536
 
@@ -152,6 +152,7 @@ def lib() -> ctypes.CDLL:
         L.shwfs_server_destroy.argtypes = [vp]
         L.shwfs_server_clock.restype = ctypes.c_double
         L.shwfs_sample_noise.argtypes = [ctypes.c_int, vp, ctypes.c_int64, ctypes.c_uint64, ctypes.c_uint64, vp, vp]
+        L.shwfs_test_correlation.argtypes = [ctypes.c_int, vp, vp]
         L.shwfs_selftest_bounded_wait.argtypes = [ctypes.c_int64, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
         L.shwfs_screen_create.argtypes = [ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp, ctypes.c_uint64,
                                           ctypes.POINTER(ctypes.c_void_p)]

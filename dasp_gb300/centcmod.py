@@ -62,6 +62,21 @@ def _is_array(x) -> bool:
     return isinstance(x, np.ndarray) or type(x).__module__.startswith("torch")
 
 
+def testcorrelation(img, corr):
+    """cmod.cent.testcorrelation (cmod/src/centmodule.c:3275-3309): ``corr``,
+    an n x n float32 half-complex pattern (as correlation mode 1 takes; see
+    dasp_gb300.correlation.transformPSF), is replaced in place by the
+    correlation of ``img`` (n x n float32) with it -- calcCorrelation with
+    corrsize = nimg = n, unnormalised.  Both are host numpy arrays."""
+    for a, name in ((img, "img"), (corr, "corr")):
+        if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags.c_contiguous):
+            raise ValueError("centmodule - %s must be float and contiguous" % name)
+    if img.ndim != 2 or corr.ndim != 2 or img.shape[0] != img.shape[1] or corr.shape != img.shape:
+        raise ValueError("centmodule - corr/img wrong shape")
+    check(_lib.lib().shwfs_test_correlation(int(img.shape[0]), img.ctypes.data, corr.ctypes.data),
+          "testcorrelation")
+
+
 class centcmod:
     """Shack-Hartmann WFS engine handle with the ``util.centcmod`` interface."""
 

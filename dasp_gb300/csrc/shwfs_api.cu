@@ -1619,6 +1619,29 @@ shwfs_status shwfs_free(shwfs_handle* h) {
   return SHWFS_OK;
 }
 
+shwfs_status shwfs_test_correlation(int n, const float* img, float* corr) {
+  if (n < 1 || n > 4096 || !img || !corr) return fail(SHWFS_ERR_INVALID, "centmodule - corr/img wrong shape");
+  const size_t nn = (size_t)n * n;
+  // the pattern's unnormalised inverse transform, as load_corr_pattern
+  std::vector<double> k;
+  hc2r_2d(corr, n, k);
+  std::vector<float> kf(nn);
+  for (size_t i = 0; i < nn; i++) kf[i] = (float)k[i];
+  float *dImg = nullptr, *dK = nullptr, *dOut = nullptr;
+  cudaError_t e = cudaMalloc((void**)&dImg, nn * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&dK, nn * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&dOut, nn * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemcpy(dImg, img, nn * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dK, kf.data(), nn * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = launch_test_corr(n, dImg, dK, dOut, nullptr);
+  if (e == cudaSuccess) e = cudaMemcpy(corr, dOut, nn * sizeof(float), cudaMemcpyDeviceToHost);
+  cudaFree(dImg);
+  cudaFree(dK);
+  cudaFree(dOut);
+  if (e != cudaSuccess) return fail(SHWFS_ERR_CUDA, "testcorrelation: %s", cudaGetErrorString(e));
+  return SHWFS_OK;
+}
+
 shwfs_status shwfs_get_info(const shwfs_handle* h, shwfs_info* info) {
   if (!h || !info) return fail(SHWFS_ERR_INVALID, "null argument");
   info->nsubx = h->nsubx;

@@ -180,7 +180,34 @@ __global__ void __launch_bounds__(kCorrThreads) wfs_corr_kernel(const WfsArgs a,
   }
 }
 
+// testcorrelation: the correlation of one n x n image with a pattern whose
+// inverse transform is K (mode 1 with corrsize = nimg = n: a circular
+// convolution, summed in the correlation kernel's order)
+__global__ void test_corr_kernel(int n, const float* __restrict__ img, const float* __restrict__ K,
+                                 float* __restrict__ out) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= n * n) return;
+  const int y = o / n, x = o - y * n;
+  float v = 0.f;
+  for (int p = 0; p < n; p++) {
+    int ky = y - p;
+    if (ky < 0) ky += n;
+    int kx = x;
+    for (int q = 0; q < n; q++) {
+      v += img[p * n + q] * K[ky * n + kx];
+      kx = kx == 0 ? n - 1 : kx - 1;
+    }
+  }
+  out[o] = v;
+}
+
 }  // namespace
+
+cudaError_t launch_test_corr(int n, const float* img, const float* K, float* out, cudaStream_t stream) {
+  const int nn = n * n;
+  test_corr_kernel<<<(nn + 255) / 256, 256, 0, stream>>>(n, img, K, out);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_corr(const WfsArgs& a, CorrArgs c, int numSMs, cudaStream_t stream) {
   const long long nwork = (long long)a.nlit * a.nframes;

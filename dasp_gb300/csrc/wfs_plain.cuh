@@ -760,6 +760,7 @@ __global__ void __launch_bounds__(kThreads) wfs_plain_kernel(const WfsArgs a) {
 
 // launcher of the unlit-subaperture kernel (wfs_unlit.cu)
 cudaError_t launch_unlit(const WfsArgs& a, const int* unlit, int nunlit, cudaStream_t stream);
+cudaError_t launch_test_corr(int n, const float* img, const float* K, float* out, cudaStream_t stream);
 // correlation centroiding (wfs_corr.cu)
 struct CorrArgs {
   int mode;       // correlationCentroiding, 1..5

@@ -225,6 +225,13 @@ shwfs_status shwfs_update(shwfs_handle* h, int code, const shwfs_value* val);
 /* cmod.cent.free: py_free, cmod/src/centmodule.c:3163-3186. */
 shwfs_status shwfs_free(shwfs_handle* h);
 
+/* cmod.cent.testcorrelation: py_testcorrelation, cmod/src/centmodule.c:
+ * 3275-3309.  img and corr are n x n float32 host arrays; corr holds a
+ * half-complex pattern (what correlation mode 1 takes) and is replaced by
+ * the correlation of img with it (calcCorrelation with corrsize = nimg = n,
+ * unnormalised).  Runs on the current device and waits for the result. */
+shwfs_status shwfs_test_correlation(int n, const float* img, float* corr);
+
 /* Message of the last failure on this thread ("" if none). */
 const char* shwfs_last_error(void);
 

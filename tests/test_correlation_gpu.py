@@ -118,3 +118,21 @@ def test_mode1_pattern_from_transform_psf(cs):
     assert np.abs(ci - oi).max() / max(np.abs(oi).max(), 1e-30) < 1e-4
     assert ec < 1e-3, "centroid error %g px" % ec
     eng.free()
+
+
+@pytest.mark.parametrize("n", [8, 9, 12, 16])
+def test_testcorrelation_module_function(n):
+    """cmod.cent.testcorrelation (cmod/src/centmodule.c:3275-3309): the
+    pattern array is replaced by calcCorrelation of the image with it
+    (corrsize = nimg), as the oracle's calc_correlation computes."""
+    from dasp_gb300.centcmod import testcorrelation
+    from dasp_gb300.correlation import transform_psf
+    from oracle.shwfs_oracle import calc_correlation
+    rng = np.random.default_rng(n)
+    img = (rng.random((n, n)) ** 2).astype(np.float32)
+    y, x = np.mgrid[0:n, 0:n] - (n - 1) / 2.0
+    corr = transform_psf((np.exp(-(x * x + y * y) / 4.0) * (1 + 0.2 * rng.random((n, n)))).astype(np.float32))
+    want = calc_correlation(n, n, corr.copy(), img, np.float64)
+    got = corr.copy()
+    testcorrelation(img, got)
+    assert np.abs(got - want).max() <= 1e-4 * np.abs(want).max()

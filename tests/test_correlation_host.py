@@ -79,3 +79,18 @@ def test_mode1_with_transformed_spot_is_cross_correlation(nimg, corrsize):
             want[ky, kx] = (pad * np.roll(s, (ky, kx), (0, 1))).sum()
     want *= corrsize * corrsize
     assert np.abs(got - want).max() <= 1e-5 * np.abs(want).max()
+
+
+def test_testcorrelation_argument_checks():
+    """testcorrelation rejects what py_testcorrelation rejects
+    (cmod/src/centmodule.c:3287-3299) before touching the device."""
+    from dasp_gb300.centcmod import testcorrelation
+    ok = np.zeros((8, 8), np.float32)
+    with pytest.raises(ValueError):
+        testcorrelation(ok.astype(np.float64), ok.copy())
+    with pytest.raises(ValueError):
+        testcorrelation(ok, np.zeros((8, 9), np.float32))
+    with pytest.raises(ValueError):
+        testcorrelation(np.zeros((8, 9), np.float32), np.zeros((8, 9), np.float32))
+    with pytest.raises(ValueError):
+        testcorrelation(np.asfortranarray(np.zeros((8, 8), np.float32))[:, ::-1], ok.copy())
