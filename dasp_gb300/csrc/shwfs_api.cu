@@ -897,13 +897,6 @@ shwfs_status enqueue_readout(shwfs_handle* h, const float* phs, float* cents, fl
       plainDirect = bimgHost != nullptr;
       if (plainDirect) bimg = bimgHost;
       WfsArgs a = make_args(h, phs, cents, bimg, nframes, phsStride, kForm | kNoiseCounter | kPost);
-      if (!h->imageOnly && !h->unlit.empty()) {
-        // the fused kernel zeroes the unlit centroids too
-        a.zeroUnlit = 1;
-        a.unlitList = h->d_unlit.p;
-        a.nunlit = (int)h->unlit.size();
-        postDone |= kPostDidUnlit;
-      }
       CK(h->entry->launch(a, grid, h->smem, st));
     }
     if (!h->unlit.empty() && !(postDone & kPostDidUnlit)) {

@@ -86,11 +86,8 @@ struct WfsArgs {
   // centroiding computes them afterwards from bimg)
   int skipCents;
   // 1: the noise/centroid kernel also zeroes the centroids of the unlit
-  // subapertures (set by launch_post when it takes that work over; for the
-  // fused FP32 kernel, the nunlit subapertures listed in unlitList)
+  // subapertures (set by launch_post when it takes that work over)
   int zeroUnlit;
-  const int* unlitList;
-  int nunlit;
   // optional second destination of the final images (same layout as bimg),
   // e.g. the device alias of a pinned host array; written by the
   // noise/centroid kernel when launch_post reports it

@@ -403,17 +403,6 @@ __global__ void __launch_bounds__(kThreads) wfs_plain_kernel(const WfsArgs a) {
   const int fA = bufA_floats(p, N, P), fB = bufB_floats(padded, C);
   const int persub = persub_floats(p, N, P, padded, C, m);
 
-  if (a.zeroUnlit) {
-    // unlit subapertures of every frame: centroids 0 (cmod/src/centmodule.c:
-    // 1964-1981), spread over the grid instead of a launch of their own
-    const long long total = (long long)a.nunlit * a.nframes;
-    for (long long w = blockIdx.x * (long long)blockDim.x + tid; w < total; w += (long long)gridDim.x * blockDim.x) {
-      const int f = (int)(w / a.nunlit), i = a.unlitList[w - (long long)f * a.nunlit];
-      float* c = a.cents + (long long)f * a.centsFrameStride;
-      c[2 * i] = 0.f;
-      c[2 * i + 1] = 0.f;
-    }
-  }
   for (int k = tid; k < p * p; k += blockDim.x) s_tilt[k] = a.tilt[k];
   for (int k = tid; k < C; k += blockDim.x) {
     s_binT[k] = a.binT[k];
