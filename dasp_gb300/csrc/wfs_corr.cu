@@ -177,6 +177,15 @@ __global__ void __launch_bounds__(kCorrThreads) wfs_corr_kernel(const WfsArgs a,
     }
     __syncthreads();
     centroid_tile(ac, ns, s_subap, s_frame, s_cw, [&](int s) { return corr + s * cc; });
+    if (ac.gaussianFit > 0 && ac.opticalBinning != 1) {
+      // the Gaussian fit logs its input in place (cmod/src/centmodule.c:
+      // 1087-1096); with correlation that input is the corrimg output
+      __syncthreads();
+      for (int s = warp; s < ns; s += nwarps) {
+        float* out = c.corrimg + (long long)s_frame[s] * c.corrimgFrameStride + (long long)s_subap[s] * cc;
+        for (int k = lane; k < cc; k += 32) out[k] = corr[s * cc + k];
+      }
+    }
   }
 }
 

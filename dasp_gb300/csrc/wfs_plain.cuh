@@ -375,6 +375,16 @@ __device__ __forceinline__ void post_tile(const WfsArgs& a, int ns, const int* s
     if (a.imageOnly != 0 || a.skipCents) return;
     __syncthreads();
     centroid_tile(a, ns, s_subap, s_frame, s_cw, img_of);
+    if (a.gaussianFit > 0 && a.opticalBinning != 1) {
+      // computeFit takes the log of the image in place before fitting
+      // (cmod/src/centmodule.c:1087-1096), and that image is the caller's
+      // bimg: the reference's output holds the log image after a Gaussian fit
+      __syncthreads();
+      for (int w = tid; w < ns * mm; w += blockDim.x) {
+        const int s = div_small(w, mm, inv_mm), pix = w - s * mm;
+        a.bimg[(long long)s_frame[s] * a.bimgFrameStride + (long long)s_subap[s] * mm + pix] = img_of(s)[pix];
+      }
+    }
 }
 
 template <int N, int P>

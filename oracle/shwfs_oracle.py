@@ -729,6 +729,9 @@ class CentOracle:
                     s = np.float32(s + a[i * n + j])
                     if a[i * n + j] < mx:
                         pos, mx = i * n + j, a[i * n + j]
+        if do_gauss:
+            # computeFit logs the caller's image in place (:1087-1096)
+            img.reshape(-1)[:] = a
         if not s >= 0:
             return np.float32(0), np.float32(0)
         startx = int(pos % n - fitsize // 2)
@@ -930,6 +933,9 @@ class CentOracle:
                 cx, cy = self._centroid(i, img[k])
                 cents[2 * i] = cx
                 cents[2 * i + 1] = cy
+                if self.gaussianFit > 0:
+                    # a Gaussian fit leaves the log image in bimg (:1087-1096)
+                    bimg[i] = img[k].astype(np.float32)
 
         if vec_cog and len(lit):
             if self.centWeightDim == 2:
@@ -973,6 +979,9 @@ class CentOracle:
             if self.parabolicFit != 0 or self.gaussianFit > 0:
                 cx, cy = self._fit(cimg, self.parabolicFit + self.gaussianFit, self.gaussianFit,
                                    self.correlationCentroiding)
+                if self.gaussianFit > 0 and cimg is not img:
+                    # the logged image is the correlation output (:1925)
+                    self.corrimg[i] = cimg.astype(np.float32)
             else:
                 if self.centWeightDim == 2:
                     w = self.centWeight
@@ -1058,9 +1067,12 @@ class CentOracle:
                     if self.imageOnly == 0:
                         if self.corrimg is None or self.corrimg.shape[-1] != self.corrsize:
                             self.corrimg = np.zeros((self.nsubaps, self.corrsize, self.corrsize), np.float32)
-                        cx, cy = self._centroid(i, b.reshape(m, m).astype(self.dt))
+                        work = b.reshape(m, m).astype(self.dt)
+                        cx, cy = self._centroid(i, work)
                         cents[2 * i] = cx
                         cents[2 * i + 1] = cy
+                        if self.gaussianFit > 0 and self.opticalBinning != 1:
+                            bimg[i] = work.astype(np.float32)
                 else:
                     if self.imageOnly == 0:
                         cents[2 * i] = 0

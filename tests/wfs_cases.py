@@ -72,6 +72,26 @@ class Case:
                         p["useBrightest"], p["preBinningFactor"], p["parabolicFit"], p["gaussianFitVals"],
                         inputImage, subapLocation)
 
+    # -- the reference's own module (oracle/_ref) --
+    def reference(self, phs=None, cents=None, bimg=None, inputImage=None, subapLocation=None, **over):
+        """The reference's cent module on this case's inputs.  Its outputs land
+        in ``self.ref_cents`` / ``self.ref_bimg`` (or the arrays given);
+        ``over`` replaces parameters for this handle only."""
+        from oracle.ref_cent import RefCent
+        p = dict(self.params)
+        p.update(over)
+        self.ref_phs = np.ascontiguousarray(self.phs if phs is None else phs, dtype=np.float32)
+        self.ref_cents = np.zeros((self.nsubaps * 2,), np.float32) if cents is None else cents
+        self.ref_bimg = np.zeros((self.nsubx, self.nsubx, self.m, self.m), np.float32) if bimg is None else bimg
+        psf = None if self.psf is None else np.ascontiguousarray(self.psf, dtype=np.float32)
+        return RefCent(p["nthreads"], self.nsubx, self.ncen, self.N, self.C, self.m, self.p, p["readnoise"],
+                       p["readbg"], p["addPoisson"], p["noiseFloor"], p["sig"], p["skybrightness"],
+                       p["calsource"], p["pxlPower"], p["nintegrations"], p["nlatency"], p["seed"],
+                       self.ref_phs, self.pup, psf, self.ref_cents, self.ref_bimg, p["minarea"],
+                       p["opticalBinning"], p["centWeight"], p["correlationCentroiding"], p["corrThresh"],
+                       p["corrPattern"], p["corrimg"], p["threshType"], p["imageOnly"], p["useBrightest"],
+                       p["preBinningFactor"], p["parabolicFit"], p["gaussianFitVals"], inputImage, subapLocation)
+
     # -- oracle --
     def oracle(self, mode="f32"):
         from oracle.shwfs_oracle import CentOracle
