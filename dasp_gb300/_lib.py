@@ -39,7 +39,7 @@ EXPORTS = ("shwfs_initialise", "shwfs_run", "shwfs_run_slope", "shwfs_update", "
            "shwfs_server_remove_system", "shwfs_server_submit", "shwfs_server_poll", "shwfs_server_get_stats",
            "shwfs_server_clock", "shwfs_server_destroy", "shwfs_selftest_bounded_wait",
            "shwfs_screen_create", "shwfs_screen_add", "shwfs_screen_window", "shwfs_screen_read",
-           "shwfs_screen_free", "shwfs_mvm_update", "shwfs_test_correlation")
+           "shwfs_screen_free", "shwfs_mvm_update", "shwfs_test_correlation", "shwfs_run_prenoise")
 
 NOALLOC_MAX_SUBAPS = 65536
 
@@ -130,6 +130,7 @@ def lib() -> ctypes.CDLL:
         L.shwfs_last_error.restype = ctypes.c_char_p
         L.shwfs_last_error.argtypes = []
         L.shwfs_run_async.argtypes = [vp, vp]
+        L.shwfs_run_prenoise.argtypes = [vp, P(ShwfsArray), P(ShwfsArray), P(ShwfsArray), P(ctypes.c_float)]
         L.shwfs_run_batch.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int64, vp, vp, vp]
         L.shwfs_set_io.argtypes = [vp, P(ShwfsArray), P(ShwfsArray), P(ShwfsArray)]
         L.shwfs_get_info.argtypes = [vp, P(ShwfsInfo)]

@@ -226,6 +226,24 @@ class centcmod:
         check(_lib.lib().shwfs_run_slope(self.centstruct, ctypes.byref(t)), "runSlope")
         return t.value
 
+    def run_prenoise(self, images, shot=None, readn=None):
+        """One readout from pre-noise images (noise injection; no reference
+        counterpart): ``images`` (nsubaps*nimg*nimg float32, numpy or CUDA
+        tensor) are the normalised, sky-added images the reference holds just
+        before poissonise; the engine adds the shot and read noise --
+        drawn by its noise generator, or ``shot`` / ``readn`` when given
+        (the Poisson draws and the read-noise values, per pixel) -- then
+        thresholds, centroids and writes cents/bimg as ``run`` does.
+        Returns the elapsed seconds."""
+        keep = []
+        a_img = as_array(images, "f", "images", keep)
+        a_shot = as_array(shot, "f", "shot", keep)
+        a_read = as_array(readn, "f", "readn", keep)
+        t = ctypes.c_float(0.0)
+        check(_lib.lib().shwfs_run_prenoise(self.centstruct, ctypes.byref(a_img), ctypes.byref(a_shot),
+                                            ctypes.byref(a_read), ctypes.byref(t)), "run_prenoise")
+        return t.value
+
     def free(self):
         if self.centstruct is not None:
             _lib.lib().shwfs_free(self.centstruct)

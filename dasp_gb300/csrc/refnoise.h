@@ -49,4 +49,30 @@ inline void seed_ref_rng(RefRng* r, uint64_t seed_t) {
 
 cudaError_t launch_refnoise(const RefNoiseArgs& a, RefRng* rng, int* status, cudaStream_t stream);
 
+// Poisson flag of every subaperture for frames whose pre-noise images come
+// from the caller: the reference poissonises subaperture i only when
+// totsig > 0, sky * fracSubArea > 0 or a sky array is set
+// (cmod/src/centmodule.c:1879), here from the handle's totals.
+cudaError_t launch_pois_flag(int nsubaps, const float* totsig, const float* frac, float sky, int skyArr,
+                             unsigned char* poisFlag, cudaStream_t stream);
+
+// Noise from caller-drawn values: shot[k] replaces the Poisson draw of pixel
+// k where the reference poissonises, readn[k] replaces (float)gsl_ran_gaussian
+// where readCCD draws (readNoise != 0 and no calibration source), then
+// readCCD's background and threshold (cmod/src/centmodule.c:785-817,
+// 1879-1881); unlit subapertures with imageOnly get readCCD of a zero image
+// (:1972-1976).  Either array may be null where the configuration draws
+// nothing from it.
+struct InjectArgs {
+  int nsubaps, m;
+  const int* subflag;
+  const unsigned char* poisFlag;
+  float* bimg;
+  const float* shot;
+  const float* readn;
+  float readNoise, readBg, floorv;
+  int threshType, addPoisson, calsource, imageOnly;
+};
+cudaError_t launch_inject_noise(const InjectArgs& a, cudaStream_t stream);
+
 }  // namespace shwfs

@@ -159,6 +159,7 @@ struct shwfs_handle {
   DevBuf<int> d_subapLoc;
   DevBuf<unsigned char> d_poisFlag;
   DevBuf<RefRng> d_rng;
+  DevBuf<float> d_inj;  // caller-drawn noise of shwfs_run_prenoise (shot, then read)
   const PlainEntry* entry = nullptr;
   int TS = 1, smem = 0, ctasPerSM = 1, numSMs = 1;
   int tileOverride = 0;  // SHWFS_TILESUBAPS; 0 = default
@@ -1016,18 +1017,110 @@ shwfs_status enqueue_slope(shwfs_handle* h, cudaStream_t st) {
   return enqueue_corr(h, cents, bimg, 1, st);
 }
 
-shwfs_status run_impl(shwfs_handle* h, cudaStream_t st, bool sync, float* elapsed, bool slope = false) {
+// caller-supplied pre-noise images (and optionally caller-drawn noise) of
+// shwfs_run_prenoise
+struct PrenoiseIn {
+  const shwfs_array* images;
+  const shwfs_array* shot;
+  const shwfs_array* readn;
+};
+
+// one readout from pre-noise images: the noise, threshold and post stages of
+// centroidsFromPhase (cmod/src/centmodule.c:1879-1981) on the caller's images
+shwfs_status enqueue_prenoise(shwfs_handle* h, const PrenoiseIn& in, cudaStream_t st) {
+  if (shwfs_status s = prepare_readout(h)) return s;
+  const size_t mm = (size_t)h->nimg * h->nimg, n = (size_t)h->nsubaps * mm;
+  float* cents = h->cents.on_device ? (float*)h->cents.data : h->d_cents.p;
+  float* bimg = h->bimg.on_device ? (float*)h->bimg.data : h->d_bimg.p;
+  CK(cudaMemcpyAsync(bimg, in.images->data, n * sizeof(float),
+                     in.images->on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+  const int nlit = (int)h->lit.size();
+  const long long ntiles = ((long long)nlit + h->TS - 1) / h->TS;
+  const int grid = (int)std::max<long long>(1, std::min<long long>(ntiles, (long long)h->numSMs * h->ctasPerSM));
+  const bool inject = !is_none(*in.shot) || !is_none(*in.readn);
+  if (inject || h->noiseMode == SHWFS_NOISE_REFERENCE)
+    CK(launch_pois_flag(h->nsubaps, h->d_totsig.p, h->d_frac.p, h->sky, h->skyIsArr ? 1 : 0, h->d_poisFlag.p, st));
+  if (inject) {
+    if (h->d_inj.n < 2 * n) CK(h->d_inj.alloc(2 * n));
+    InjectArgs g{};
+    g.nsubaps = h->nsubaps;
+    g.m = h->nimg;
+    g.subflag = h->d_subflag.p;
+    g.poisFlag = h->d_poisFlag.p;
+    g.bimg = bimg;
+    const shwfs_array* src[2] = {in.shot, in.readn};
+    for (int k = 0; k < 2; k++) {
+      if (is_none(*src[k])) continue;
+      CK(cudaMemcpyAsync(h->d_inj.p + k * n, src[k]->data, n * sizeof(float),
+                         src[k]->on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+    }
+    g.shot = is_none(*in.shot) ? nullptr : h->d_inj.p;
+    g.readn = is_none(*in.readn) ? nullptr : h->d_inj.p + n;
+    g.readNoise = h->readNoise;
+    g.readBg = h->readBg;
+    g.floorv = h->noiseFloor;
+    g.threshType = h->threshType;
+    g.addPoisson = h->addPoisson;
+    g.calsource = h->calsource;
+    g.imageOnly = h->imageOnly;
+    CK(launch_inject_noise(g, st));
+  } else if (h->noiseMode == SHWFS_NOISE_REFERENCE) {
+    RefNoiseArgs r{};
+    r.nthreads = h->nthreads;
+    r.subapStart = h->d_subapStart.p;
+    r.subflag = h->d_subflag.p;
+    r.poisFlag = h->d_poisFlag.p;
+    r.bimg = bimg;
+    r.m = h->nimg;
+    r.nexp = (int)mm;
+    r.readNoise = h->readNoise;
+    r.readBg = h->readBg;
+    r.floorv = h->noiseFloor;
+    r.threshType = h->threshType;
+    r.addPoisson = h->addPoisson;
+    r.calsource = h->calsource;
+    r.imageOnly = h->imageOnly;
+    CK(launch_refnoise(r, h->d_rng.p, h->d_status.p, st));
+  } else {
+    // counter streams on the caller's images, then the post stages
+    unsigned postDone = 0;
+    if (nlit) {
+      WfsArgs a = make_args(h, nullptr, cents, bimg, 1, 0, kNoiseCounter | kPost);
+      CK(launch_post(a, h->numSMs, st, &postDone));
+    }
+    if (!h->unlit.empty() && !(postDone & kPostDidUnlit)) {
+      WfsArgs a = make_args(h, nullptr, cents, bimg, 1, 0, 0);
+      CK(launch_unlit(a, h->d_unlit.p, (int)h->unlit.size(), st));
+    }
+    return enqueue_corr(h, cents, bimg, 1, st);
+  }
+  if (nlit) {
+    WfsArgs a = make_args(h, nullptr, cents, bimg, 1, 0, kPost);
+    CK(h->entry->launch(a, grid, h->smem, st));
+  }
+  if (!h->unlit.empty() && !h->imageOnly) {
+    WfsArgs a = make_args(h, nullptr, cents, bimg, 1, 0, 0);
+    CK(launch_unlit(a, h->d_unlit.p, (int)h->unlit.size(), st));
+  }
+  return enqueue_corr(h, cents, bimg, 1, st);
+}
+
+shwfs_status run_impl(shwfs_handle* h, cudaStream_t st, bool sync, float* elapsed, bool slope = false,
+                      const PrenoiseIn* pre = nullptr) {
   auto t0 = std::chrono::steady_clock::now();
   CK(cudaSetDevice(h->device));
   if (!st) st = h->stream;
   if (slope && is_none(h->inputImage)) return fail(SHWFS_ERR_STATE, "centmodule - inputImage is NULL");
-  if (!slope && is_none(h->phs)) return fail(SHWFS_ERR_STATE, "no phase array is bound (image-input handle)");
-  const bool readout = slope || readout_frame(h);
+  if (!slope && !pre && is_none(h->phs))
+    return fail(SHWFS_ERR_STATE, "no phase array is bound (image-input handle)");
+  const bool readout = slope || pre || readout_frame(h);
   h->centsDirect = h->bimgDirect = h->inDirect = false;
   if (readout) {
     shwfs_status s;
     if (slope) {
       s = enqueue_slope(h, st);
+    } else if (pre) {
+      s = enqueue_prenoise(h, *pre, st);
     } else {
       const size_t nph = (size_t)numel(h->phs);
       const float* phs = (const float*)h->phs.data;
@@ -1054,7 +1147,7 @@ shwfs_status run_impl(shwfs_handle* h, cudaStream_t st, bool sync, float* elapse
     if ((s = publish_outputs(h, st, &sync))) return s;
     h->framesRead++;
   }
-  if (!slope) {
+  if (!slope && !pre) {
     // py_run advances the integration counter; py_runSlope does not
     h->curInteg++;
     if (h->curInteg >= h->nintegrations + h->nlatency) h->curInteg = 0;
@@ -1062,7 +1155,8 @@ shwfs_status run_impl(shwfs_handle* h, cudaStream_t st, bool sync, float* elapse
   // the kernels' status word comes back in stream order with the outputs:
   // the tensor-core forms' noise/centroid kernel writes it to the pinned
   // host word, the reference-stream path copies it
-  const bool checkStatus = sync && readout && (h->noiseMode == SHWFS_NOISE_REFERENCE || gemm_active(h));
+  const bool checkStatus =
+      sync && readout && (h->noiseMode == SHWFS_NOISE_REFERENCE || (gemm_active(h) && !slope && !pre));
   if (checkStatus && h->noiseMode == SHWFS_NOISE_REFERENCE)
     CK(cudaMemcpyAsync(h->h_status, h->d_status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   if (sync) {
@@ -1355,6 +1449,36 @@ shwfs_status shwfs_run_async(shwfs_handle* h, void* stream) {
 shwfs_status shwfs_run_slope(shwfs_handle* h, float* elapsed_s) {
   if (!h) return fail(SHWFS_ERR_INVALID, "null handle");
   return run_impl(h, nullptr, true, elapsed_s, true);
+}
+
+shwfs_status shwfs_run_prenoise(shwfs_handle* h, const shwfs_array* images, const shwfs_array* shot,
+                                const shwfs_array* readn, float* elapsed_s) {
+  if (!h) return fail(SHWFS_ERR_INVALID, "null handle");
+  const shwfs_array none{};
+  if (!shot) shot = &none;
+  if (!readn) readn = &none;
+  const int64_t n = (int64_t)h->nsubaps * h->nimg * h->nimg;
+  if (!images || is_none(*images)) return fail(SHWFS_ERR_INVALID, "pre-noise images are required");
+  const shwfs_array* arrs[3] = {images, shot, readn};
+  const char* names[3] = {"images", "shot", "readn"};
+  for (int k = 0; k < 3; k++) {
+    if (is_none(*arrs[k])) continue;
+    if (arrs[k]->dtype != SHWFS_F32 || numel(*arrs[k]) != n)
+      return fail(SHWFS_ERR_INVALID, "%s must be float32 with nsubaps*nimg*nimg = %lld values", names[k],
+                  (long long)n);
+  }
+  if (h->opticalBinning == 1)
+    return fail(SHWFS_ERR_UNSUPPORTED, "pre-noise images with optical binning (images are binned before noise)");
+  if (h->phaseAmp)
+    return fail(SHWFS_ERR_UNSUPPORTED, "pre-noise images on a phase+amplitude handle (its Poisson flag needs the amplitude)");
+  const bool drawsShot = h->addPoisson == 1 && h->calsource == 0;
+  const bool drawsRead = h->readNoise != 0.f && h->calsource == 0;
+  const bool inject = !is_none(*shot) || !is_none(*readn);
+  if (inject && ((drawsShot && is_none(*shot)) || (drawsRead && is_none(*readn))))
+    return fail(SHWFS_ERR_INVALID, "injected noise needs %s for this configuration",
+                drawsShot && is_none(*shot) ? "shot (Poisson draws)" : "readn (read-noise draws)");
+  PrenoiseIn in{images, shot, readn};
+  return run_impl(h, nullptr, true, elapsed_s, false, &in);
 }
 
 shwfs_status shwfs_run_batch(shwfs_handle* h, int nframes, const float* phs, int64_t phs_frame_stride, float* cents,

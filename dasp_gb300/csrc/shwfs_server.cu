@@ -184,10 +184,16 @@ struct shwfs_server {
     while (true) {
       bool progress = false;
       std::vector<System*> admitNow, toRemove;
+      // the systems of this pass: add_system may grow `systems` (and move its
+      // storage) at any time, so the pass walks a copy of the pointers taken
+      // under the lock; each System stays where it is until the server goes
+      std::vector<System*> snap;
       {
         std::lock_guard<std::mutex> lk(mu);
         if (stop) break;
         wake = false;
+        snap.reserve(systems.size());
+        for (auto& sp : systems) snap.push_back(sp.get());
         // 1. admission in arrival order, against the budget
         for (auto& sp : systems) {
           System& s = *sp;
@@ -233,7 +239,7 @@ struct shwfs_server {
         progress = true;
       }
       // 2. retire finished frames
-      for (auto& sp : systems) {
+      for (System* sp : snap) {
         System& s = *sp;
         if (!s.busy) continue;
         const cudaError_t q = cudaEventQuery(s.ev);
@@ -255,7 +261,7 @@ struct shwfs_server {
       }
       // 3. launch released requests of idle systems
       const double tnow = now();
-      for (auto& sp : systems) {
+      for (System* sp : snap) {
         System& s = *sp;
         Request r{};
         {
@@ -299,7 +305,12 @@ struct shwfs_server {
       }
     }
     // drain: wait for frames on the device, then free everything
-    for (auto& sp : systems) {
+    std::vector<System*> all;
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      for (auto& sp : systems) all.push_back(sp.get());
+    }
+    for (System* sp : all) {
       if (sp->st) cudaStreamSynchronize(sp->st);
       release_system(*sp);
     }
@@ -345,6 +356,20 @@ shwfs_status shwfs_server_remove_system(shwfs_server* s, int system) {
   if (system < 0 || system >= (int)s->systems.size()) return SHWFS_ERR_INVALID;
   System& sys = *s->systems[system];
   sys.removing = true;
+  // frames still queued will not run: each completes with SHWFS_ERR_STATE so
+  // that every submitted request is reported exactly once
+  const double t = s->now();
+  for (const auto& r : sys.queue) {
+    shwfs_completion c{};
+    c.request = r.id;
+    c.system = sys.id;
+    c.status = SHWFS_ERR_STATE;
+    c.readout = 0;
+    c.done_s = t;
+    c.latency_s = t - r.release;
+    s->done.push_back(c);
+    s->completed++;
+  }
   sys.queue.clear();
   if (!sys.admitted) sys.failed = true;
   s->wake = true;

@@ -186,4 +186,50 @@ cudaError_t launch_refnoise(const RefNoiseArgs& a, RefRng* rng, int* status, cud
   return cudaGetLastError();
 }
 
+__global__ void pois_flag_kernel(int nsubaps, const float* __restrict__ totsig, const float* __restrict__ frac,
+                                 float sky, int skyArr, unsigned char* __restrict__ flag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nsubaps) flag[i] = totsig[i] > 0.f || sky * frac[i] > 0.f || skyArr != 0;
+}
+
+cudaError_t launch_pois_flag(int nsubaps, const float* totsig, const float* frac, float sky, int skyArr,
+                             unsigned char* poisFlag, cudaStream_t stream) {
+  pois_flag_kernel<<<(nsubaps + 255) / 256, 256, 0, stream>>>(nsubaps, totsig, frac, sky, skyArr, poisFlag);
+  return cudaGetLastError();
+}
+
+__global__ void inject_noise_kernel(const InjectArgs a) {
+  const long long mm = (long long)a.m * a.m;
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= mm * a.nsubaps) return;
+  const int i = (int)(k / mm);
+  const float rn = a.calsource == 0 ? a.readNoise : 0.f;
+  float v;
+  if (a.subflag[i] == 1) {
+    v = a.bimg[k];
+    if (a.addPoisson == 1 && a.calsource == 0 && a.poisFlag[i]) v = a.shot[k];
+  } else if (a.imageOnly != 0) {
+    v = 0.f;
+  } else {
+    return;
+  }
+  // readCCD: data += (float)gaussian + noiseMean, or data += noiseMean
+  if (rn == 0.f)
+    v += a.readBg;
+  else
+    v += a.readn[k] + a.readBg;
+  if (a.threshType == 0)
+    v = v < a.floorv ? 0.f : v - a.floorv;
+  else if (a.threshType == 1)
+    v = v < a.floorv ? 0.f : v;
+  a.bimg[k] = v;
+}
+
+cudaError_t launch_inject_noise(const InjectArgs& a, cudaStream_t stream) {
+  const long long n = (long long)a.m * a.m * a.nsubaps;
+  if (n == 0) return cudaSuccess;
+  inject_noise_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
 }  // namespace shwfs

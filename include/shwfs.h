@@ -242,6 +242,34 @@ const char* shwfs_last_error(void);
  * once the stream has drained. */
 shwfs_status shwfs_run_async(shwfs_handle* h, void* stream);
 
+/* One readout frame from caller-supplied pre-noise images ("noise
+ * injection"; no reference counterpart).  ``images`` holds, for every
+ * subaperture, the image centroidsFromPhase has just before poissonise:
+ * normalised, sky added (cmod/src/centmodule.c:1864-1872), float32
+ * nsubaps*nimg*nimg, host or device memory.  The engine then runs the rest
+ * of the readout as shwfs_run does -- shot noise, read noise, background
+ * and threshold (:1879-1881), brightest pixels, pixel power, correlation,
+ * centroids, calibration, references (:1882-1963), unlit subapertures
+ * (:1964-1981) -- and writes cents/bimg; the integration state is neither
+ * consulted nor advanced.
+ * shot and readn (each NULL, or a shwfs_array of the same shape and type):
+ *   both NULL  -- the handle's noise generator draws (SHWFS_NOISE_REFERENCE:
+ *                 the reference's per-thread PCG32/MT19937 streams, so the
+ *                 result equals the reference's noisy frame for the same
+ *                 pre-noise images, seed and nthreads);
+ *   otherwise  -- caller-drawn noise: shot[k] is used as the Poisson draw of
+ *                 pixel k wherever the reference poissonises (addPoisson,
+ *                 no calibration source, lit subaperture with light or sky),
+ *                 readn[k] as the value of (float)gsl_ran_gaussian(r,
+ *                 readNoise) wherever readCCD draws (readNoise != 0, no
+ *                 calibration source, lit subapertures and, with imageOnly,
+ *                 unlit ones).  An array the configuration draws from must
+ *                 be given; the other may be NULL.
+ * Rejected: optical binning and phase+amplitude handles
+ * (SHWFS_ERR_UNSUPPORTED).  Blocks until the outputs are written. */
+shwfs_status shwfs_run_prenoise(shwfs_handle* h, const shwfs_array* images, const shwfs_array* shot,
+                                const shwfs_array* readn, float* elapsed_s);
+
 /* Independent readout frames in one launch, all pointers device memory:
  * phase frames ``phs + f*phs_frame_stride`` (elements), outputs
  * ``cents + f*nsubaps*2`` and ``bimg + f*nsubaps*nimg*nimg``.  The
@@ -359,8 +387,9 @@ shwfs_status shwfs_selftest_bounded_wait(int64_t max_cycles, int* timed_out, int
  * exits; larger sensors are rejected with SHWFS_ERR_INVALID.
  *
  * The first call on a device looks up that array's device address (once per
- * device); make that first call before any stream capture.  The call waits
- * once on ``stream`` to read the subaperture counts.  All calls share the one
+ * device); make that first call before any stream capture.  Every call
+ * synchronises ``stream`` once, to read the subaperture counts back to the
+ * host before it launches the centroiding kernels.  All calls share the one
  * array, which keeps the last call's contents (each call rebuilds what it
  * reads), so calls whose GPU work overlaps -- other streams, other host
  * threads -- race and must not be issued.  ``err`` (may be NULL) receives a

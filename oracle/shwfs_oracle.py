@@ -877,11 +877,44 @@ class CentOracle:
         if self.curInteg >= self.nintegrations + self.nlatency:
             self.curInteg = 0
 
-    def _readout(self, phs, cents, bimg, amp):
+    def run_prenoise(self, images, cents, bimg, shot=None, readn=None):
+        """A readout from pre-noise images (the engine's shwfs_run_prenoise):
+        ``images`` (nsubaps, m, m) replace stages a3-a9 for the lit
+        subapertures; the noise comes from the reference's streams, or from
+        ``shot`` (the Poisson draws) / ``readn`` (the (float)gsl_ran_gaussian
+        values) per pixel where the reference would draw them.  The
+        integration state is not advanced."""
+        lit = np.nonzero(self.subflag == 1)[0]
+        img = np.asarray(images, np.float32).reshape(self.nsubaps, self.m, self.m)[lit].astype(self.dt)
+        frac = self.frac[lit].astype(self.dt)
+        pre = (img, self.totsig[lit], (self.dt(self.sky) * frac).astype(self.dt))
+        inj = None
+        if shot is not None or readn is not None:
+            inj = (None if shot is None else np.asarray(shot, np.float32).reshape(self.nsubaps, -1),
+                   None if readn is None else np.asarray(readn, np.float32).reshape(self.nsubaps, -1))
+        self._readout(None, cents.reshape(-1), bimg.reshape(self.nsubaps, self.m, self.m), None, pre=pre,
+                      inject=inj)
+
+    @staticmethod
+    def _readccd_injected(buf, readn, readBg, readNoise, floor_, threshType):
+        """readCCD (:785-817) with the gaussian draws given: float adds in the
+        reference's order, data += (g + noiseMean)."""
+        f32 = np.float32
+        if readNoise == 0:
+            v = (buf + f32(readBg)).astype(f32)
+        else:
+            v = (buf + (readn.astype(f32) + f32(readBg)).astype(f32)).astype(f32)
+        if threshType == 0:
+            v = np.where(v < f32(floor_), f32(0), (v - f32(floor_)).astype(f32))
+        elif threshType == 1:
+            v = np.where(v < f32(floor_), f32(0), v)
+        buf[:] = v.astype(f32)
+
+    def _readout(self, phs, cents, bimg, amp, pre=None, inject=None):
         m, npxl = self.m, self.m * self.m
         lit = np.nonzero(self.subflag == 1)[0]
         if len(lit):
-            img, totsig, skyv = self.pre_noise_images(phs, lit, amp)
+            img, totsig, skyv = self.pre_noise_images(phs, lit, amp) if pre is None else pre
             if self.opticalBinning == 1:
                 self._optically_bin(img)
                 nexp = 2 * self.ncen
@@ -901,14 +934,25 @@ class CentOracle:
                 if k is not None:
                     buf = np.ascontiguousarray(img[k].reshape(-1).astype(np.float32))
                     if do_noise and (totsig[k] > 0 or skyv[k] > 0 or self.skyArr is not None):
-                        lib.orc_poissonise(self.pcg[t].buf, buf.ctypes.data, nexp)
-                    lib.orc_readccd(self.mt[t].buf, buf.ctypes.data, nexp, self.readBg, readNoise,
-                                    self.noiseFloor, self.threshType)
+                        if inject is None:
+                            lib.orc_poissonise(self.pcg[t].buf, buf.ctypes.data, nexp)
+                        else:
+                            buf[:nexp] = inject[0][i, :nexp]
+                    if inject is None:
+                        lib.orc_readccd(self.mt[t].buf, buf.ctypes.data, nexp, self.readBg, readNoise,
+                                        self.noiseFloor, self.threshType)
+                    else:
+                        self._readccd_injected(buf[:nexp], None if inject[1] is None else inject[1][i, :nexp],
+                                               self.readBg, readNoise, self.noiseFloor, self.threshType)
                     img[k] = buf.reshape(m, m).astype(self.dt)
                 elif self.imageOnly != 0:
                     buf = np.zeros(npxl, np.float32)
-                    lib.orc_readccd(self.mt[t].buf, buf.ctypes.data, npxl, self.readBg, readNoise,
-                                    self.noiseFloor, self.threshType)
+                    if inject is None:
+                        lib.orc_readccd(self.mt[t].buf, buf.ctypes.data, npxl, self.readBg, readNoise,
+                                        self.noiseFloor, self.threshType)
+                    else:
+                        self._readccd_injected(buf, None if inject[1] is None else inject[1][i],
+                                               self.readBg, readNoise, self.noiseFloor, self.threshType)
                     bimg[i] = buf.reshape(m, m)
                 else:
                     cents[2 * i] = 0

@@ -344,3 +344,68 @@ def test_testcorrelation(n):
     got = pat.copy()
     ref_cent.testcorrelation(img, got)
     assert np.abs(got - want).max() <= 1e-5 * np.abs(want).max()
+
+
+def _ref_lambda(c, **over):
+    """Pre-noise images of the reference module: the same handle settings with
+    shot and read noise, background and threshold off, so bimg holds the
+    normalised, sky-added images the noisy run poissonises."""
+    quiet = dict(addPoisson=0, readnoise=0.0, readbg=0.0, noiseFloor=0.0, useBrightest=0, pxlPower=1.0)
+    quiet.update(over)
+    lam_c = np.zeros(c.nsubaps * 2, np.float32)
+    lam_b = np.zeros((c.nsubx, c.nsubx, c.m, c.m), np.float32)
+    ref = c.reference(cents=lam_c, bimg=lam_b, **quiet)
+    ref.run(0)
+    ref.free()
+    return lam_b.reshape(c.nsubaps, c.m, c.m).copy()
+
+
+def test_prenoise_oracle_equals_reference_noisy_frames():
+    # the oracle's run_prenoise on the reference's own pre-noise images, with
+    # the reference's streams, reproduces the reference's noisy frames
+    c = Case(nsubx=16, p=8, N=16, sig=3e3, addPoisson=1, readnoise=3.0, skybrightness=10.0, noiseFloor=6.0,
+             nthreads=5, seed=17, useBrightest=-20)
+    lam = _ref_lambda(c)
+    ref = c.reference()
+    orc = c.oracle()
+    oc = np.zeros(c.nsubaps * 2, np.float32)
+    ob = np.zeros((c.nsubaps, c.m, c.m), np.float32)
+    for f in range(3):
+        ref.run(0)
+        orc.run_prenoise(lam, oc, ob)
+        np.testing.assert_array_equal(c.ref_bimg.reshape(ob.shape)[c.lit()], ob[c.lit()])
+        np.testing.assert_allclose(c.ref_cents, oc, atol=1e-5, rtol=0)
+    ref.free()
+
+
+def test_prenoise_oracle_injected_draws():
+    # injected draws equal to the streams' own draws give the same frame
+    c = Case(nsubx=8, p=8, N=16, sig=3e3, addPoisson=1, readnoise=2.0, skybrightness=5.0, noiseFloor=2.0,
+             nthreads=1, seed=5, imageOnly=0)
+    lam = _ref_lambda(c)
+    ref = c.reference()
+    ref.run(0)
+    # the streams' draws, recovered from an oracle run without threshold
+    # and background: Poisson counts from a run with read noise off, read
+    # noise values as the difference of the two runs
+    o1 = c.oracle()
+    o1.update(7, -1e30)  # NOISEFLOOR far below: threshold keeps every pixel
+    o1.threshType = 1
+    o1.update(5, 0.0)
+    b1 = np.zeros((64, 8, 8), np.float32)
+    o1.run_prenoise(lam, np.zeros(128, np.float32), b1)
+    o2 = c.oracle()
+    o2.update(7, -1e30)
+    o2.threshType = 1
+    b2 = np.zeros((64, 8, 8), np.float32)
+    o2.run_prenoise(lam, np.zeros(128, np.float32), b2)
+    shot = b1.copy()
+    readn = (b2 - b1).astype(np.float32)
+    o3 = c.oracle()
+    oc = np.zeros(128, np.float32)
+    ob = np.zeros((64, 8, 8), np.float32)
+    o3.run_prenoise(lam, oc, ob, shot=shot, readn=readn)
+    lit = c.lit()
+    # equal up to the float rounding of recovering readn by subtraction
+    assert np.abs(ob[lit] - c.ref_bimg.reshape(64, 8, 8)[lit]).max() <= 1e-3
+    ref.free()

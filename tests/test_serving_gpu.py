@@ -156,3 +156,39 @@ def test_poisson_load_latency_and_throughput():
     srv.close()
     assert r["errors"] == 0 and r["requests"] == len(sched)
     assert r["latency_ms"]["p99"] < 50.0
+
+
+def test_removed_system_completes_every_queued_request():
+    # requests still queued when their system is removed complete with
+    # SHWFS_ERR_STATE (5); nothing stays pending
+    from dasp_gb300.serving import WfsServer
+    a = Case(nsubx=8, p=8, N=16, seed=2, **NOISY)
+    ph = _phases(a, 2, 50)
+    srv = WfsServer(4 << 30, max_inflight=2)
+    sid = srv.add_system(form="fp32", **_kw(a))
+    far = srv.clock() + 30.0
+    ids = [srv.submit(sid, ph[k % 2], release_s=far) for k in range(5)]
+    srv.remove_system(sid)
+    done = srv.drain(10)
+    assert sorted(c["request"] for c in done) == sorted(ids)
+    assert all(c["status"] == 5 for c in done)
+    assert srv.stats()["completed"] == srv.stats()["submitted"]
+    srv.close()
+
+
+def test_systems_added_while_the_dispatcher_runs():
+    # add_system grows the server's system list while the dispatcher walks it
+    from dasp_gb300.serving import WfsServer
+    srv = WfsServer(8 << 30, max_inflight=8)
+    cases = [Case(nsubx=8, p=8, N=16, seed=30 + k, **NOISY) for k in range(24)]
+    ph = _phases(cases[0], 2, 90)
+    outs = []
+    for k, c in enumerate(cases):
+        sid = srv.add_system(form="fp32", **_kw(c))
+        for j in range(2):
+            o = np.zeros(c.nsubaps * 2, np.float32)
+            outs.append(o)
+            srv.submit(sid, ph[j], out=o)
+    done = srv.drain(60)
+    assert len(done) == 48 and all(c["status"] == 0 for c in done)
+    srv.close()
