@@ -85,7 +85,7 @@ def make_engine(pup, phs, cents, bimg, noiseless=False):
 
 # DRAM bytes (read + write) per launch of the 64-frame step, from one ncu
 # capture of each kernel (commands and figures in profiles/)
-NCU_TRAFFIC = {"wfs_gemm_kernel": 162.4e6, "wfs_post_slots_kernel": 190.0e6}
+NCU_TRAFFIC = {"wfs_gemm_kernel": 162.4e6, "wfs_post_warp_kernel": None}
 
 
 def tensor_flops_per_subap():
@@ -1115,13 +1115,13 @@ def main():
         post_s = rl["post_kernel_ms"] / 1e3
         post_gbs = B_post * units / post_s / 1e9
         post = {"bound": "hbm", "achieved": post_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": post_gbs / hbm_peak,
-                "traffic": NCU_TRAFFIC.get("wfs_post_slots_kernel"), "peak_source": peak_src + " (copy bandwidth)",
+                "traffic": NCU_TRAFFIC.get("wfs_post_warp_kernel"), "peak_source": peak_src + " (copy bandwidth)",
                 "algorithmic_bytes_per_subap_frame": B_post,
-                "kernel": "wfs_post_slots_kernel (noise, threshold, centroids); timed between engine-recorded events",
+                "kernel": "wfs_post_warp_kernel (noise, threshold, centroids); timed between engine-recorded events",
                 "kernel_ms": rl["post_kernel_ms"],
                 "note": "issue-bound on the Philox/Poisson/normal samplers, far below its HBM roofline"}
         roof = dict(post if rl["post_kernel_ms"] > rl["formation_kernel_ms"] else gemm)
-        roof["kernels"] = {"wfs_gemm_kernel": gemm, "wfs_post_slots_kernel": post}
+        roof["kernels"] = {"wfs_gemm_kernel": gemm, "wfs_post_warp_kernel": post}
     roof["step_ms_per_launch"] = per_launch_ms
     roof["units_per_launch"] = units
     line = {

@@ -20,8 +20,17 @@ __device__ PoisTab g_poistab;
 
 namespace {
 
+// keep threshold of a column kept with probability q: the 32-bit coin keeps
+// the column when it is below round(q 2^32) (q = 1: always, up to 2^-32)
+uint32_t keep32(double q) {
+  if (q >= 1.0) return 0xffffffffu;
+  if (q <= 0.0) return 0u;
+  const double t = std::floor(q * 4294967296.0 + 0.5);
+  return t >= 4294967295.0 ? 0xffffffffu : (uint32_t)t;
+}
+
 // Walker/Vose alias table of Poisson(L) over 0..n-1 into prob/alias[o..o+n)
-void alias_table(const std::vector<double>& P, float* prob, uint8_t* alias) {
+void alias_table(const std::vector<double>& P, uint32_t* prob, uint8_t* alias) {
   const int n = (int)P.size();
   std::vector<double> q(n);
   std::vector<int> small, large;
@@ -30,14 +39,14 @@ void alias_table(const std::vector<double>& P, float* prob, uint8_t* alias) {
     (q[k] < 1.0 ? small : large).push_back(k);
   }
   for (int k = 0; k < n; k++) {
-    prob[k] = 1.0f;
+    prob[k] = 0xffffffffu;
     alias[k] = (uint8_t)k;
   }
   while (!small.empty() && !large.empty()) {
     const int l = small.back(), g = large.back();
     small.pop_back();
     large.pop_back();
-    prob[l] = (float)q[l];
+    prob[l] = keep32(q[l]);
     alias[l] = (uint8_t)g;
     q[g] = (q[g] + q[l]) - 1.0;
     (q[g] < 1.0 ? small : large).push_back(g);
@@ -48,9 +57,8 @@ void alias_table(const std::vector<double>& P, float* prob, uint8_t* alias) {
 bool build_host_table(PoisTab* t) {
   memset(t, 0, sizeof(*t));
   int pos = 0;
-  t->off[0] = 0;
-  t->len[0] = 1;
-  t->prob[pos] = 1.0f;  // Poisson(0) = 0
+  t->offlen[0] = 1u;  // entry 0, one column: Poisson(0) = 0
+  t->prob[pos] = 0xffffffffu;
   t->alias[pos++] = 0;
   for (int L = 1; L < kPoisTabL; L++) {
     std::vector<double> P;
@@ -63,8 +71,7 @@ bool build_host_table(PoisTab* t) {
     }
     P.back() += 1.0 - c;  // the last entry takes the remaining mass
     if (pos + (int)P.size() > kPoisCdfMax || P.size() > 255) return false;
-    t->off[L] = (uint16_t)pos;
-    t->len[L] = (uint16_t)P.size();
+    t->offlen[L] = ((uint32_t)pos << 8) | (uint32_t)P.size();
     alias_table(P, t->prob + pos, t->alias + pos);
     pos += (int)P.size();
   }

@@ -648,6 +648,8 @@ WfsArgs make_args(shwfs_handle* h, const float* phs, float* cents, float* bimg, 
   a.nframes = nframes;
   a.TS = h->TS;
   a.lit = h->d_lit.p;
+  a.unlit = h->d_unlit.p;
+  a.nunlit = (int)h->unlit.size();
   a.subflag = h->d_subflag.p;
   a.phs = phs;
   a.pup = h->d_pup.p;

@@ -34,6 +34,8 @@ struct WfsArgs {
   int nlit, nframes;
   int TS;  // subapertures per CTA tile
   const int* lit;
+  const int* unlit;  // unlit subapertures (nunlit), for kernels that zero their centroids
+  int nunlit;
   const int* subflag;  // per subaperture: 1 = lit
   const float* phs;
   const float* pup;
@@ -153,6 +155,12 @@ __device__ __forceinline__ U4 philox4x32_10_rk(U4 c, const PhiloxKeys& K) {
   return c;
 }
 
+// the streams' uniform in (0, 1) from one 32-bit word: 24 random bits,
+// centred in their bin
+__device__ __forceinline__ float u32_to_uniform(uint32_t w) {
+  return ((float)(w >> 8) + 0.5f) * (1.0f / 16777216.0f);
+}
+
 // Sequential uniform stream for one (frame, subap, pixel, purpose).
 struct CounterStream {
   U4 ctr;
@@ -180,9 +188,7 @@ struct CounterStream {
     return v;
   }
   // uniform in (0, 1): 24 random bits, centred in their bin
-  __device__ __forceinline__ float uniform() {
-    return ((float)(next_u32() >> 8) + 0.5f) * (1.0f / 16777216.0f);
-  }
+  __device__ __forceinline__ float uniform() { return u32_to_uniform(next_u32()); }
 };
 
 // The same stream as CounterStream(seed, ...), with the seed's round keys
@@ -212,9 +218,7 @@ struct KeyedStream {
     avail--;
     return v;
   }
-  __device__ __forceinline__ float uniform() {
-    return ((float)(next_u32() >> 8) + 0.5f) * (1.0f / 16777216.0f);
-  }
+  __device__ __forceinline__ float uniform() { return u32_to_uniform(next_u32()); }
 };
 
 // log Gamma(x) by the Stirling series with upward recursion below 7, as the
@@ -299,62 +303,60 @@ __device__ __forceinline__ float poisson_modal(float u, float lam) {
 //   Poisson(L): Walker's alias method (Walker 1977; table construction of
 //     Vose 1991) over the support 0..n_L-1 of Poisson(L), L = 1..63, built
 //     on the host in double (each support runs until the upper tail is
-//     below 2^-30, the last entry taking the remaining mass): one uniform u
-//     gives the column i = floor(u n_L) and, from its fractional part,
-//     either i or its alias -- two table reads, no search;
-//   Poisson(d): inversion of a second uniform, the first four CDF terms
-//     without branches, a short loop beyond them (probability < 2%).
+//     below 2^-30, the last entry taking the remaining mass): one 32-bit
+//     word w gives the column i = floor(w n_L / 2^32) and, from the low 32
+//     bits of w n_L, either i or its alias -- integer arithmetic, two table
+//     reads, no search;
+//   Poisson(d): inversion of a uniform, the first four CDF terms without
+//     branches, a short loop beyond them (probability < 2%).
 // The sum of independent Poisson variables is Poisson, so the draw is exact
-// up to the float rounding of the tables and the 2^-16 resolution of the
-// column fraction.  ~22 KB, staged into shared memory by the kernels that
+// up to the 2^-32 resolution of the keep thresholds and the float rounding
+// of the inversion.  ~22 KB, staged into shared memory by the kernels that
 // use it.
 constexpr int kPoisTabL = 64;      // L = 0..63
 constexpr int kPoisCdfMax = 4480;  // >= sum of the support lengths
 struct PoisTab {
-  float prob[kPoisCdfMax];   // probability of keeping the column itself
+  uint32_t prob[kPoisCdfMax];  // keep the column itself when the coin (32 bits) is below this
   uint8_t alias[kPoisCdfMax];
-  uint16_t off[kPoisTabL];
-  uint16_t len[kPoisTabL];
+  uint32_t offlen[kPoisTabL];  // first entry << 8 | support length (<= 255)
 };
 
-// Poisson(L), integer 0 <= L < 64, by the alias method on u
-__device__ __forceinline__ int poisson_table_int(const PoisTab& T, int L, float u) {
-  if (L <= 0) return 0;
-  const int n = T.len[L], o = T.off[L];
-  const float x = u * (float)n;
-  int i = (int)x;
-  if (i > n - 1) i = n - 1;  // u n may round up to n
-  return x - (float)i < T.prob[o + i] ? i : (int)T.alias[o + i];
+// Poisson(L), integer 0 <= L < 64, by the alias method on one 32-bit word w:
+// the column is floor(w n / 2^32), the coin the low 32 bits of w n (uniform
+// at 2^-32 / n resolution and independent of the column); L = 0 is a
+// one-column table that always gives 0
+__device__ __forceinline__ int poisson_table_int(const PoisTab& T, int L, uint32_t w) {
+  const uint32_t e = T.offlen[L], n = e & 0xffu, o = e >> 8;
+  const uint32_t i = __umulhi(w, n), coin = w * n;
+  return coin < T.prob[o + i] ? (int)i : (int)T.alias[o + i];
 }
 
-__device__ __forceinline__ float poisson_tab(const PoisTab& T, float u3, float u4, float lam) {
+__device__ __forceinline__ float poisson_tab(const PoisTab& T, uint32_t w3, float u4, float lam) {
   const int L = (int)lam;
   const float d = lam - (float)L;  // exact
-  int k = poisson_table_int(T, L, u3);
-  if (d > 0.0f) {
-    // smallest j with u4 <= F_j, F_j the CDF of Poisson(d)
-    float t = __expf(-d), F = t;
-    int k2 = u4 > F ? 1 : 0;
-    t *= d;
-    F += t;
-    k2 += u4 > F ? 1 : 0;
-    t *= d * 0.5f;
-    F += t;
-    k2 += u4 > F ? 1 : 0;
-    t *= d * (1.0f / 3.0f);
-    F += t;
-    if (u4 > F) {
-      int j = 3;
-      while (u4 > F && j < 40) {
-        j++;
-        t *= __fdividef(d, (float)j);
-        F += t;
-      }
-      k2 = j;
+  const int k = poisson_table_int(T, L, w3);
+  // Poisson(d), d < 1: smallest j with u4 <= F_j, F_j the CDF (d = 0 gives
+  // F_0 = 1, hence j = 0, without a branch)
+  float t = __expf(-d), F = t;
+  int k2 = u4 > F ? 1 : 0;
+  t *= d;
+  F += t;
+  k2 += u4 > F ? 1 : 0;
+  t *= d * 0.5f;
+  F += t;
+  k2 += u4 > F ? 1 : 0;
+  t *= d * (1.0f / 3.0f);
+  F += t;
+  if (u4 > F) {
+    int j = 3;
+    while (u4 > F && j < 40) {
+      j++;
+      t *= __fdividef(d, (float)j);
+      F += t;
     }
-    k += k2;
+    k2 = j;
   }
-  return (float)k;
+  return (float)(k + k2);
 }
 
 // Below lambda 64 the modal inversion above (one uniform); above, Hormann's
@@ -401,19 +403,29 @@ template <class Stream>
 __device__ __forceinline__ float poisson_counter_tab(Stream& st, float lam, const PoisTab& T) {
   if (!(lam > 0.0f)) return 0.0f;
   if (lam < kModalMaxLam) {
-    const float u3 = st.uniform(), u4 = st.uniform();
-    return poisson_tab(T, u3, u4, lam);
+    const uint32_t w3 = st.next_u32();
+    const float u4 = st.uniform();
+    return poisson_tab(T, w3, u4, lam);
   }
   return poisson_counter(st, lam);
 }
 
-// one standard normal deviate (Box-Muller, cosine branch)
-template <class Stream>
-__device__ __forceinline__ float normal_counter(Stream& st) {
-  const float u1 = st.uniform(), u2 = st.uniform();
+// one standard normal deviate from two uniforms (Box-Muller, cosine branch)
+__device__ __forceinline__ float normal_from_uniforms(float u1, float u2) {
   const float q = -2.0f * __logf(u1);  // > 0: u1 < 1
   const float r = q * rsqrtf(q);
   return r * __cosf(6.28318530717958648f * u2 - 3.14159265358979324f) * -1.0f;
+}
+
+__device__ __forceinline__ float normal_from_u32(uint32_t w1, uint32_t w2) {
+  return normal_from_uniforms(u32_to_uniform(w1), u32_to_uniform(w2));
+}
+
+// one standard normal deviate from the stream's next two uniforms
+template <class Stream>
+__device__ __forceinline__ float normal_counter(Stream& st) {
+  const float u1 = st.uniform(), u2 = st.uniform();
+  return normal_from_uniforms(u1, u2);
 }
 
 // floor(w / d) for 0 <= w < 2^22 and d >= 1 with the float reciprocal

@@ -175,37 +175,47 @@ __global__ void __launch_bounds__(kPostThreads, 4) wfs_post_kernel(const WfsArgs
   }
 }
 
-constexpr int kSlotThreads = 512;
-constexpr int kSlotCtasPerSM = 2;  // one copy of the Poisson tables per CTA
-constexpr int kSlotStages = 2;
-constexpr int kSlotMaxTS = 96;
+constexpr int kWarpThreads = 256;  // 8 warps per CTA
+constexpr int kWarpQ = 32;         // queued bright pixels per warp and chunk
+constexpr int kWarpMaxK = 16;      // subaperture-frames per chunk
+
+// Per-warp shared memory: two pixel buffers of bufPx floats (the chunk being
+// drawn and the next one, copied in asynchronously), the chunk's item table
+// (subaperture, frame, Poisson flag) for both buffers, the window-row
+// partial sums of the centroids and the bright-pixel queue.
+__host__ __device__ inline int warp_smem_floats(int bufPx, int ncen) {
+  return 2 * bufPx + 2 * 3 * kWarpMaxK + 2 * kWarpMaxK * ncen + 2 * kWarpQ;
+}
 
 // The common configuration (window CoG or image only; no brightest-pixel
-// selection, fit or optical binning) over tiles of TS consecutive
-// subaperture slots of one frame: a tile's pixels are one contiguous range
-// of bimg, so its copies into shared memory depend on nothing but the tile
-// index and run kSlotStages - 1 tiles ahead (cp.async groups), whatever the
-// lit pattern.  Unlit slots are copied but neither drawn nor written.
-// RN (read noise on) and POIS (Poisson on) are compile-time so that each
-// pixel's stream is consumed along a fixed path.  Pixels and streams are
-// those of wfs_post_kernel (same images); the window CoG sums each window
-// row first (one thread per subaperture row), then the rows.
+// selection, fit or optical binning), one warp per chunk of K consecutive
+// lit subaperture-frames: the chunk's pixels are drawn with the lanes over
+// the flattened pixel index (every lane busy whatever nimg is), bright
+// pixels (lambda >= 64, the rejection sampler) queued and drawn together
+// afterwards, then the window centroids from the chunk's images in shared
+// memory.  Warps are independent (no block barrier after the table load);
+// each copies its next chunk into shared memory with cp.async while it
+// draws the current one.  Unlit subapertures are not visited; their
+// centroids are zeroed at the end (zeroUnlit).  Pixels and streams are
+// those of wfs_post_kernel and of the fused FP32 kernel: the pixel of
+// subaperture i, frame f and index p draws from the counter stream
+// (seed, f, i, p) -- read-noise normal first, then the Poisson draw.
+// RN (read noise on) and POIS (Poisson on) are compile-time.
 template <bool RN, bool POIS>
-__global__ void __launch_bounds__(kSlotThreads, kSlotCtasPerSM)
-    wfs_post_slots_kernel(const WfsArgs a, const PoisTab* __restrict__ tab) {
+__global__ void __launch_bounds__(kWarpThreads, 3)
+    wfs_post_warp_kernel(const WfsArgs a, const PoisTab* __restrict__ tab, int K, int bufPx) {
   extern __shared__ __align__(16) float smem_post[];
-  __shared__ int s_nbright[2];  // bright-pixel queue length, alternating between tiles
-  __shared__ int s_bright[kPostBright];
-  __shared__ float s_brightv[kPostBright];
-  const int tid = threadIdx.x;
-  const int m = a.m, mm = m * m, TS = a.TS;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int m = a.m, mm = m * m, ncen = a.ncen;
   const bool cw2d = a.centWeightDim == 2;
   PoisTab* s_tab = reinterpret_cast<PoisTab*>(smem_post);
   float* s_cw = smem_post + (POIS ? sizeof(PoisTab) / sizeof(float) : 0);
-  // per stage: TS*mm pixels, then TS each of totsig, frac, subflag
-  float* ring = s_cw + ((cw2d ? mm : 0) + 3) / 4 * 4;
-  const int stageFloats = (TS * mm + 3 * TS + 3) / 4 * 4;
-  float* s_part = ring + kSlotStages * stageFloats;  // CoG row sums: TS*ncen pairs
+  float* wbase = s_cw + ((cw2d ? mm : 0) + 3) / 4 * 4 + warp * warp_smem_floats(bufPx, ncen);
+  // buffer b: pixels wbase + b * bufPx, item table info0 + b * 3 * kWarpMaxK
+  int* info0 = reinterpret_cast<int*>(wbase + 2 * bufPx);
+  float* s_rows = wbase + 2 * bufPx + 6 * kWarpMaxK;
+  int* q_idx = reinterpret_cast<int*>(s_rows + 2 * kWarpMaxK * ncen);
+  float* q_val = reinterpret_cast<float*>(q_idx + kWarpQ);
   if constexpr (POIS) {
     const int4* src = reinterpret_cast<const int4*>(tab);
     int4* dst = reinterpret_cast<int4*>(s_tab);
@@ -213,195 +223,262 @@ __global__ void __launch_bounds__(kSlotThreads, kSlotCtasPerSM)
   }
   if (cw2d)
     for (int k = tid; k < mm; k += blockDim.x) s_cw[k] = a.centWeight[k];
+  __syncthreads();
   // launched programmatically behind the image-formation kernel: everything
   // above reads constants only; bimg is read after that grid has completed
   // and its writes are visible (a no-op for an ordinary launch)
   asm volatile("griddepcontrol.wait;" ::: "memory");
   if (a.statusOut && blockIdx.x == 0 && tid == 0) *(volatile int*)a.statusOut = *(const volatile int*)a.statusIn;
 
-  const int tpf = (a.nsubaps + TS - 1) / TS;  // tiles per frame
-  const long long ntiles = (long long)tpf * a.nframes;
+  const long long items = (long long)a.nlit * a.nframes;
+  const long long nchunks = (items + K - 1) / K;
+  const long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + warp, nw = (long long)gridDim.x * (blockDim.x >> 5);
   const bool noise = a.mode & kNoiseCounter;
   const float rn = a.readNoise;
   const unsigned long long fbase = frame_base(a);
   const bool vec = (mm & 3) == 0 && (a.bimgFrameStride & 3) == 0 && ((uintptr_t)a.bimg & 15) == 0;
   const bool cents = a.imageOnly == 0 && !a.skipCents;
+  const int sx0 = (m - ncen) / 2;
+  const float inv_mm = 1.0f / (float)mm, inv_nc = 1.0f / (float)ncen;
+  // readCCD's threshold (cmod/src/centmodule.c:785-817) without branches:
+  // type 0 subtracts the floor, type 1 keeps the value, other types leave
+  // the pixel as it is
+  const float thr = (a.threshType == 0 || a.threshType == 1) ? a.floorv : -INFINITY;
+  const float tsub = a.threshType == 0 ? a.floorv : 0.f;
+  const bool pw1 = a.pxlPower == 1.f || a.pxlPower == 0.f;
+  const bool out2 = a.bimgOut != nullptr;
 
-  // copies of tile t (k-th of this CTA) into stage k % kSlotStages; one
-  // cp.async group per tile and thread, empty past the last tile
-  auto issue = [&](long long t, int k) {
-    if (t < ntiles) {
-      float* st = ring + (k % kSlotStages) * stageFloats;
-      const int f = (int)(t / tpf), s0 = (int)(t - (long long)f * tpf) * TS;
-      const int ns = min(TS, a.nsubaps - s0);
-      const float* src = a.bimg + (long long)f * a.bimgFrameStride + (long long)s0 * mm;
-      const int n = ns * mm;
-      if (vec) {
-        for (int c = tid; c < n / 4; c += blockDim.x)
-          asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(st + 4 * c)),
-                       "l"(src + 4 * c)
-                       : "memory");
-      } else {
-        for (int c = tid; c < n; c += blockDim.x)
-          asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(st + c)),
-                       "l"(src + c)
-                       : "memory");
+  // item table of chunk c into buffer b's table (lanes < K), then its
+  // pixels into buffer b with cp.async (one commit group per lane, empty
+  // past the end)
+  // the first item of this warp's current chunk as (frame cf, lit index
+  // cl), advanced by whole strides of nw chunks without a division
+  long long cf = (gw * K) / a.nlit;
+  int cl = (int)(gw * K - cf * a.nlit);
+  const long long strideItems = nw * (long long)K;
+  const long long sf = strideItems / a.nlit;
+  const int sl = (int)(strideItems - sf * a.nlit);
+  auto issue = [&](long long c, int b, long long f0, int l0) {
+    int* inf = info0 + b * 3 * kWarpMaxK;
+    if (c < nchunks) {
+      const long long w0 = c * K;
+      const int nk = (int)min((long long)K, items - w0);
+      if (lane < nk) {
+        int li = l0 + lane, f = (int)f0;
+        while (li >= a.nlit) {
+          li -= a.nlit;
+          f++;
+        }
+        const int i = a.lit[li];
+        inf[lane] = i;
+        inf[kWarpMaxK + lane] = f;
+        inf[2 * kWarpMaxK + lane] =
+            POIS ? (a.totsig[i] > 0.f || a.sky * a.frac[i] > 0.f || a.skyArr != nullptr) : 0;
       }
-      float* info = st + TS * mm;
-      for (int c = tid; c < 3 * ns; c += blockDim.x) {
-        const int which = c / ns, s = c - which * ns;
-        const void* g = which == 0 ? (const void*)(a.totsig + s0 + s)
-                                   : (which == 1 ? (const void*)(a.frac + s0 + s) : (const void*)(a.subflag + s0 + s));
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(info + which * TS + s)),
-                     "l"(g)
-                     : "memory");
+      __syncwarp();
+      float* dst = wbase + b * bufPx;
+      if (vec) {
+        const int nq = nk * mm / 4, q4 = mm / 4;
+        const float inv_q4 = 1.0f / (float)q4;
+        for (int q = lane; q < nq; q += 32) {
+          const int s = div_small(q, q4, inv_q4), r = q - s * q4;
+          const float* src = a.bimg + (long long)inf[kWarpMaxK + s] * a.bimgFrameStride + (long long)inf[s] * mm + 4 * r;
+          asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst + 4 * q)),
+                       "l"(src)
+                       : "memory");
+        }
+      } else {
+        for (int g = lane; g < nk * mm; g += 32) {
+          const int s = div_small(g, mm, inv_mm), pix = g - s * mm;
+          const float* src = a.bimg + (long long)inf[kWarpMaxK + s] * a.bimgFrameStride + (long long)inf[s] * mm + pix;
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst + g)),
+                       "l"(src)
+                       : "memory");
+        }
       }
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
   };
 
-  long long t = blockIdx.x;
-  int k = 0;
-  for (int d = 0; d < kSlotStages - 1; d++) issue(t + (long long)d * gridDim.x, d);
-  if (tid == 0) s_nbright[0] = s_nbright[1] = 0;
-  const int ncen = a.ncen, sx0 = (m - ncen) / 2;
-  const float inv_mm = 1.0f / (float)mm, inv_nc = 1.0f / (float)ncen;
-  for (; t < ntiles; t += gridDim.x, k++) {
-    asm volatile("cp.async.wait_group %0;" ::"n"(kSlotStages - 2) : "memory");
-    // tile t is in shared memory and every thread is done with tile t - 1,
-    // whose stage is refilled next
-    __syncthreads();
-    issue(t + (long long)(kSlotStages - 1) * gridDim.x, k + kSlotStages - 1);
-    if (tid == 0) s_nbright[(k + 1) & 1] = 0;  // the next tile's queue
-    int* nbright = &s_nbright[k & 1];
-    float* imgs = ring + (k % kSlotStages) * stageFloats;
-    const float* s_tot = imgs + TS * mm;
-    const float* s_frac = s_tot + TS;
-    const int* s_flag = reinterpret_cast<const int*>(s_frac + TS);
-    const int f = (int)(t / tpf), s0 = (int)(t - (long long)f * tpf) * TS;
-    const int ns = min(TS, a.nsubaps - s0);
-    float* dstF = a.bimg + (long long)f * a.bimgFrameStride + (long long)s0 * mm;
-    // noise and threshold of pixel pix of slot s (pf: Poisson applies)
-    // (bright: lambda >= 64, the rejection sampler; otherwise the tables,
-    // whose path the first loop compiles without the rejection loop)
-    auto draw = [&](float v, int s, int pix, bool pf, auto bright) {
-      KeyedStream st(a.philoxKeys, fbase + f, s0 + s, pix, 0);
+  int b = 0;
+  issue(gw, 0, cf, cl);
+  for (long long c = gw; c < nchunks; c += nw, b ^= 1) {
+    const long long w0 = c * K;
+    const int nk = (int)min((long long)K, items - w0);
+    cf += sf;  // the next chunk of this warp
+    cl += sl;
+    if (cl >= a.nlit) {
+      cl -= a.nlit;
+      cf++;
+    }
+    issue(c + nw, b ^ 1, cf, cl);  // the next chunk's copies, in flight while this one is drawn
+    asm volatile("cp.async.wait_group 1;" ::: "memory");
+    __syncwarp();
+    float* img = wbase + b * bufPx;
+    const int* s_i = info0 + b * 3 * kWarpMaxK;
+    const int* s_f = s_i + kWarpMaxK;
+    const int* s_pf = s_i + 2 * kWarpMaxK;
+    // noise and threshold of a pixel drawn from its stream (seed, frame,
+    // subaperture, pixel): the read-noise normal takes the block's first two
+    // uniforms, the tabulated Poisson draw the next two (the first two
+    // without read noise) -- KeyedStream's order, with the block explicit
+    auto draw_fast = [&](float v, uint32_t sub, uint32_t frm, int pix, int pf) {
+      U4 c;
+      c.x = 0u;
+      c.y = (uint32_t)pix;
+      c.z = sub;
+      c.w = frm;
+      const U4 r = philox4x32_10_rk(c, a.philoxKeys);
       float g = 0.f;
-      if constexpr (RN) g = normal_counter(st);
+      if constexpr (RN) g = normal_from_u32(r.x, r.y);
       if constexpr (POIS) {
         if (pf) {
-          if constexpr (decltype(bright)::value) {
-            v = poisson_counter_tab(st, v, *s_tab);
-          } else if (v > 0.f) {  // as poisson_counter_tab for 0 < lambda < 64
-            const float u3 = st.uniform();
-            const float u4 = st.uniform();
-            v = poisson_tab(*s_tab, u3, u4, v);
-          } else {
-            v = 0.f;
-          }
+          const uint32_t w3 = RN ? r.z : r.x, w4 = RN ? r.w : r.y;
+          v = v > 0.f ? poisson_tab(*s_tab, w3, u32_to_uniform(w4), v) : 0.f;
         }
       }
       if constexpr (RN)
         v += rn * g + a.readBg;
       else
         v += a.readBg;
-      return threshold_px(v, a.floorv, a.threshType);
+      return v < thr ? 0.f : v - tsub;
     };
-    float* outF = a.bimgOut ? a.bimgOut + (long long)f * a.bimgFrameStride + (long long)s0 * mm : nullptr;
-    auto store = [&](int w, float v) {
-      if (a.pxlPower == 2.f)
-        v = v * v;
-      else if (a.pxlPower != 1.f && a.pxlPower != 0.f)
-        v = powf(v, a.pxlPower);
-      dstF[w] = v;
-      if (outF) outF[w] = v;
-      imgs[w] = v;
+    // the rejection-sampler path (lambda >= 64): the same stream, continued
+    auto draw_bright = [&](float v, uint32_t sub, uint32_t frm, int pix) {
+      KeyedStream st(a.philoxKeys, frm, (int)sub, pix, 0);
+      float g = 0.f;
+      if constexpr (RN) g = normal_counter(st);
+      if constexpr (POIS) v = poisson_counter_tab(st, v, *s_tab);
+      if constexpr (RN)
+        v += rn * g + a.readBg;
+      else
+        v += a.readBg;
+      return v < thr ? 0.f : v - tsub;
     };
-    for (int w = tid; w < ns * mm; w += blockDim.x) {
-      const int s = div_small(w, mm, inv_mm);
-      if (s_flag[s] != 1) continue;
-      float v = imgs[w];
-      if (noise) {
-        const bool pf = POIS && (s_tot[s] > 0.f || a.sky * s_frac[s] > 0.f || a.skyArr);
-        if (POIS && pf && v >= kModalMaxLam) {
-          // lambda >= 64 (the rejection sampler): queued and drawn after
-          // the others by the whole CTA, so that one such pixel does not
-          // hold the other lanes of its warp (same streams, same draws)
-          const int slot = atomicAdd(nbright, 1);
-          if (slot < kPostBright) {
-            s_bright[slot] = w;
-            s_brightv[slot] = v;
-            continue;
-          }
-          // queue full: drawn here
-          store(w, draw(v, s, w - s * mm, pf, std::true_type{}));
-          continue;
-        }
-        v = draw(v, s, w - s * mm, pf, std::false_type{});
-      }
-      store(w, v);
+    auto store = [&](long long off, int g, float v) {
+      if (!pw1) v = a.pxlPower == 2.f ? v * v : powf(v, a.pxlPower);
+      a.bimg[off] = v;
+      if (out2) a.bimgOut[off] = v;
+      if (cents) img[g] = v;
+    };
+    int nq = 0;  // bright pixels queued (warp-uniform)
+    const int npx = nk * mm;
+    // this lane's pixel g = g0 + lane is pixel pix of item s; the item's
+    // subaperture, frame, Poisson flag and output offset are cached while
+    // s stays the same
+    int s = 0, pix = lane;
+    while (pix >= mm) {
+      pix -= mm;
+      s++;
     }
-    if (a.zeroUnlit) {
-      // unlit subapertures: centroids 0 (cmod/src/centmodule.c:1964-1981)
-      float* c = a.cents + (long long)f * a.centsFrameStride + 2LL * s0;
-      for (int s = tid; s < ns; s += blockDim.x)
-        if (s_flag[s] != 1) {
-          c[2 * s] = 0.f;
-          c[2 * s + 1] = 0.f;
+    int cs = -1, ipf = 0;
+    uint32_t isub = 0, ifrm = 0;
+    long long obase = 0;
+    for (int g0 = 0; g0 < npx; g0 += 32) {
+      const int g = g0 + lane;
+      const bool in = g < npx;
+      if (in && s != cs) {
+        cs = s;
+        isub = (uint32_t)s_i[s];
+        ifrm = (uint32_t)(fbase + (unsigned long long)s_f[s]);
+        ipf = s_pf[s];
+        obase = (long long)s_f[s] * a.bimgFrameStride + (long long)s_i[s] * mm;
+      }
+      float v = in ? img[g] : 0.f;
+      bool queued = false, bright = false;
+      if constexpr (POIS) {
+        bright = noise && in && ipf && v >= kModalMaxLam;
+        const unsigned bm = __ballot_sync(0xffffffffu, bright);
+        if (bm) {
+          if (bright) {
+            const int slot = nq + __popc(bm & ((1u << lane) - 1u));
+            if (slot < kWarpQ) {
+              q_idx[slot] = g;
+              q_val[slot] = v;
+              queued = true;
+            }
+          }
+          nq += __popc(bm);
         }
+      }
+      if (in && !queued) {
+        if (noise) v = bright ? draw_bright(v, isub, ifrm, pix) : draw_fast(v, isub, ifrm, pix, ipf);
+        store(obase + pix, g, v);
+      }
+      pix += 32;
+      while (pix >= mm) {
+        pix -= mm;
+        s++;
+      }
     }
     if constexpr (POIS) {
-      if (noise) {
-        __syncthreads();
-        const int nb = min(*nbright, kPostBright);
-        for (int b = tid; b < nb; b += blockDim.x) {
-          const int w = s_bright[b];
-          const int s = div_small(w, mm, inv_mm);
-          store(w, draw(s_brightv[b], s, w - s * mm, true, std::true_type{}));
+      if (noise && nq) {
+        __syncwarp();
+        for (int q = lane; q < min(nq, kWarpQ); q += 32) {
+          const int g = q_idx[q];
+          const int sq = div_small(g, mm, inv_mm), pq = g - sq * mm;
+          const long long off = (long long)s_f[sq] * a.bimgFrameStride + (long long)s_i[sq] * mm + pq;
+          store(off, g, draw_bright(q_val[q], (uint32_t)s_i[sq], (uint32_t)(fbase + (unsigned long long)s_f[sq]), pq));
         }
       }
     }
-    if (!cents) continue;
-    __syncthreads();
-    // centred-window CoG: sums of each window row (one thread per
-    // subaperture row), then of the rows (one thread per subaperture)
-    for (int pr = tid; pr < ns * ncen; pr += blockDim.x) {
-      const int s = div_small(pr, ncen, inv_nc), rr = pr - s * ncen;
-      float ps = 0.f, px = 0.f;
-      if (s_flag[s] == 1) {
+    if (cents) {
+      __syncwarp();
+      // centred-window CoG: sums of each window row (one lane per item
+      // row), then of the rows (one lane per item), in a fixed order
+      for (int t = lane; t < nk * ncen; t += 32) {
+        const int s = div_small(t, ncen, inv_nc), rr = t - s * ncen;
         const int r = sx0 + rr;
-        const float* row = imgs + s * mm + r * m + sx0;
+        const float* row = img + s * mm + r * m + sx0;
         const float* wrow = cw2d ? s_cw + r * m + sx0
-                                 : (a.centWeightDim == 4 ? a.centWeight + (long long)(s0 + s) * mm + r * m + sx0 : nullptr);
-        for (int c = 0; c < ncen; c++) {
-          float v = row[c];
-          if (wrow) v *= wrow[c];
-          ps += v;
-          px += v * (float)(sx0 + c);
+                                 : (a.centWeightDim == 4 ? a.centWeight + (long long)s_i[s] * mm + r * m + sx0 : nullptr);
+        float ps = 0.f, px = 0.f;
+        if (wrow) {
+          for (int c2 = 0; c2 < ncen; c2++) {
+            const float v = row[c2] * wrow[c2];
+            ps += v;
+            px += v * (float)(sx0 + c2);
+          }
+        } else {
+          for (int c2 = 0; c2 < ncen; c2++) {
+            const float v = row[c2];
+            ps += v;
+            px += v * (float)(sx0 + c2);
+          }
         }
+        s_rows[2 * t] = ps;
+        s_rows[2 * t + 1] = px;
       }
-      s_part[2 * pr] = ps;
-      s_part[2 * pr + 1] = px;
+      __syncwarp();
+      if (lane < nk) {
+        float sum = 0.f, sxv = 0.f, syv = 0.f;
+        for (int rr = 0; rr < ncen; rr++) {
+          const float ps = s_rows[2 * (lane * ncen + rr)];
+          sum += ps;
+          sxv += s_rows[2 * (lane * ncen + rr) + 1];
+          syv += ps * (float)(sx0 + rr);
+        }
+        float cx = 0.f, cy = 0.f;
+        if (sum > 0.f) {
+          cx = sxv / sum - 0.5f * (float)(m - 1);
+          cy = syv / sum - 0.5f * (float)(m - 1);
+        }
+        calibrate_and_store(a, s_i[lane], s_f[lane], cx, cy);
+      }
     }
-    __syncthreads();
-    for (int s = tid; s < ns; s += blockDim.x) {
-      if (s_flag[s] != 1) continue;
-      float sum = 0.f, sxv = 0.f, syv = 0.f;
-      for (int rr = 0; rr < ncen; rr++) {
-        const float ps = s_part[2 * (s * ncen + rr)];
-        sum += ps;
-        sxv += s_part[2 * (s * ncen + rr) + 1];
-        syv += ps * (float)(sx0 + rr);
-      }
-      float cx = 0.f, cy = 0.f;
-      if (sum > 0.f) {
-        cx = sxv / sum - 0.5f * (float)(m - 1);
-        cy = syv / sum - 0.5f * (float)(m - 1);
-      }
-      calibrate_and_store(a, s0 + s, f, cx, cy);
-    }
+    __syncwarp();  // every lane is done with buffer b before it is refilled
   }
   asm volatile("cp.async.wait_all;" ::: "memory");
+  if (a.zeroUnlit) {
+    // unlit subapertures: centroids 0 (cmod/src/centmodule.c:1964-1981)
+    const long long nu = (long long)a.nunlit * a.nframes;
+    for (long long u = (long long)blockIdx.x * blockDim.x + tid; u < nu; u += (long long)gridDim.x * blockDim.x) {
+      const int f = (int)(u / a.nunlit), i = a.unlit[u - (long long)f * a.nunlit];
+      float* c = a.cents + (long long)f * a.centsFrameStride + 2LL * i;
+      c[0] = 0.f;
+      c[1] = 0.f;
+    }
+  }
 }
 
 }  // namespace
@@ -424,48 +501,46 @@ cudaError_t launch_post(const WfsArgs& a0, int numSMs, cudaStream_t stream, unsi
                       a.fitSize == 0 && a.gaussianFit <= 0 && a.cob == 0;
   const int tabB = pois ? (int)sizeof(PoisTab) : 0;
   const int cwB = ((a.centWeightDim == 2 ? mm : 0) + 3) / 4 * 16;
-  const int perSlot = (kSlotStages * (mm + 3) + 2 * a.ncen) * (int)sizeof(float);
-  if (simple && a.subflag && tabB + cwB + 2 * perSlot <= 160 * 1024) {
-    // slot tiles: kSlotStages stages of TS slots, sized for kSlotCtasPerSM CTAs per SM
-    const int budget = (228 * 1024) / kSlotCtasPerSM - 1024 - 4 * kPostBright * 2 - 64 - tabB - cwB;
-    int ts = budget / perSlot - 1;
-    ts = ts < 1 ? 1 : (ts > kSlotMaxTS ? kSlotMaxTS : ts);
-    // small batches: tiles no larger than it takes to give every resident
-    // CTA one (latency), nor smaller than one pixel per thread
-    const long long slots = (long long)a.nsubaps * a.nframes;
-    const long long fill = (slots + (long long)numSMs * kSlotCtasPerSM - 1) / ((long long)numSMs * kSlotCtasPerSM);
-    const int minTs = (kSlotThreads + mm - 1) / mm;
-    if (fill < ts) ts = (int)std::max<long long>(fill, std::min(minTs, ts));
-    a.TS = ts;
+  const int bufPx = (std::max(512, mm) + 3) / 4 * 4;
+  const int warpB = warp_smem_floats(bufPx, a.ncen) * (int)sizeof(float);
+  const int wsmem = tabB + cwB + (kWarpThreads / 32) * warpB;
+  if (simple && a.ncen >= 1 && wsmem <= 200 * 1024) {
+    const bool rnOn = a.calsource == 0 && a.readNoise != 0.f;
+    auto kern = pois ? (rnOn ? wfs_post_warp_kernel<true, true> : wfs_post_warp_kernel<false, true>)
+                     : (rnOn ? wfs_post_warp_kernel<true, false> : wfs_post_warp_kernel<false, false>);
+    if (a.calsource != 0) a.readNoise = 0.f;
+    int ctas = 0;
+    cudaError_t e = kernel_smem_setup((const void*)kern, wsmem, kWarpThreads, &ctas);
+    if (e != cudaSuccess) return e;
+    if (ctas < 1) return cudaErrorInvalidConfiguration;
+    const long long cap = (long long)numSMs * ctas;
+    const long long warps = cap * (kWarpThreads / 32);
+    // chunk size: as many items as fill the buffer, fewer when that would
+    // leave resident warps without a chunk (small batches: latency)
+    int K = std::max(1, std::min(kWarpMaxK, bufPx / mm));
+    const long long perWarp = (nwork + warps - 1) / warps;
+    if (perWarp < K) K = (int)std::max(1LL, perWarp);
+    const long long nchunks = (nwork + K - 1) / K;
+    const long long needCtas = (nchunks + kWarpThreads / 32 - 1) / (kWarpThreads / 32);
+    const int grid = (int)std::max(1LL, std::min(cap, needCtas));
     if (done) {
-      if (!a.imageOnly) {
+      if (!a.imageOnly && a.unlit && a.nunlit > 0) {
         a.zeroUnlit = 1;
         *done |= kPostDidUnlit;
+      } else if (!a.imageOnly) {
+        *done |= kPostDidUnlit;  // nothing unlit to zero
       }
       if (a.bimgOut) *done |= kPostDidOut;
     } else {
       a.bimgOut = nullptr;
     }
-    const int stageFloats = (ts * mm + 3 * ts + 3) / 4 * 4;
-    const int smem = tabB + cwB + (kSlotStages * stageFloats + 2 * ts * a.ncen) * (int)sizeof(float);
-    const bool rnOn = a.calsource == 0 && a.readNoise != 0.f;
-    auto kern = pois ? (rnOn ? wfs_post_slots_kernel<true, true> : wfs_post_slots_kernel<false, true>)
-                     : (rnOn ? wfs_post_slots_kernel<true, false> : wfs_post_slots_kernel<false, false>);
-    if (a.calsource != 0) a.readNoise = 0.f;
-    int ctas = 0;
-    cudaError_t e = kernel_smem_setup((const void*)kern, smem, kSlotThreads, &ctas);
-    if (e != cudaSuccess) return e;
-    if (ctas < 1) return cudaErrorInvalidConfiguration;
-    const long long ntiles = (long long)((a.nsubaps + ts - 1) / ts) * a.nframes;
-    const long long cap = (long long)numSMs * ctas;
-    const int grid = (int)(ntiles < cap ? ntiles : cap);
     // programmatic launch: CTAs may become resident while the previous
     // kernel of the stream (the image formation) still runs and wait for it
     // in griddepcontrol.wait after loading their tables
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
-    cfg.blockDim = dim3(kSlotThreads);
-    cfg.dynamicSmemBytes = (size_t)smem;
+    cfg.blockDim = dim3(kWarpThreads);
+    cfg.dynamicSmemBytes = (size_t)wsmem;
     cfg.stream = stream;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -473,7 +548,7 @@ cudaError_t launch_post(const WfsArgs& a0, int numSMs, cudaStream_t stream, unsi
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     const PoisTab* tabArg = pois ? tab : nullptr;
-    return cudaLaunchKernelEx(&cfg, kern, a, tabArg);
+    return cudaLaunchKernelEx(&cfg, kern, a, tabArg, K, bufPx);
   }
   const int smem = (a.TS * mm + (a.centWeightDim == 2 ? mm : 0)) * (int)sizeof(float) +
                    (pois ? (int)sizeof(PoisTab) : 0);

@@ -31,7 +31,7 @@ def _job(_lib, c, img_dev, subflag_dev, cents_dev, bimg_dev):
     j = _lib.ShwfsImageJob()
     j.nsubx, j.nimg, j.ncen = c.nsubx, c.m, c.ncen
     j.image_ndim = 2
-    j.image_rows, j.image_cols = img_dev.shape
+    j.image_rows, j.image_cols = img_dev.shape[-2], img_dev.shape[-1]
     j.image = img_dev.data_ptr()
     j.subflag = subflag_dev.data_ptr()
     j.refCents = None
