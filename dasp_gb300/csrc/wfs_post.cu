@@ -181,10 +181,11 @@ constexpr int kWarpMaxK = 16;      // subaperture-frames per chunk
 
 // Per-warp shared memory: two pixel buffers of bufPx floats (the chunk being
 // drawn and the next one, copied in asynchronously), the chunk's item table
-// (subaperture, frame, Poisson flag) for both buffers, the window-row
-// partial sums of the centroids and the bright-pixel queue.
+// for both buffers (per item an int4 {subaperture, noise frame index,
+// Poisson flag, frame} and the 64-bit offset of its image in bimg), the
+// window-row partial sums of the centroids and the bright-pixel queue.
 __host__ __device__ inline int warp_smem_floats(int bufPx, int ncen) {
-  return 2 * bufPx + 2 * 3 * kWarpMaxK + 2 * kWarpMaxK * ncen + 2 * kWarpQ;
+  return 2 * bufPx + 2 * 6 * kWarpMaxK + 2 * kWarpMaxK * ncen + 2 * kWarpQ;
 }
 
 // The common configuration (window CoG or image only; no brightest-pixel
@@ -211,9 +212,11 @@ __global__ void __launch_bounds__(kWarpThreads, 3)
   PoisTab* s_tab = reinterpret_cast<PoisTab*>(smem_post);
   float* s_cw = smem_post + (POIS ? sizeof(PoisTab) / sizeof(float) : 0);
   float* wbase = s_cw + ((cw2d ? mm : 0) + 3) / 4 * 4 + warp * warp_smem_floats(bufPx, ncen);
-  // buffer b: pixels wbase + b * bufPx, item table info0 + b * 3 * kWarpMaxK
-  int* info0 = reinterpret_cast<int*>(wbase + 2 * bufPx);
-  float* s_rows = wbase + 2 * bufPx + 6 * kWarpMaxK;
+  // buffer b: pixels wbase + b * bufPx, items item0 + b * kWarpMaxK, image
+  // offsets off0 + b * kWarpMaxK
+  int4* item0 = reinterpret_cast<int4*>(wbase + 2 * bufPx);
+  long long* off0 = reinterpret_cast<long long*>(item0 + 2 * kWarpMaxK);
+  float* s_rows = wbase + 2 * bufPx + 12 * kWarpMaxK;
   int* q_idx = reinterpret_cast<int*>(s_rows + 2 * kWarpMaxK * ncen);
   float* q_val = reinterpret_cast<float*>(q_idx + kWarpQ);
   if constexpr (POIS) {
@@ -259,7 +262,8 @@ __global__ void __launch_bounds__(kWarpThreads, 3)
   const long long sf = strideItems / a.nlit;
   const int sl = (int)(strideItems - sf * a.nlit);
   auto issue = [&](long long c, int b, long long f0, int l0) {
-    int* inf = info0 + b * 3 * kWarpMaxK;
+    int4* itb = item0 + b * kWarpMaxK;
+    long long* ofb = off0 + b * kWarpMaxK;
     if (c < nchunks) {
       const long long w0 = c * K;
       const int nk = (int)min((long long)K, items - w0);
@@ -270,10 +274,9 @@ __global__ void __launch_bounds__(kWarpThreads, 3)
           f++;
         }
         const int i = a.lit[li];
-        inf[lane] = i;
-        inf[kWarpMaxK + lane] = f;
-        inf[2 * kWarpMaxK + lane] =
-            POIS ? (a.totsig[i] > 0.f || a.sky * a.frac[i] > 0.f || a.skyArr != nullptr) : 0;
+        const int pf = POIS ? (a.totsig[i] > 0.f || a.sky * a.frac[i] > 0.f || a.skyArr != nullptr) : 0;
+        itb[lane] = make_int4(i, (int)(uint32_t)(fbase + (unsigned long long)f), pf, f);
+        ofb[lane] = (long long)f * a.bimgFrameStride + (long long)i * mm;
       }
       __syncwarp();
       float* dst = wbase + b * bufPx;
@@ -282,7 +285,7 @@ __global__ void __launch_bounds__(kWarpThreads, 3)
         const float inv_q4 = 1.0f / (float)q4;
         for (int q = lane; q < nq; q += 32) {
           const int s = div_small(q, q4, inv_q4), r = q - s * q4;
-          const float* src = a.bimg + (long long)inf[kWarpMaxK + s] * a.bimgFrameStride + (long long)inf[s] * mm + 4 * r;
+          const float* src = a.bimg + ofb[s] + 4 * r;
           asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst + 4 * q)),
                        "l"(src)
                        : "memory");
@@ -290,7 +293,7 @@ __global__ void __launch_bounds__(kWarpThreads, 3)
       } else {
         for (int g = lane; g < nk * mm; g += 32) {
           const int s = div_small(g, mm, inv_mm), pix = g - s * mm;
-          const float* src = a.bimg + (long long)inf[kWarpMaxK + s] * a.bimgFrameStride + (long long)inf[s] * mm + pix;
+          const float* src = a.bimg + ofb[s] + pix;
           asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst + g)),
                        "l"(src)
                        : "memory");
@@ -315,9 +318,8 @@ __global__ void __launch_bounds__(kWarpThreads, 3)
     asm volatile("cp.async.wait_group 1;" ::: "memory");
     __syncwarp();
     float* img = wbase + b * bufPx;
-    const int* s_i = info0 + b * 3 * kWarpMaxK;
-    const int* s_f = s_i + kWarpMaxK;
-    const int* s_pf = s_i + 2 * kWarpMaxK;
+    const int4* items = item0 + b * kWarpMaxK;
+    const long long* offs = off0 + b * kWarpMaxK;
     // noise and threshold of a pixel drawn from its stream (seed, frame,
     // subaperture, pixel): the read-noise normal takes the block's first two
     // uniforms, the tabulated Poisson draw the next two (the first two
@@ -332,10 +334,10 @@ __global__ void __launch_bounds__(kWarpThreads, 3)
       float g = 0.f;
       if constexpr (RN) g = normal_from_u32(r.x, r.y);
       if constexpr (POIS) {
-        if (pf) {
-          const uint32_t w3 = RN ? r.z : r.x, w4 = RN ? r.w : r.y;
-          v = v > 0.f ? poisson_tab(*s_tab, w3, u32_to_uniform(w4), v) : 0.f;
-        }
+        // lambda <= 0 (or NaN) draws 0, as the table's L = 0 column gives
+        const uint32_t w3 = RN ? r.z : r.x, w4 = RN ? r.w : r.y;
+        const float vp = poisson_tab(*s_tab, w3, u32_to_uniform(w4), fmaxf(v, 0.f));
+        v = pf ? vp : v;
       }
       if constexpr (RN)
         v += rn * g + a.readBg;
@@ -363,31 +365,22 @@ __global__ void __launch_bounds__(kWarpThreads, 3)
     };
     int nq = 0;  // bright pixels queued (warp-uniform)
     const int npx = nk * mm;
-    // this lane's pixel g = g0 + lane is pixel pix of item s; the item's
-    // subaperture, frame, Poisson flag and output offset are cached while
-    // s stays the same
+    // this lane's pixel g = g0 + lane is pixel pix of item s
     int s = 0, pix = lane;
     while (pix >= mm) {
       pix -= mm;
       s++;
     }
-    int cs = -1, ipf = 0;
-    uint32_t isub = 0, ifrm = 0;
-    long long obase = 0;
-    for (int g0 = 0; g0 < npx; g0 += 32) {
+    // one round of 32 pixels; TAIL: the last, partial round
+    auto round = [&](int g0, auto TAIL) {
       const int g = g0 + lane;
-      const bool in = g < npx;
-      if (in && s != cs) {
-        cs = s;
-        isub = (uint32_t)s_i[s];
-        ifrm = (uint32_t)(fbase + (unsigned long long)s_f[s]);
-        ipf = s_pf[s];
-        obase = (long long)s_f[s] * a.bimgFrameStride + (long long)s_i[s] * mm;
-      }
-      float v = in ? img[g] : 0.f;
+      const bool in = !decltype(TAIL)::value || g < npx;
+      const int4 it = items[in ? s : 0];
+      const long long ob = offs[in ? s : 0];
+      float v = img[in ? g : 0];
       bool queued = false, bright = false;
       if constexpr (POIS) {
-        bright = noise && in && ipf && v >= kModalMaxLam;
+        bright = noise && in && it.z && v >= kModalMaxLam;
         const unsigned bm = __ballot_sync(0xffffffffu, bright);
         if (bm) {
           if (bright) {
@@ -402,23 +395,31 @@ __global__ void __launch_bounds__(kWarpThreads, 3)
         }
       }
       if (in && !queued) {
-        if (noise) v = bright ? draw_bright(v, isub, ifrm, pix) : draw_fast(v, isub, ifrm, pix, ipf);
-        store(obase + pix, g, v);
+        if (noise) {
+          if (POIS && bright)
+            v = draw_bright(v, (uint32_t)it.x, (uint32_t)it.y, pix);
+          else
+            v = draw_fast(v, (uint32_t)it.x, (uint32_t)it.y, pix, it.z);
+        }
+        store(ob + pix, g, v);
       }
       pix += 32;
       while (pix >= mm) {
         pix -= mm;
         s++;
       }
-    }
+    };
+    const int nfull = npx & ~31;
+    for (int g0 = 0; g0 < nfull; g0 += 32) round(g0, std::false_type{});
+    if (nfull < npx) round(nfull, std::true_type{});
     if constexpr (POIS) {
       if (noise && nq) {
         __syncwarp();
         for (int q = lane; q < min(nq, kWarpQ); q += 32) {
           const int g = q_idx[q];
           const int sq = div_small(g, mm, inv_mm), pq = g - sq * mm;
-          const long long off = (long long)s_f[sq] * a.bimgFrameStride + (long long)s_i[sq] * mm + pq;
-          store(off, g, draw_bright(q_val[q], (uint32_t)s_i[sq], (uint32_t)(fbase + (unsigned long long)s_f[sq]), pq));
+          const int4 it = items[sq];
+          store(offs[sq] + pq, g, draw_bright(q_val[q], (uint32_t)it.x, (uint32_t)it.y, pq));
         }
       }
     }
@@ -431,7 +432,7 @@ __global__ void __launch_bounds__(kWarpThreads, 3)
         const int r = sx0 + rr;
         const float* row = img + s * mm + r * m + sx0;
         const float* wrow = cw2d ? s_cw + r * m + sx0
-                                 : (a.centWeightDim == 4 ? a.centWeight + (long long)s_i[s] * mm + r * m + sx0 : nullptr);
+                                 : (a.centWeightDim == 4 ? a.centWeight + (long long)items[s].x * mm + r * m + sx0 : nullptr);
         float ps = 0.f, px = 0.f;
         if (wrow) {
           for (int c2 = 0; c2 < ncen; c2++) {
@@ -463,7 +464,7 @@ __global__ void __launch_bounds__(kWarpThreads, 3)
           cx = sxv / sum - 0.5f * (float)(m - 1);
           cy = syv / sum - 0.5f * (float)(m - 1);
         }
-        calibrate_and_store(a, s_i[lane], s_f[lane], cx, cy);
+        calibrate_and_store(a, items[lane].x, items[lane].w, cx, cy);
       }
     }
     __syncwarp();  // every lane is done with buffer b before it is refilled
