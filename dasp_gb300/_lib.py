@@ -45,7 +45,8 @@ NOALLOC_MAX_SUBAPS = 65536
 
 
 class ShwfsServerConfig(ctypes.Structure):
-    _fields_ = [("hbm_budget_bytes", ctypes.c_int64), ("max_inflight", ctypes.c_int), ("device", ctypes.c_int)]
+    _fields_ = [("hbm_budget_bytes", ctypes.c_int64), ("max_inflight", ctypes.c_int), ("device", ctypes.c_int),
+                ("integration_mode", ctypes.c_int)]
 
 
 class ShwfsCompletion(ctypes.Structure):

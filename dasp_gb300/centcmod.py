@@ -52,9 +52,11 @@ FORMS = {"fp32": 0, "bf16": 1, "bf16x3": 2, "fp16": 3, "tf32": 4}
 HOSTIO = 103  # extension: zero-copy host I/O switches (HOSTIO_* below)
 HOSTIO_OUTPUTS = 1  # kernels write cents / final images into the pinned host arrays
 HOSTIO_PHASE = 2  # image-formation kernels read the pinned host phase directly
+INTEGMODE = 104  # extension: integration mode (INTEGMODES below)
+INTEGMODES = {"compat": 0, "physical": 1}
 
 _INT_CODES = {CALSOURCE, ADDPOISSON, NCEN, NTHREADS, OPTICALBINNING, CORRELATIONCENTROIDING, INTEGSTEPS,
-              NOISEMODE, TILESUBAPS, FORM}
+              NOISEMODE, TILESUBAPS, FORM, INTEGMODE}
 _INT_ARRAY_CODES = {USEBRIGHTEST}
 
 
@@ -301,6 +303,17 @@ class centcmod:
         (the reference's per-thread PCG32/MT19937 streams)."""
         code = {"counter": NOISE_COUNTER, "reference": NOISE_REFERENCE}[mode]
         self.update(NOISEMODE, code)
+
+    def set_integration_mode(self, mode):
+        """How sub-exposures (nintegrations > 1) form the image.  "compat"
+        (default) is the reference's: it zeroes its image accumulator on
+        every sub-exposure (cmod/src/centmodule.c:478), so only the readout
+        frame's phase reaches the image.  "physical": every exposed frame
+        (start, middle and readout frames; frame-transfer frames are not
+        exposed) forms its normalised, sky-added image on the device and the
+        readout frame's image is their mean, to which noise, threshold and
+        centroiding are applied once.  Starts a new exposure."""
+        self.update(INTEGMODE, INTEGMODES[mode] if isinstance(mode, str) else int(mode))
 
     def set_host_io(self, outputs=True, phase=True):
         """Zero-copy transfers of ``run`` with host (numpy) arrays: with

@@ -160,6 +160,11 @@ struct shwfs_handle {
   DevBuf<unsigned char> d_poisFlag;
   DevBuf<RefRng> d_rng;
   DevBuf<float> d_inj;  // caller-drawn noise of shwfs_run_prenoise (shot, then read)
+  // physical integration (SHWFS_INTEG_PHYSICAL): this sub-exposure's
+  // pre-noise images and the exposure's running sum (nsubaps*nimg^2 each)
+  int integMode = SHWFS_INTEG_COMPAT;
+  int accumCount = 0;
+  DevBuf<float> d_sub, d_accum;
   const PlainEntry* entry = nullptr;
   int TS = 1, smem = 0, ctasPerSM = 1, numSMs = 1;
   int tileOverride = 0;  // SHWFS_TILESUBAPS; 0 = default
@@ -925,6 +930,74 @@ int readout_frame(const shwfs_handle* h) {
   return 1;
 }
 
+// caller-supplied pre-noise images (and optionally caller-drawn noise) of
+// shwfs_run_prenoise
+struct PrenoiseIn {
+  const shwfs_array* images;
+  const shwfs_array* shot;
+  const shwfs_array* readn;
+};
+
+// the reference's state of this frame (cmod/src/centmodule.c:1774-1788):
+// 0 start of an exposure, 1 middle, 2 readout, -1 start and readout,
+// 3 frame transfer (no exposure)
+int integ_state(const shwfs_handle* h) {
+  if (h->curInteg == 0) return h->nintegrations + h->nlatency == 1 ? -1 : 0;
+  if (h->curInteg + 1 < h->nintegrations) return 1;
+  if (h->curInteg + 1 < h->nintegrations + h->nlatency) return 3;
+  return 2;
+}
+
+shwfs_status enqueue_prenoise(shwfs_handle* h, const PrenoiseIn& in, cudaStream_t st);
+
+// physical integration, one exposed frame (state 0, 1, 2 or -1) of device
+// phase phs: this sub-exposure's normalised, sky-added images into d_sub,
+// added to the exposure's sum; at the readout the sum becomes the mean and
+// goes through noise, threshold and the post stages (as shwfs_run_prenoise)
+shwfs_status enqueue_physical(shwfs_handle* h, const float* phs, int state, cudaStream_t st) {
+  if (h->interp || h->phaseAmp || h->opticalBinning == 1)
+    return fail(SHWFS_ERR_UNSUPPORTED,
+                "physical integration with phase interpolation, phase+amplitude or optical binning");
+  const size_t n = (size_t)h->nsubaps * h->nimg * h->nimg;
+  for (DevBuf<float>* b : {&h->d_sub, &h->d_accum}) {
+    if (b->n < n) {
+      CK(b->alloc(n));
+      CK(cudaMemsetAsync(b->p, 0, n * sizeof(float), st));  // unlit subapertures stay 0
+    }
+  }
+  const int nlit = (int)h->lit.size();
+  if (nlit) {
+    if (gemm_active(h)) {
+      WfsArgs a = make_args(h, phs, h->d_cents.p, h->d_sub.p, 1, 0, kForm);
+      GemmGeom g = h->gemm;
+      g.w2 = h->d_w2.p;
+      g.kc2 = h->d_kc2.p;
+      g.pupT = h->d_pupT.p;
+      CK(launch_gemm(a, g, g.fmt == kFmtFP16 ? h->d_iscale.p : nullptr, h->numSMs, h->d_status.p, st));
+    } else {
+      const long long ntiles = ((long long)nlit + h->TS - 1) / h->TS;
+      const int grid =
+          (int)std::max<long long>(1, std::min<long long>(ntiles, (long long)h->numSMs * h->ctasPerSM));
+      WfsArgs a = make_args(h, phs, h->d_cents.p, h->d_sub.p, 1, 0, kForm | kStorePreNoise);
+      CK(h->entry->launch(a, grid, h->smem, st));
+    }
+  }
+  const bool first = state == 0 || state == -1, ro = state == 2 || state == -1;
+  h->accumCount = first ? 1 : h->accumCount + 1;
+  CK(launch_accumulate(h->d_accum.p, h->d_sub.p, (long long)n, first ? 1 : 0, ro ? 1.0f / (float)h->accumCount : 1.0f,
+                       st));
+  if (!ro) return SHWFS_OK;
+  shwfs_array acc{};
+  acc.data = h->d_accum.p;
+  acc.ndim = 1;
+  acc.shape[0] = (int64_t)n;
+  acc.dtype = SHWFS_F32;
+  acc.on_device = 1;
+  const shwfs_array none{};
+  PrenoiseIn in{&acc, &none, &none};
+  return enqueue_prenoise(h, in, st);
+}
+
 // publish exactly what the reference writes on a readout frame: every
 // centroid unless imageOnly; every image with imageOnly, else the lit ones
 shwfs_status publish_outputs(shwfs_handle* h, cudaStream_t st, bool* sync) {
@@ -1019,13 +1092,6 @@ shwfs_status enqueue_slope(shwfs_handle* h, cudaStream_t st) {
   return enqueue_corr(h, cents, bimg, 1, st);
 }
 
-// caller-supplied pre-noise images (and optionally caller-drawn noise) of
-// shwfs_run_prenoise
-struct PrenoiseIn {
-  const shwfs_array* images;
-  const shwfs_array* shot;
-  const shwfs_array* readn;
-};
 
 // one readout from pre-noise images: the noise, threshold and post stages of
 // centroidsFromPhase (cmod/src/centmodule.c:1879-1981) on the caller's images
@@ -1117,7 +1183,24 @@ shwfs_status run_impl(shwfs_handle* h, cudaStream_t st, bool sync, float* elapse
     return fail(SHWFS_ERR_STATE, "no phase array is bound (image-input handle)");
   const bool readout = slope || pre || readout_frame(h);
   h->centsDirect = h->bimgDirect = h->inDirect = false;
-  if (readout) {
+  const int istate = integ_state(h);
+  const bool physical = h->integMode == SHWFS_INTEG_PHYSICAL && !slope && !pre;
+  if (physical && istate != 3) {
+    // physical integration: every exposed frame forms its images on the
+    // device; the readout frame also draws the noise and centroids
+    const float* phs = (const float*)h->phs.data;
+    if (!h->phs.on_device) {
+      CK(cudaMemcpyAsync(h->d_phs.p, h->phs.data, (size_t)numel(h->phs) * sizeof(float), cudaMemcpyHostToDevice,
+                         st));
+      phs = h->d_phs.p;
+    }
+    shwfs_status s = enqueue_physical(h, phs, istate, st);
+    if (s) return s;
+    if (readout) {
+      if ((s = publish_outputs(h, st, &sync))) return s;
+      h->framesRead++;
+    }
+  } else if (readout && !physical) {
     shwfs_status s;
     if (slope) {
       s = enqueue_slope(h, st);
@@ -1158,7 +1241,7 @@ shwfs_status run_impl(shwfs_handle* h, cudaStream_t st, bool sync, float* elapse
   // the tensor-core forms' noise/centroid kernel writes it to the pinned
   // host word, the reference-stream path copies it
   const bool checkStatus =
-      sync && readout && (h->noiseMode == SHWFS_NOISE_REFERENCE || (gemm_active(h) && !slope && !pre));
+      sync && readout && (h->noiseMode == SHWFS_NOISE_REFERENCE || (gemm_active(h) && !slope && !pre && !physical));
   if (checkStatus && h->noiseMode == SHWFS_NOISE_REFERENCE)
     CK(cudaMemcpyAsync(h->h_status, h->d_status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   if (sync) {
@@ -1715,6 +1798,16 @@ shwfs_status shwfs_update(shwfs_handle* h, int code, const shwfs_value* v) {
         return fail(SHWFS_ERR_INVALID, "unknown host I/O switches %lld", (long long)v->ival);
       h->hostIO = (int)v->ival;
       break;
+    case SHWFS_INTEGMODE:
+      if ((s = need(SHWFS_VAL_INT, "int"))) return s;
+      if (v->ival != SHWFS_INTEG_COMPAT && v->ival != SHWFS_INTEG_PHYSICAL)
+        return fail(SHWFS_ERR_INVALID, "unknown integration mode %lld", (long long)v->ival);
+      if (v->ival == SHWFS_INTEG_PHYSICAL && (h->interp || h->phaseAmp || h->opticalBinning == 1))
+        return fail(SHWFS_ERR_UNSUPPORTED,
+                    "physical integration with phase interpolation, phase+amplitude or optical binning");
+      h->integMode = (int)v->ival;
+      h->curInteg = 0;  // a new exposure starts
+      break;
     case SHWFS_NOISEMODE:
       if ((s = need(SHWFS_VAL_INT, "int"))) return s;
       if (v->ival != SHWFS_NOISE_COUNTER && v->ival != SHWFS_NOISE_REFERENCE)
@@ -2063,7 +2156,15 @@ namespace shwfs {
 
 shwfs_status engine_frame(shwfs_handle* h, const float* phs_dev, cudaStream_t st, int* readout) {
   *readout = readout_frame(h);
-  if (*readout) {
+  if (h->integMode == SHWFS_INTEG_PHYSICAL) {
+    const int state = integ_state(h);
+    if (state != 3) {
+      if (!h->cents.on_device || !h->bimg.on_device)
+        return fail(SHWFS_ERR_STATE, "engine_frame needs device-resident cents and bimg");
+      if (shwfs_status s = enqueue_physical(h, phs_dev, state, st)) return s;
+    }
+    if (*readout) h->framesRead++;
+  } else if (*readout) {
     if (!h->cents.on_device || !h->bimg.on_device)
       return fail(SHWFS_ERR_STATE, "engine_frame needs device-resident cents and bimg");
     if (shwfs_status s = enqueue_readout(h, phs_dev, (float*)h->cents.data, (float*)h->bimg.data, 1, 0, st))
@@ -2083,6 +2184,7 @@ int64_t engine_device_bytes(const shwfs_handle* h) {
   add(h->d_binT); add(h->d_binN); add(h->d_psf); add(h->d_lit); add(h->d_unlit); add(h->d_binII);
   add(h->d_binLo); add(h->d_binHi); add(h->d_ubArr); add(h->d_calBounds); add(h->d_subflag);
   add(h->d_subapStart); add(h->d_status); add(h->d_psfSpec); add(h->d_phs); add(h->d_cents); add(h->d_bimg);
+  add(h->d_sub); add(h->d_accum); add(h->d_inj);
   add(h->d_image); add(h->d_subapLoc); add(h->d_poisFlag); add(h->d_rng); add(h->d_w2); add(h->d_kc2);
   add(h->d_iscale); add(h->d_pupT); add(h->d_interp); add(h->d_frameCtr);
   return b;

@@ -72,7 +72,7 @@ int64_t numel(const shwfs_array& a) {
 }
 
 // device bytes a system will hold, from its init (before the engine exists)
-int64_t estimate_bytes(const shwfs_init& in, int form) {
+int64_t estimate_bytes(const shwfs_init& in, int form, int integMode) {
   const int64_t ns = in.nsubaps, p = in.phasesize, m = in.nimg;
   const int64_t phs = numel(in.phs), P = in.spotpsf.data ? in.spotpsf.shape[in.spotpsf.ndim - 1] : 0;
   const int64_t npsf = in.spotpsf.data ? (in.spotpsf.ndim == 4 ? ns : 1) : 0;
@@ -85,6 +85,7 @@ int64_t estimate_bytes(const shwfs_init& in, int form) {
   if (in.skybrightnessArr.data) b += ns * m * m * 4;
   if (in.centWeight.data) b += numel(in.centWeight) * 4;
   if (form != SHWFS_FORM_FP32) b += 4 << 20;     // GEMM-DFT constants
+  if (integMode == SHWFS_INTEG_PHYSICAL) b += 2 * ns * m * m * 4;  // sub-exposure and exposure sum
   return b;
 }
 
@@ -157,6 +158,15 @@ struct shwfs_server {
       v.kind = SHWFS_VAL_INT;
       v.ival = s.form;
       if (shwfs_update(s.h, SHWFS_FORM, &v) != SHWFS_OK) {
+        s.error = shwfs_last_error();
+        return false;
+      }
+    }
+    if (cfg.integration_mode != SHWFS_INTEG_COMPAT) {
+      shwfs_value v{};
+      v.kind = SHWFS_VAL_INT;
+      v.ival = cfg.integration_mode;
+      if (shwfs_update(s.h, SHWFS_INTEGMODE, &v) != SHWFS_OK) {
         s.error = shwfs_last_error();
         return false;
       }
@@ -322,6 +332,8 @@ extern "C" {
 shwfs_status shwfs_server_create(const shwfs_server_config* cfg, shwfs_server** out) {
   if (!cfg || !out || cfg->hbm_budget_bytes <= 0 || cfg->max_inflight < 1)
     return shwfs::engine_fail(SHWFS_ERR_INVALID, "server needs a positive HBM budget and max_inflight >= 1");
+  if (cfg->integration_mode != SHWFS_INTEG_COMPAT && cfg->integration_mode != SHWFS_INTEG_PHYSICAL)
+    return shwfs::engine_fail(SHWFS_ERR_INVALID, "unknown integration mode");
   shwfs_server* s = new shwfs_server;
   s->cfg = *cfg;
   s->t0 = Clock::now();
@@ -338,7 +350,7 @@ shwfs_status shwfs_server_add_system(shwfs_server* s, const shwfs_init* init, in
   auto sys = std::make_unique<System>();
   sys->init = *init;
   sys->form = form;
-  sys->estimate = estimate_bytes(*init, form);
+  sys->estimate = estimate_bytes(*init, form, s->cfg.integration_mode);
   std::lock_guard<std::mutex> lk(s->mu);
   if (sys->estimate > s->cfg.hbm_budget_bytes)
     return shwfs::engine_fail(SHWFS_ERR_NOMEM, "system needs more device memory than the whole HBM budget");

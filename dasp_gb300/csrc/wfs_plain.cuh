@@ -794,5 +794,8 @@ cudaError_t launch_image(const WfsArgs& a, const float* img, int dims, int npxlx
                          cudaStream_t stream);
 // copy the listed subapertures' images src -> dst (dst: mapped host memory)
 cudaError_t launch_publish(const float* src, float* dst, const int* list, int n, int mm, cudaStream_t stream);
+// physical integration: acc = (first ? sub : acc + sub), then acc *= scale
+// (the exposure's mean at its readout frame), over n values
+cudaError_t launch_accumulate(float* acc, const float* sub, long long n, int first, float scale, cudaStream_t stream);
 
 }  // namespace shwfs

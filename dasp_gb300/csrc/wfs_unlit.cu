@@ -1,4 +1,6 @@
 // Unlit-subaperture kernel of the WFS step.
+#include <algorithm>
+
 #include "wfs_plain.cuh"
 
 namespace shwfs {
@@ -100,6 +102,22 @@ cudaError_t launch_unlit(const WfsArgs& a, const int* unlit, int nunlit, cudaStr
   if (total == 0) return cudaSuccess;
   const int blocks = (int)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
   wfs_unlit_kernel<<<blocks, 256, 0, stream>>>(a, unlit, nunlit);
+  return cudaGetLastError();
+}
+
+__global__ void accumulate_kernel(float* __restrict__ acc, const float* __restrict__ sub, long long n, int first,
+                                  float scale) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    float v = first ? sub[k] : acc[k] + sub[k];
+    if (scale != 1.0f) v *= scale;
+    acc[k] = v;
+  }
+}
+
+cudaError_t launch_accumulate(float* acc, const float* sub, long long n, int first, float scale, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  const long long blocks = std::min<long long>((n + 255) / 256, 4096);
+  accumulate_kernel<<<(unsigned)blocks, 256, 0, stream>>>(acc, sub, n, first, scale);
   return cudaGetLastError();
 }
 

@@ -34,8 +34,12 @@ class _SystemSpec(centcmod):
 
 
 class WfsServer:
-    def __init__(self, hbm_budget_bytes: int, max_inflight: int = 32, device: int = 0):
-        cfg = ShwfsServerConfig(int(hbm_budget_bytes), int(max_inflight), int(device))
+    def __init__(self, hbm_budget_bytes: int, max_inflight: int = 32, device: int = 0, integration: str = "compat"):
+        """integration: "compat" (the reference's: only the readout frame's
+        phase reaches the image) or "physical" (each system's sub-exposures
+        averaged on the device; see centcmod.set_integration_mode)."""
+        cfg = ShwfsServerConfig(int(hbm_budget_bytes), int(max_inflight), int(device),
+                                {"compat": 0, "physical": 1}[integration])
         s = ctypes.c_void_p()
         check(_lib.lib().shwfs_server_create(ctypes.byref(cfg), ctypes.byref(s)), "server_create")
         self._s = s

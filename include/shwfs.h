@@ -72,7 +72,25 @@ enum {
   SHWFS_FORM = 102,
   /* extension: zero-copy host I/O of shwfs_run/shwfs_run_async, ival = an
    * OR of SHWFS_HOSTIO_* (default: both) */
-  SHWFS_HOSTIO = 103
+  SHWFS_HOSTIO = 103,
+  /* extension: how sub-exposures (nintegrations > 1) form the image, ival =
+   * SHWFS_INTEG_COMPAT (default) or SHWFS_INTEG_PHYSICAL */
+  SHWFS_INTEGMODE = 104
+};
+
+/* integration modes (SHWFS_INTEGMODE) */
+enum {
+  /* the reference's behaviour: the image accumulator is zeroed on every
+   * sub-exposure (cmod/src/centmodule.c:478), so only the readout frame's
+   * phase reaches the image */
+  SHWFS_INTEG_COMPAT = 0,
+  /* every exposed sub-exposure (the reference's start, middle and readout
+   * frames; frame-transfer frames are not exposed) forms its normalised,
+   * sky-added image on the device; the readout frame's image is their mean,
+   * to which shot noise, read noise, threshold and centroiding are applied
+   * once.  The total signal per readout stays sig.  Not available with
+   * phase interpolation, phase+amplitude input or optical binning. */
+  SHWFS_INTEG_PHYSICAL = 1
 };
 
 /* zero-copy host I/O switches (SHWFS_HOSTIO).  They apply to host arrays
@@ -434,6 +452,7 @@ typedef struct shwfs_server_config {
   int64_t hbm_budget_bytes; /* device memory the admitted systems may hold */
   int max_inflight;         /* frames on the device at once (all systems) */
   int device;               /* CUDA device ordinal */
+  int integration_mode;     /* SHWFS_INTEG_* for every system (0: the reference's) */
 } shwfs_server_config;
 typedef struct shwfs_completion {
   uint64_t request;  /* id returned by shwfs_server_submit */

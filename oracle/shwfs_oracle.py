@@ -466,7 +466,10 @@ class CentOracle:
         self.mt = [MT19937(base + i) for i in range(self.nthreads)]
 
     def update(self, code, val):
-        if code == CALSOURCE:
+        if code == 104:  # the engine's integration-mode extension
+            self.integMode = int(val)
+            self.curInteg = 0
+        elif code == CALSOURCE:
             self.calsource = int(val)
         elif code == SIG:
             self.set_sig(val)
@@ -858,6 +861,25 @@ class CentOracle:
     def run(self, phs, cents, bimg, amp=None):
         """One frame: py_run -> centroidsFromPhase for every thread partition."""
         add = self.additive()
+        if getattr(self, "integMode", 0) == 1:
+            # physical integration (the engine's SHWFS_INTEG_PHYSICAL): every
+            # exposed frame's normalised, sky-added images are summed in
+            # float; the readout frame's image is the sum times 1/count
+            if add is not None:
+                lit = np.nonzero(self.subflag == 1)[0]
+                img, totsig, skyv = self.pre_noise_images(np.asarray(phs), lit, amp)
+                img = img.astype(np.float32)
+                first = add in (0, -1)
+                self._acc = img.copy() if first else (self._acc + img).astype(np.float32)
+                self._accn = 1 if first else self._accn + 1
+                if add in (2, -1):
+                    mean = (self._acc * np.float32(np.float32(1.0) / np.float32(self._accn))).astype(np.float32)
+                    self._readout(None, cents.reshape(-1), bimg.reshape(self.nsubaps, self.m, self.m), None,
+                                  pre=(mean.astype(self.dt), totsig, skyv))
+            self.curInteg += 1
+            if self.curInteg >= self.nintegrations + self.nlatency:
+                self.curInteg = 0
+            return
         if add is not None and add in (2, -1):
             phs = np.asarray(phs)
             W = self.nsubx * self.p
