@@ -39,7 +39,8 @@ EXPORTS = ("shwfs_initialise", "shwfs_run", "shwfs_run_slope", "shwfs_update", "
            "shwfs_server_remove_system", "shwfs_server_submit", "shwfs_server_poll", "shwfs_server_get_stats",
            "shwfs_server_clock", "shwfs_server_destroy", "shwfs_selftest_bounded_wait",
            "shwfs_screen_create", "shwfs_screen_add", "shwfs_screen_window", "shwfs_screen_read",
-           "shwfs_screen_free", "shwfs_mvm_update", "shwfs_test_correlation", "shwfs_run_prenoise")
+           "shwfs_screen_free", "shwfs_mvm_update", "shwfs_test_correlation", "shwfs_run_prenoise",
+           "shwfs_screens_pupil_phase")
 
 NOALLOC_MAX_SUBAPS = 65536
 
@@ -162,6 +163,9 @@ def lib() -> ctypes.CDLL:
         L.shwfs_screen_window.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp,
                                           ctypes.c_int64, vp]
         L.shwfs_screen_read.argtypes = [vp, vp]
+        L.shwfs_screens_pupil_phase.argtypes = [P(vp), ctypes.c_int, P(ctypes.c_int), P(ctypes.c_int),
+                                                P(ctypes.c_float), P(ctypes.c_float), ctypes.c_int, vp,
+                                                ctypes.c_double, ctypes.c_int, ctypes.c_float, vp, vp]
         L.shwfs_screen_free.argtypes = [vp]
         L.shwfs_mvm_update.argtypes = [ctypes.c_int, ctypes.c_int, vp, vp, vp, ctypes.c_float, vp, ctypes.c_float, vp,
                                        vp]

@@ -128,7 +128,7 @@ class DeviceScreen:
         coeff = (self.L0 / r0) ** (5. / 6)
         if noise is not None:
             noise = np.ascontiguousarray(noise, np.float64)
-            if noise.size != n * (self.ny if axis == 0 else self.nx):
+            if noise.size != n * self._check_noise_axis(axis):
                 raise ValueError("noise must hold n * (screen height or width) values")
         self._lib.check(self._lib.lib().shwfs_screen_add(self._s, axis, int(n), coeff, float(step),
                                                          None if noise is None else noise.ctypes.data, None),
@@ -140,6 +140,17 @@ class DeviceScreen:
     def add_rows(self, n, r0, step=0.0, noise=None):
         self._add(1, n, r0, step, noise)
 
+    def add_columns_start(self, n, r0, step=0.0, noise=None):
+        """n new columns at the start (the wind blowing the other way;
+        addNewColumnOnStart, science/infScrn.py:793-823): the last column is
+        dropped for each."""
+        self._add(2, n, r0, step, noise)
+
+    def add_rows_start(self, n, r0, step=0.0, noise=None):
+        """n new rows at the start (addNewRowOnStart, science/infScrn.py:
+        857-887)."""
+        self._add(3, n, r0, step, noise)
+
     def window(self, y0, x0, out, stream=None):
         """The out.shape[-2:] window at (y0, x0) into the CUDA tensor out."""
         h, w = out.shape[-2], out.shape[-1]
@@ -148,6 +159,9 @@ class DeviceScreen:
         s = getattr(stream, "cuda_stream", stream)
         self._lib.check(self._lib.lib().shwfs_screen_window(self._s, int(y0), int(x0), h, w, out.data_ptr(), w, s),
                         "screen_window")
+
+    def _check_noise_axis(self, axis):
+        return self.ny if axis in (0, 2) else self.nx
 
     def numpy(self):
         out = np.empty((self.ny, self.nx), np.float32)
@@ -164,3 +178,33 @@ class DeviceScreen:
             self.free()
         except Exception:
             pass
+
+
+def pupil_phase(layers, pupil, out, pupil_area=None, wavelength=500.0, remove_piston=True, stream=None):
+    """Pupil phase of a source at infinity from several device screens
+    (util/atmos.py:678-833, createPupilPhs for an NGS): ``layers`` is a list
+    of ``(screen, y0, x0, yshift, xshift)`` -- the (npup+1)-square window of
+    the screen at logical (y0, x0) and its fractional row / column shifts in
+    [0, 1] (linearshift, cmod/src/interpmodule.c:1234-1300) -- added in the
+    order given (the reference sorts by height); the piston over ``pupil``
+    is removed, the result multiplied by ``pupil`` and by 500/wavelength.
+    ``pupil`` and ``out`` are npup x npup float32 CUDA tensors."""
+    from . import _lib
+    n = len(layers)
+    npup = int(out.shape[-1])
+    for t in (pupil, out):
+        if not (t.is_cuda and t.is_contiguous() and str(t.dtype) == "torch.float32" and tuple(t.shape) == (npup, npup)):
+            raise ValueError("pupil and out must be npup x npup contiguous float32 CUDA tensors")
+    if pupil_area is None:
+        pupil_area = float(pupil.double().sum().item())
+    arr_s = (ctypes.c_void_p * n)(*[ly[0]._s.value for ly in layers])
+    y0 = (ctypes.c_int * n)(*[int(ly[1]) for ly in layers])
+    x0 = (ctypes.c_int * n)(*[int(ly[2]) for ly in layers])
+    ys = (ctypes.c_float * n)(*[float(ly[3]) for ly in layers])
+    xs = (ctypes.c_float * n)(*[float(ly[4]) for ly in layers])
+    s = getattr(stream, "cuda_stream", stream)
+    _lib.check(_lib.lib().shwfs_screens_pupil_phase(arr_s, n, y0, x0, ys, xs, npup, pupil.data_ptr(),
+                                                    float(pupil_area), 1 if remove_piston else 0,
+                                                    float(500.0 / wavelength), out.data_ptr(), s),
+               "screens_pupil_phase")
+    return out

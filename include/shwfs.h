@@ -350,7 +350,10 @@ shwfs_status shwfs_sample_noise(int kind, const float* lam, int64_t n, uint64_t 
  * each A Z + coeff_turb B noise (+ step on the first one), Z the last two
  * columns (rows) stacked oldest first, as addNewColumnOnEnd /
  * addNewRowOnEnd (science/infScrn.py:747-791, 825-855); the oldest column
- * (row) is dropped.  ay (ny x 2ny), by (ny x ny), ax (nx x 2nx), bx
+ * (row) is dropped.  axis 2 (columns) and 3 (rows) add them at the start
+ * instead, as addNewColumnOnStart / addNewRowOnStart (:793-823, 857-887)
+ * with AStart, A's column blocks in reverse order (:722-731), on the first
+ * two lines; the last column (row) is dropped.  ay (ny x 2ny), by (ny x ny), ax (nx x 2nx), bx
  * (nx x nx) are row-major float64 host arrays (either axis may be NULL if
  * never extruded); init is the initial screen (ny x nx, host).  noise: NULL
  * for the device's counter-based normals (seed, extrusion index), else n
@@ -366,6 +369,18 @@ shwfs_status shwfs_screen_add(shwfs_screen* s, int axis, int n, double coeff_tur
 shwfs_status shwfs_screen_window(shwfs_screen* s, int y0, int x0, int h, int w, float* out, int64_t out_stride,
                                  void* stream);
 shwfs_status shwfs_screen_read(shwfs_screen* s, float* host_out);
+/* Pupil phase from several layers for a source at infinity (createPupilPhs,
+ * util/atmos.py:678-833, NGS path): layer q contributes the (npup+1)-square
+ * window of screens[q] at logical (y0[q], x0[q]) shifted by linearshift
+ * (cmod/src/interpmodule.c:1234-1300) with fractional shifts yshift[q]
+ * (rows) and xshift[q] (columns) in [0, 1]; layers are added in order, the
+ * piston sum(phase * pupil) / pupil_area is removed when remove_piston, and
+ * the result is multiplied by the pupil and by scale (500 / wavelength in
+ * the reference).  pupil and out are npup x npup device arrays; 1..16
+ * layers.  With stream NULL the call waits for the result. */
+shwfs_status shwfs_screens_pupil_phase(shwfs_screen* const* screens, int nlayers, const int* y0, const int* x0,
+                                       const float* yshift, const float* xshift, int npup, const float* pupil,
+                                       double pupil_area, int remove_piston, float scale, float* out, void* stream);
 shwfs_status shwfs_screen_free(shwfs_screen* s);
 
 /* ---- reconstructor step (science/tomoRecon.py:1077-1107, 1196-1223) ----
