@@ -493,94 +493,164 @@ PRECISION = dict(nsubx=40, Dtel=8.0, obs=0.2, L0=25.0, wavelength=500.0, cases=[
                  r0s=[0.05, 0.1, 0.2, 0.3], sig=1e4, psf_fwhm=1.5)
 
 
+_PREC = {}
+
+
+def _prec_setup(p, N, bases):
+    """Per process: the case's oracle inputs and base screens (pool initializer)."""
+    from dasp_gb300.screens import gaussian_psf
+    from dasp_gb300.tel import Pupil
+    P = PRECISION
+    nsx = P["nsubx"]
+    npup = nsx * p
+    pup = Pupil(npup, npup / 2.0, npup / 2.0 * P["obs"])
+    _PREC.update(p=p, N=N, nsx=nsx, bases=bases, pupfn=pup.perSubap(nsx, 0), subflag=pup.getSubapFlag(nsx, 0.5),
+                 frac=(pup.getSubarea(nsx) / (p * p)).astype(np.float32), psf=gaussian_psf(N, P["psf_fwhm"]))
+
+
+def _prec_frame(bases, f, scale):
+    """Frame f of a case: a flip/transpose/roll of one of the base screens
+    (deterministic in f), scaled for r0."""
+    npup = bases[0].shape[0]
+    rng = np.random.default_rng(1000 + f)
+    s_ = bases[f % len(bases)]
+    s_ = s_[::-1] if rng.random() < 0.5 else s_
+    s_ = s_.T if rng.random() < 0.5 else s_
+    s_ = np.roll(s_, (int(rng.integers(0, npup)), int(rng.integers(0, npup))), axis=(0, 1))
+    return np.ascontiguousarray(s_ * np.float32(scale), dtype=np.float32)
+
+
+def _prec_ref(job):
+    """float64 oracle of frames [f0, f1) at one r0 scale: lit centroids of
+    every frame, lit images of frames below nimg_frames."""
+    from oracle.shwfs_oracle import CentOracle
+    f0, f1, scale, nimg_frames = job
+    c_ = _PREC
+    p, N, nsx = c_["p"], c_["N"], c_["nsx"]
+    lit = c_["subflag"].reshape(-1) == 1
+    orc = CentOracle(nsubx=nsx, phasesize=p, fftsize=N, clipsize=N, nimg=p, ncen=p, pupfn=c_["pupfn"],
+                     subflag=c_["subflag"], fracSubArea=c_["frac"], sig=PRECISION["sig"], spotpsf=c_["psf"],
+                     mode="f64")
+    cents, imgs = [], []
+    for f in range(f0, f1):
+        c = np.zeros(nsx * nsx * 2, np.float32)
+        b = np.zeros((nsx * nsx, p, p), np.float32)
+        orc.run(_prec_frame(c_["bases"], f, scale), c, b)
+        cents.append(c.reshape(-1, 2)[lit].astype(np.float64))
+        if f < nimg_frames:
+            imgs.append(b.reshape(nsx * nsx, -1)[lit].astype(np.float64))
+    return f0, cents, imgs
+
+
 def run_precision(args):
     """Noiseless centroid error (mean/max px over lit subapertures) and
     image-plane relative L2 error of every compute form against the float64
     oracle, on a 40x40-subaperture WFS, phasesize 8/16/32 with fftsize
     16/32/64 (2x padding, nimg = phasesize), r0 0.05-0.3 m on an 8 m pupil
-    (peak-to-valley phase up to a few hundred rad).  The oracle bounds the
-    sample: --precision-frames frames per (phasesize, r0) case."""
-    import torch
+    (peak-to-valley phase up to a few hundred rad).  --precision-frames
+    frames per (phasesize, r0) case (phasesize 32, where only the FP32 form
+    runs, at most 200), the float64 references computed by a pool of host
+    processes over all cores; image errors on the first 16 frames."""
+    import multiprocessing as mp
     from dasp_gb300.centcmod import centcmod
     from dasp_gb300.screens import gaussian_psf, von_karman_screen
     from dasp_gb300.tel import Pupil
-    from oracle.shwfs_oracle import CentOracle
-    torch.cuda.set_device(0)
     P = PRECISION
     nsx = P["nsubx"]
     FORMS = ("fp32", "tf32", "bf16", "fp16", "bf16x3")
     codes = {"fp32": 0, "bf16": 1, "bf16x3": 2, "fp16": 3, "tf32": 4}
-    nfr = int(args.precision_frames)
+    nimg_frames = 16
+    cores = host_cores()
     out = []
     t0 = time.time()
+    # references first (a spawn pool, before the GPU is touched)
+    plan = []
     for p, N in P["cases"]:
+        nfr = int(args.precision_frames) if p < 32 else min(int(args.precision_frames), 200)
+        npup = nsx * p
+        nb = 8 if p < 32 else 4
+        bases = [von_karman_screen(npup, P["Dtel"], P["r0s"][0], P["L0"], 500 + 10 * p + k, P["wavelength"])
+                 for k in range(nb)]
+        refs = {}
+        ctx = mp.get_context("spawn")
+        per = max(1, (nfr + 4 * cores - 1) // (4 * cores))
+        with ctx.Pool(cores, initializer=_prec_setup, initargs=(p, N, bases)) as pool:
+            for r0 in P["r0s"]:
+                scale = (P["r0s"][0] / r0) ** (5.0 / 6.0)
+                jobs = [(f, min(nfr, f + per), scale, nimg_frames) for f in range(0, nfr, per)]
+                cents, imgs = [None] * nfr, [None] * min(nfr, nimg_frames)
+                for f0, cs, ims in pool.imap_unordered(_prec_ref, jobs):
+                    for k, cc in enumerate(cs):
+                        cents[f0 + k] = cc
+                    for k, im in enumerate(ims):
+                        imgs[f0 + k] = im
+                refs[r0] = (scale, cents, imgs)
+        plan.append((p, N, nfr, bases, refs))
+    t_ref = time.time() - t0
+    import torch
+    torch.cuda.set_device(0)
+    for p, N, nfr, bases, refs in plan:
         m = p
         npup = nsx * p
         pup = Pupil(npup, npup / 2.0, npup / 2.0 * P["obs"])
         psf = gaussian_psf(N, P["psf_fwhm"])
-        pupfn = pup.perSubap(nsx, 0)
-        subflag = pup.getSubapFlag(nsx, 0.5)
-        frac = (pup.getSubarea(nsx) / (p * p)).astype(np.float32)
-        lit = subflag.reshape(-1) == 1
-        # one screen per case; von Karman phase scales as r0^(-5/6), and the
-        # frames are flips/transposes/rolls of it
-        base = von_karman_screen(npup, P["Dtel"], P["r0s"][0], P["L0"], 500 + p, P["wavelength"])
-        rng = np.random.default_rng(p)
-        shapes = []
-        for f in range(nfr):
-            s_ = base[::-1] if rng.random() < 0.5 else base
-            s_ = s_.T if rng.random() < 0.5 else s_
-            shapes.append(np.roll(s_, (int(rng.integers(0, npup)), int(rng.integers(0, npup))), axis=(0, 1)))
+        lit = pup.getSubapFlag(nsx, 0.5).reshape(-1) == 1
+        hp = np.zeros((npup, npup), np.float32)  # the engines' bound phase buffer
+        hc = np.zeros(nsx * nsx * 2, np.float32)
+        hb = np.zeros((nsx, nsx, m, m), np.float32)
+        engines = {}
+        for form in FORMS:
+            e = centcmod(1, nsx, m, N, N, m, p, 0.0, 0.0, 0, 0.0, P["sig"], 0.0, 0, 1.0, 1, 0, 1, hp, pup, psf,
+                         hc, hb, 0.5, 0, None, 0, 0.0, None, None, 0, 0, 0, 1, 0, None)
+            e.set_form(form)
+            if e.info()["form_active"] == codes[form]:
+                engines[form] = e
+            else:
+                e.free()
         for r0 in P["r0s"]:
-            scale = np.float32((P["r0s"][0] / r0) ** (5.0 / 6.0))
-            frames = [np.ascontiguousarray(sh * scale, dtype=np.float32) for sh in shapes]
-            pv = float(max(fr.max() - fr.min() for fr in frames))
-            orc = CentOracle(nsubx=nsx, phasesize=p, fftsize=N, clipsize=N, nimg=m, ncen=m, pupfn=pupfn,
-                             subflag=subflag, fracSubArea=frac, sig=P["sig"], spotpsf=psf, mode="f64")
-            ref = []
-            for fr in frames:
-                c = np.zeros(nsx * nsx * 2, np.float32)
-                b = np.zeros((nsx * nsx, m, m), np.float32)
-                orc.run(np.ascontiguousarray(fr), c, b)
-                ref.append((c.reshape(-1, 2)[lit].astype(np.float64), b.reshape(nsx * nsx, -1)[lit].astype(np.float64)))
-            hp = frames[0].copy()  # the engine's bound phase buffer; frames stay intact
-            hc = np.zeros(nsx * nsx * 2, np.float32)
-            hb = np.zeros((nsx, nsx, m, m), np.float32)
-            eng = centcmod(1, nsx, m, N, N, m, p, 0.0, 0.0, 0, 0.0, P["sig"], 0.0, 0, 1.0, 1, 0, 1, hp, pup, psf,
-                           hc, hb, 0.5, 0, None, 0, 0.0, None, None, 0, 0, 0, 1, 0, None)
-            case = {"phasesize": p, "fftsize": N, "nimg": m, "r0_m": r0, "phase_pv_rad": round(pv, 1),
-                    "frames": nfr, "lit_subaps": int(lit.sum()), "forms": {}}
+            scale, rcents, rimgs = refs[r0]
+            case = {"phasesize": p, "fftsize": N, "nimg": m, "r0_m": r0, "frames": nfr,
+                    "image_frames": len(rimgs), "lit_subaps": int(lit.sum()), "forms": {}}
+            errs = {f: [] for f in engines}
+            l2 = {f: [] for f in engines}
+            pv = 0.0
+            for f in range(nfr):
+                hp[...] = _prec_frame(bases, f, scale)
+                pv = max(pv, float(hp.max() - hp.min()))
+                for form, e in engines.items():
+                    e.run(0)
+                    errs[form].append(np.abs(hc.reshape(-1, 2)[lit].astype(np.float64) - rcents[f]).ravel())
+                    if f < len(rimgs):
+                        eb = hb.reshape(nsx * nsx, -1)[lit].astype(np.float64)
+                        l2[form].append(np.linalg.norm(eb - rimgs[f]) / np.linalg.norm(rimgs[f]))
+            case["phase_pv_rad"] = round(pv, 1)
             for form in FORMS:
-                eng.set_form(form)
-                if eng.info()["form_active"] != codes[form]:
-                    case["forms"][form] = {"active": False, "note": "geometry outside the tensor-core limits; FP32 form runs"}
+                if form not in engines:
+                    case["forms"][form] = {"active": False,
+                                           "note": "geometry outside the tensor-core kernel's limits; FP32 form runs"}
                     continue
-                errs, l2 = [], []
-                for fr, (rc, rb) in zip(frames, ref):
-                    hp[...] = fr
-                    eng.run(0)
-                    ec = hc.reshape(-1, 2)[lit].astype(np.float64)
-                    eb = hb.reshape(nsx * nsx, -1)[lit].astype(np.float64)
-                    errs.append(np.abs(ec - rc).ravel())
-                    l2.append(np.linalg.norm(eb - rb) / np.linalg.norm(rb))
-                e = np.concatenate(errs)
-                case["forms"][form] = {"active": True, "mean_err_px": float(e.mean()), "max_err_px": float(e.max()),
-                                       "img_rel_l2": float(np.mean(l2))}
-            eng.free()
+                ee = np.concatenate(errs[form])
+                case["forms"][form] = {"active": True, "mean_err_px": float(ee.mean()), "max_err_px": float(ee.max()),
+                                       "p99_err_px": float(np.percentile(ee, 99)), "img_rel_l2": float(np.mean(l2[form]))}
             out.append(case)
             print(json.dumps({"case": case}), file=sys.stderr, flush=True)
+        for e in engines.values():
+            e.free()
     worst = {f: max((c["forms"][f]["max_err_px"] for c in out if c["forms"][f].get("active")), default=None)
              for f in FORMS}
     line = {
         "metric": "precision sweep: max centroid error vs FP64 oracle (px), noiseless, 40x40 subaps",
-        "value": worst["fp16"], "unit": "px", "n_gpus": 1, "steps": len(out) * nfr, "warmup": 0,
+        "value": worst["fp16"], "unit": "px", "n_gpus": 1, "steps": sum(c["frames"] for c in out), "warmup": 0,
         "ms_per_step": None, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "per form (fp32, tf32, bf16, fp16 with per-subaperture scaling, bf16x3)",
-        "data": "synthetic: seeded von Karman screens (r0 %s m at 500 nm, L0 %g m, %g m pupil)"
+        "data": "synthetic: seeded von Karman screens (r0 %s m at 500 nm, L0 %g m, %g m pupil); frames are "
+                "flips/transposes/rolls of 8 base screens per case (4 for phasesize 32)"
                 % (P["r0s"], P["L0"], P["Dtel"]),
         "config": {"workload": "precision_sweep_40x40", "nsubx": nsx, "cases": P["cases"], "r0_m": P["r0s"],
-                   "frames_per_case": nfr, "note": "frames bounded by the float64 oracle's CPU time"},
+                   "frames_per_case": {str(c[0]): c[2] for c in plan}, "image_error_frames": nimg_frames,
+                   "reference": "float64 oracle on %d host processes" % cores},
         "max_err_px_by_form": worst, "cases": out, "wall_s": round(time.time() - t0, 1),
+        "reference_wall_s": round(t_ref, 1),
     }
     print(json.dumps(line), flush=True)
 
