@@ -336,12 +336,10 @@ __device__ __forceinline__ int poisson_table_int(const PoisTab& T, int L, uint32
   return coin < T.prob[o + i] ? (int)i : (int)T.alias[o + i];
 }
 
-__device__ __forceinline__ float poisson_tab(const PoisTab& T, uint32_t w3, float u4, float lam) {
-  const int L = (int)lam;
-  const float d = lam - (float)L;  // exact
-  const int k = poisson_table_int(T, L, w3);
-  // Poisson(d), d < 1: smallest j with u4 <= F_j, F_j the CDF (d = 0 gives
-  // F_0 = 1, hence j = 0, without a branch)
+// Poisson(d), 0 <= d < 1, by inversion of the uniform u4: the smallest j
+// with u4 <= F_j, F_j the CDF (d = 0 gives F_0 = 1, hence j = 0, without a
+// branch); the first four terms without branches
+__device__ __forceinline__ int poisson_frac(float d, float u4) {
   float t = __expf(-d), F = t;
   int k2 = u4 > F ? 1 : 0;
   t *= d;
@@ -361,7 +359,13 @@ __device__ __forceinline__ float poisson_tab(const PoisTab& T, uint32_t w3, floa
     }
     k2 = j;
   }
-  return (float)(k + k2);
+  return k2;
+}
+
+__device__ __forceinline__ float poisson_tab(const PoisTab& T, uint32_t w3, float u4, float lam) {
+  const int L = (int)lam;
+  const float d = lam - (float)L;  // exact
+  return (float)(poisson_table_int(T, L, w3) + poisson_frac(d, u4));
 }
 
 // Below lambda 64 the modal inversion above (one uniform); above, Hormann's
@@ -400,21 +404,6 @@ cudaError_t pois_table_device(const PoisTab** out);
 // (ctasPerSM may be NULL)
 cudaError_t kernel_smem_setup(const void* kern, int smem, int threads, int* ctasPerSM);
 
-// Poisson(lam) from the pixel's stream: below lambda 64 the tabulated
-// sampler (two uniforms, poisson_tab), above PTRS (poisson_counter).  (Summing
-// tabulated Poisson(63) parts for larger lambda is exact too, but measured
-// slower than PTRS from lambda 64 on.)
-template <class Stream>
-__device__ __forceinline__ float poisson_counter_tab(Stream& st, float lam, const PoisTab& T) {
-  if (!(lam > 0.0f)) return 0.0f;
-  if (lam < kModalMaxLam) {
-    const uint32_t w3 = st.next_u32();
-    const float u4 = st.uniform();
-    return poisson_tab(T, w3, u4, lam);
-  }
-  return poisson_counter(st, lam);
-}
-
 // one standard normal deviate from two uniforms (Box-Muller, cosine branch)
 __device__ __forceinline__ float normal_from_uniforms(float u1, float u2) {
   const float q = -2.0f * __logf(u1);  // > 0: u1 < 1
@@ -422,15 +411,104 @@ __device__ __forceinline__ float normal_from_uniforms(float u1, float u2) {
   return r * __cosf(6.28318530717958648f * u2 - 3.14159265358979324f) * -1.0f;
 }
 
-__device__ __forceinline__ float normal_from_u32(uint32_t w1, uint32_t w2) {
-  return normal_from_uniforms(u32_to_uniform(w1), u32_to_uniform(w2));
-}
-
 // one standard normal deviate from the stream's next two uniforms
 template <class Stream>
 __device__ __forceinline__ float normal_counter(Stream& st) {
   const float u1 = st.uniform(), u2 = st.uniform();
   return normal_from_uniforms(u1, u2);
+}
+
+// Counter-based noise of one quad of pixels -- pixels 4q .. 4q+3 of
+// subaperture i in frame f (the last quad of an image may be partial):
+// blocks 0, 1, 2 of the stream (seed, f, i, quad q, purpose 0).  Block 0
+// holds two Box-Muller pairs, the four pixels' read-noise normals (cosine
+// then sine branch of each pair); block 1 the four alias words and block 2
+// the four inversion uniforms of the tabulated Poisson draws (lambda < 64).
+// A pixel whose mean needs the rejection sampler (lambda >= 64) draws it
+// from its own stream (seed, f, i, pixel, purpose 4); summing tabulated
+// Poisson(63) parts would be exact there too, but measured slower than PTRS
+// from lambda 64 on.  Three blocks for four pixels: every 32-bit word is used
+// once.
+constexpr uint32_t kPurposeQuad = 0u, kPurposePtrs = 4u;
+
+// block b of the stream of quad `quad` of subaperture `subap` in `frame`
+__device__ __forceinline__ U4 quad_block(const PhiloxKeys& K, uint32_t frame, uint32_t subap, uint32_t quad,
+                                         uint32_t b) {
+  U4 c;
+  c.x = b;
+  c.y = quad | (kPurposeQuad << 24);
+  c.z = subap;
+  c.w = frame;
+  return philox4x32_10_rk(c, K);
+}
+
+// two standard normal deviates from two words (Box-Muller: cosine and sine
+// branch of one pair)
+__device__ __forceinline__ void normal_pair(uint32_t w1, uint32_t w2, float& g0, float& g1) {
+  const float u1 = u32_to_uniform(w1), u2 = u32_to_uniform(w2);
+  const float q = -2.0f * __logf(u1);  // > 0: u1 < 1
+  const float r = q * rsqrtf(q);
+  float sn, cs;
+  __sincosf(6.28318530717958648f * u2 - 3.14159265358979324f, &sn, &cs);
+  g0 = -r * cs;
+  g1 = -r * sn;
+}
+
+// the read-noise normals of the quad's four pixels (block 0)
+__device__ __forceinline__ void quad_normals(const PhiloxKeys& K, uint32_t frame, uint32_t subap, uint32_t quad,
+                                             float (&g)[4]) {
+  const U4 r = quad_block(K, frame, subap, quad, 0u);
+  normal_pair(r.x, r.y, g[0], g[1]);
+  normal_pair(r.z, r.w, g[2], g[3]);
+}
+
+// the read-noise normal of pixel `pixel` alone (its quad's block 0)
+__device__ __forceinline__ float pixel_normal(const PhiloxKeys& K, uint32_t frame, uint32_t subap, uint32_t pixel) {
+  const U4 r = quad_block(K, frame, subap, pixel >> 2, 0u);
+  const bool hi = (pixel & 2u) != 0;
+  float g0, g1;
+  normal_pair(hi ? r.z : r.x, hi ? r.w : r.y, g0, g1);
+  return (pixel & 1u) ? g1 : g0;
+}
+
+// Shot noise of the quad's pixels in place (blocks 1 and 2): v[k] becomes a
+// Poisson(v[k]) draw of the tabulated sampler; lambda <= 0 or NaN draws 0.
+// Pixels whose bit is set in `skip` keep their value: every pixel with
+// lambda >= 64 must be among them (drawn by ptrs_pixel).
+__device__ __forceinline__ void quad_poisson(const PhiloxKeys& K, uint32_t frame, uint32_t subap, uint32_t quad,
+                                             const PoisTab& T, float (&v)[4], unsigned skip) {
+  const U4 w = quad_block(K, frame, subap, quad, 1u);
+  const U4 u = quad_block(K, frame, subap, quad, 2u);
+  const uint32_t ws[4] = {w.x, w.y, w.z, w.w}, us[4] = {u.x, u.y, u.z, u.w};
+  // the four alias-table draws first, without branches (skipped pixels draw
+  // Poisson(0)), so that their shared-memory reads overlap; then the
+  // fractional parts
+  float lam[4];
+  int kt[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    lam[k] = ((skip >> k) & 1u) ? 0.0f : fmaxf(v[k], 0.0f);
+    kt[k] = poisson_table_int(T, (int)lam[k], ws[k]);
+  }
+#pragma unroll
+  for (int k = 0; k < 4; k++)
+    if (!((skip >> k) & 1u))
+      v[k] = (float)(kt[k] + poisson_frac(lam[k] - (float)(int)lam[k], u32_to_uniform(us[k])));
+}
+
+// shot noise of a pixel with lambda >= 64 from its own stream (PTRS)
+__device__ __forceinline__ float ptrs_pixel(const PhiloxKeys& K, uint32_t frame, uint32_t subap, uint32_t pixel,
+                                            float lam) {
+  KeyedStream st(K, frame, (int)subap, (int)pixel, (int)kPurposePtrs);
+  return poisson_counter(st, lam);
+}
+
+// ptrs_pixel as an out-of-line call (the same stream, keys from the seed),
+// for a rare path of a kernel whose registers are tight
+static __device__ __noinline__ float ptrs_pixel_cold(unsigned long long seed, uint32_t frame, uint32_t subap,
+                                              uint32_t pixel, float lam) {
+  CounterStream st(seed, frame, (int)subap, (int)pixel, (int)kPurposePtrs);
+  return poisson_counter(st, lam);
 }
 
 // floor(w / d) for 0 <= w < 2^22 and d >= 1 with the float reciprocal

@@ -722,25 +722,36 @@ __global__ void __launch_bounds__(kThreads) wfs_plain_kernel(const WfsArgs a) {
     }
 
     // ---- 6: Poisson + read noise + threshold (counter-based streams) ----
+    // one thread per quad of pixels (quad_normals, quad_poisson; lambda >= 64
+    // from the pixel's own stream, ptrs_pixel), pixels from nexp on untouched
     if (doNoise) {
       const bool pois = a.addPoisson == 1 && a.calsource == 0;
       const float rn = a.calsource == 0 ? a.readNoise : 0.f;
-      for (int w = tid; w < ns * mm; w += blockDim.x) {
-        const int s = w / mm, pix = w - (w / mm) * mm;
-        if (pix >= nexp) continue;
-        const int i = s_subap[s];
-        const unsigned long long fr = frame_base(a) + s_frame[s];
-        float v = IMG(s)[pix];
-        // one stream per pixel: the read-noise normal takes the first two
-        // uniforms, the Poisson sampler continues from the third
-        CounterStream st(a.seed, fr, i, pix, 0);
-        const float g = rn != 0.f ? normal_counter(st) : 0.f;
-        if (pois && SCAL(s)[0] != 0.f) v = poisson_counter_tab(st, v, *a.poisTab);
-        if (rn != 0.f)
-          v += rn * g + a.readBg;
-        else
-          v += a.readBg;
-        IMG(s)[pix] = threshold_px(v, a.floorv, a.threshType);
+      const int nqi = (nexp + 3) >> 2;
+      for (int wq = tid; wq < ns * nqi; wq += blockDim.x) {
+        const int s = wq / nqi, qd = wq - s * nqi;
+        const int p0 = 4 * qd, np = min(4, nexp - p0);
+        const uint32_t i = (uint32_t)s_subap[s];
+        const uint32_t fr = (uint32_t)(frame_base(a) + s_frame[s]);
+        float* px = IMG(s) + p0;
+        float v[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) v[k] = k < np ? px[k] : 0.f;
+        if (pois && SCAL(s)[0] != 0.f) {
+          unsigned bm = 0;
+#pragma unroll
+          for (int k = 0; k < 4; k++)
+            if (v[k] >= kModalMaxLam) bm |= 1u << k;
+          quad_poisson(a.philoxKeys, fr, i, (uint32_t)qd, *a.poisTab, v, bm);
+#pragma unroll
+          for (int k = 0; k < 4; k++)
+            if ((bm >> k) & 1u) v[k] = ptrs_pixel_cold(a.seed, fr, i, (uint32_t)(p0 + k), v[k]);
+        }
+        float g[4] = {0.f, 0.f, 0.f, 0.f};
+        if (rn != 0.f) quad_normals(a.philoxKeys, fr, i, (uint32_t)qd, g);
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+          if (k < np) px[k] = threshold_px(v[k] + (rn * g[k] + a.readBg), a.floorv, a.threshType);
       }
       __syncthreads();
     }

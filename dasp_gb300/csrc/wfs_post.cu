@@ -4,15 +4,15 @@
 // normalised pre-noise image in bimg; this kernel adds the counter-based
 // Poisson and read noise, thresholds (cmod/src/centmodule.c:1874-1882,
 // 785-817) and runs the shared post stages (post_tile: brightest pixels,
-// pixel power, bimg write, centroids, calibration, references).  Each pixel
-// draws from the same (seed, frame, subaperture, pixel) stream as in the
-// fused FP32 kernel, so equal pre-noise images give equal noisy images.
+// pixel power, bimg write, centroids, calibration, references).  Each quad
+// of pixels draws from the same (seed, frame, subaperture, quad) stream as
+// in the fused FP32 kernel, so equal pre-noise images give equal noisy
+// images.
 //
 // A separate launch rather than a stage of the tensor-core kernel: the noise
 // samplers are latency-bound scalar code that wants many resident warps,
 // while the tensor-core kernel holds one 608-thread CTA per SM.
 #include <algorithm>
-#include <type_traits>
 
 #include "gemm_form.h"
 #include "wfs_plain.cuh"
@@ -25,7 +25,9 @@ constexpr int kPostThreads = 256;
 constexpr int kPostMaxTS = 64;
 constexpr int kPostBright = 512;  // queued bright pixels per tile (overflow: drawn in place)
 
-__global__ void __launch_bounds__(kPostThreads, 4) wfs_post_kernel(const WfsArgs a, const PoisTab* __restrict__ tab) {
+// three CTAs per SM: a tile's images (up to 32 KB) and the Poisson table
+// (22 KB) in shared memory allow no more
+__global__ void __launch_bounds__(kPostThreads, 3) wfs_post_kernel(const WfsArgs a, const PoisTab* __restrict__ tab) {
   extern __shared__ __align__(16) float smem_post[];
   __shared__ int s_subap[kPostMaxTS];
   __shared__ int s_frame[kPostMaxTS];
@@ -86,52 +88,80 @@ __global__ void __launch_bounds__(kPostThreads, 4) wfs_post_kernel(const WfsArgs
     }
     asm volatile("cp.async.wait_all;" ::: "memory");
     __syncthreads();
-    // noise, threshold [, power, bimg write] of pixel w of the tile
-    auto pixel = [&](int w, float v) {
-      const int s = div_small(w, mm, inv_mm), pix = w - s * mm;
-      const int i = s_subap[s];
-      if (noise) {
-        // one stream per pixel: the read-noise normal takes the first two
-        // uniforms, the Poisson sampler continues from the third
-        CounterStream st(a.seed, fbase + s_frame[s], i, pix, 0);
-        const float g = rn != 0.f ? normal_counter(st) : 0.f;
-        if (pois && s_pflag[s]) v = poisson_counter_tab(st, v, *s_tab);
-        if (rn != 0.f)
-          v += rn * g + a.readBg;
-        else
-          v += a.readBg;
-        v = threshold_px(v, a.floorv, a.threshType);
-      }
+    // threshold [, power, bimg write] of pixel pix of tile item s, value v
+    // after the noise
+    auto store = [&](int s, int pix, float v) {
       if (simple) {
         // pixel power and the bimg write of post_tile's stage 8, here
         if (a.pxlPower == 2.f)
           v = v * v;
         else if (a.pxlPower != 1.f && a.pxlPower != 0.f)
           v = powf(v, a.pxlPower);
-        a.bimg[(long long)s_frame[s] * a.bimgFrameStride + (long long)i * mm + pix] = v;
+        a.bimg[(long long)s_frame[s] * a.bimgFrameStride + (long long)s_subap[s] * mm + pix] = v;
       }
       imgs[s * mm + pix] = v;
     };
-    // Pixels whose Poisson mean needs the rejection sampler (lambda >= 64)
-    // are queued and drawn afterwards with the whole CTA, so that one bright
+    auto finish = [&](float v, float g) {
+      if (noise) {
+        v += rn * g + a.readBg;
+        v = threshold_px(v, a.floorv, a.threshType);
+      }
+      return v;
+    };
+    // one lane per quad of pixels (quad_normals, quad_poisson).  Pixels
+    // whose Poisson mean needs the rejection sampler (lambda >= 64) are
+    // queued and drawn afterwards with the whole CTA, so that one bright
     // pixel does not hold the other 31 lanes of its warp (same streams, same
     // draws).
-    for (int w = tid; w < ns * mm; w += blockDim.x) {
-      const int s = div_small(w, mm, inv_mm);
-      const float v = imgs[w];
-      if (noise && pois && s_pflag[s] && v >= kModalMaxLam) {
-        const int slot = atomicAdd(&s_nbright, 1);
-        if (slot < kPostBright) {
-          s_bright[slot] = w;
-          s_brightv[slot] = v;
-          continue;
+    const int nqi = (mm + 3) >> 2;
+    const float inv_nqi = 1.0f / (float)nqi;
+    for (int wq = tid; wq < ns * nqi; wq += blockDim.x) {
+      const int s = div_small(wq, nqi, inv_nqi), qd = wq - s * nqi;
+      const int p0 = 4 * qd, np = min(4, mm - p0);
+      const int i = s_subap[s];
+      const uint32_t fr = (uint32_t)(fbase + s_frame[s]);
+      float v[4];
+#pragma unroll
+      for (int k = 0; k < 4; k++) v[k] = k < np ? imgs[s * mm + p0 + k] : 0.f;
+      unsigned bm = 0;  // bright pixels, queued
+      float g[4] = {0.f, 0.f, 0.f, 0.f};
+      if (noise) {
+        if (pois && s_pflag[s]) {
+          unsigned inplace = 0;  // bright pixels past the queue's end
+#pragma unroll
+          for (int k = 0; k < 4; k++) {
+            if (k < np && v[k] >= kModalMaxLam) {
+              const int slot = atomicAdd(&s_nbright, 1);
+              if (slot < kPostBright) {
+                s_bright[slot] = s * mm + p0 + k;
+                s_brightv[slot] = v[k];
+                bm |= 1u << k;
+              } else {
+                inplace |= 1u << k;
+              }
+            }
+          }
+          quad_poisson(a.philoxKeys, fr, (uint32_t)i, (uint32_t)qd, *s_tab, v, bm | inplace);
+#pragma unroll
+          for (int k = 0; k < 4; k++)
+            if ((inplace >> k) & 1u) v[k] = ptrs_pixel_cold(a.seed, fr, (uint32_t)i, (uint32_t)(p0 + k), v[k]);
         }
+        if (rn != 0.f) quad_normals(a.philoxKeys, fr, (uint32_t)i, (uint32_t)qd, g);
       }
-      pixel(w, v);
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+        if (k < np && !((bm >> k) & 1u)) store(s, p0 + k, finish(v[k], g[k]));
     }
     __syncthreads();
     const int nb = min(s_nbright, kPostBright);
-    for (int k = tid; k < nb; k += blockDim.x) pixel(s_bright[k], s_brightv[k]);
+    for (int k = tid; k < nb; k += blockDim.x) {
+      const int w = s_bright[k];
+      const int s = div_small(w, mm, inv_mm), pix = w - s * mm;
+      const int i = s_subap[s];
+      const uint32_t fr = (uint32_t)(fbase + s_frame[s]);
+      const float g = rn != 0.f ? pixel_normal(a.philoxKeys, fr, (uint32_t)i, (uint32_t)pix) : 0.f;
+      store(s, pix, finish(ptrs_pixel(a.philoxKeys, fr, (uint32_t)i, (uint32_t)pix, s_brightv[k]), g));
+    }
     __syncthreads();
     if (!simple) {
       post_tile(a, ns, s_subap, s_frame, s_cw, [&](int s) { return imgs + s * mm; }, [&](int) { return mm; });
@@ -176,7 +206,7 @@ __global__ void __launch_bounds__(kPostThreads, 4) wfs_post_kernel(const WfsArgs
 }
 
 constexpr int kWarpThreads = 256;  // 8 warps per CTA
-constexpr int kWarpQ = 32;         // queued bright pixels per warp and chunk
+constexpr int kWarpQ = 160;        // queued bright pixels per warp (at most 32 + one round's 128); even
 constexpr int kWarpMaxK = 16;      // subaperture-frames per chunk
 
 // Per-warp shared memory: two pixel buffers of bufPx floats (the chunk being
@@ -185,23 +215,26 @@ constexpr int kWarpMaxK = 16;      // subaperture-frames per chunk
 // Poisson flag, frame} and the 64-bit offset of its image in bimg), the
 // window-row partial sums of the centroids and the bright-pixel queue.
 __host__ __device__ inline int warp_smem_floats(int bufPx, int ncen) {
-  return 2 * bufPx + 2 * 6 * kWarpMaxK + 2 * kWarpMaxK * ncen + 2 * kWarpQ;
+  return 2 * bufPx + 2 * 6 * kWarpMaxK + 2 * kWarpMaxK * ncen + kWarpQ / 2;
 }
 
 // The common configuration (window CoG or image only; no brightest-pixel
 // selection, fit or optical binning), one warp per chunk of K consecutive
-// lit subaperture-frames: the chunk's pixels are drawn with the lanes over
-// the flattened pixel index (every lane busy whatever nimg is), bright
-// pixels (lambda >= 64, the rejection sampler) queued and drawn together
-// afterwards, then the window centroids from the chunk's images in shared
+// lit subaperture-frames: the chunk's pixels are drawn a quad (four
+// consecutive pixels of one image) per lane, lanes over the chunk's
+// flattened quad index (every lane busy whatever nimg is), with 16-byte
+// loads and stores when nimg^2 is a multiple of 4.  Bright pixels
+// (lambda >= 64, the rejection sampler) are queued and drawn by the whole
+// warp after a round that left more than 32 in the queue and after the
+// last, then the window centroids come from the chunk's images in shared
 // memory.  Warps are independent (no block barrier after the table load);
 // each copies its next chunk into shared memory with cp.async while it
 // draws the current one.  Unlit subapertures are not visited; their
 // centroids are zeroed at the end (zeroUnlit).  Pixels and streams are
-// those of wfs_post_kernel and of the fused FP32 kernel: the pixel of
-// subaperture i, frame f and index p draws from the counter stream
-// (seed, f, i, p) -- read-noise normal first, then the Poisson draw.
-// RN (read noise on) and POIS (Poisson on) are compile-time.
+// those of wfs_post_kernel and of the fused FP32 kernel (quad_normals,
+// quad_poisson, ptrs_pixel), so equal pre-noise images give equal noisy
+// images in every form.  RN (read noise on) and POIS (Poisson on) are
+// compile-time.
 template <bool RN, bool POIS>
 __global__ void __launch_bounds__(kWarpThreads, 3)
     wfs_post_warp_kernel(const WfsArgs a, const PoisTab* __restrict__ tab, int K, int bufPx) {
@@ -217,8 +250,9 @@ __global__ void __launch_bounds__(kWarpThreads, 3)
   int4* item0 = reinterpret_cast<int4*>(wbase + 2 * bufPx);
   long long* off0 = reinterpret_cast<long long*>(item0 + 2 * kWarpMaxK);
   float* s_rows = wbase + 2 * bufPx + 12 * kWarpMaxK;
-  int* q_idx = reinterpret_cast<int*>(s_rows + 2 * kWarpMaxK * ncen);
-  float* q_val = reinterpret_cast<float*>(q_idx + kWarpQ);
+  // queued pixels as 16-bit indices into the chunk's buffer (bufPx <= 3200:
+  // the launcher's 200 KB bound on 16 buffers of bufPx floats)
+  unsigned short* q_idx = reinterpret_cast<unsigned short*>(s_rows + 2 * kWarpMaxK * ncen);
   if constexpr (POIS) {
     const int4* src = reinterpret_cast<const int4*>(tab);
     int4* dst = reinterpret_cast<int4*>(s_tab);
@@ -250,6 +284,9 @@ __global__ void __launch_bounds__(kWarpThreads, 3)
   const float tsub = a.threshType == 0 ? a.floorv : 0.f;
   const bool pw1 = a.pxlPower == 1.f || a.pxlPower == 0.f;
   const bool out2 = a.bimgOut != nullptr;
+  // whole quads with 16-byte loads and stores
+  const bool vec4 = (mm & 3) == 0 && (a.bimgFrameStride & 3) == 0 && ((uintptr_t)a.bimg & 15) == 0 &&
+                    (!out2 || ((uintptr_t)a.bimgOut & 15) == 0);
 
   // item table of chunk c into buffer b's table (lanes < K), then its
   // pixels into buffer b with cp.async (one commit group per lane, empty
@@ -320,108 +357,125 @@ __global__ void __launch_bounds__(kWarpThreads, 3)
     float* img = wbase + b * bufPx;
     const int4* items = item0 + b * kWarpMaxK;
     const long long* offs = off0 + b * kWarpMaxK;
-    // noise and threshold of a pixel drawn from its stream (seed, frame,
-    // subaperture, pixel): the read-noise normal takes the block's first two
-    // uniforms, the tabulated Poisson draw the next two (the first two
-    // without read noise) -- KeyedStream's order, with the block explicit
-    auto draw_fast = [&](float v, uint32_t sub, uint32_t frm, int pix, int pf) {
-      U4 c;
-      c.x = 0u;
-      c.y = (uint32_t)pix;
-      c.z = sub;
-      c.w = frm;
-      const U4 r = philox4x32_10_rk(c, a.philoxKeys);
-      float g = 0.f;
-      if constexpr (RN) g = normal_from_u32(r.x, r.y);
-      if constexpr (POIS) {
-        // lambda <= 0 (or NaN) draws 0, as the table's L = 0 column gives
-        const uint32_t w3 = RN ? r.z : r.x, w4 = RN ? r.w : r.y;
-        const float vp = poisson_tab(*s_tab, w3, u32_to_uniform(w4), fmaxf(v, 0.f));
-        v = pf ? vp : v;
-      }
+    // noise, threshold, power and stores of one pixel (x: its mean; g: its
+    // read-noise normal)
+    auto finish = [&](float x, float g) {
       if constexpr (RN)
-        v += rn * g + a.readBg;
+        x += rn * g + a.readBg;
       else
-        v += a.readBg;
-      return v < thr ? 0.f : v - tsub;
-    };
-    // the rejection-sampler path (lambda >= 64): the same stream, continued
-    auto draw_bright = [&](float v, uint32_t sub, uint32_t frm, int pix) {
-      KeyedStream st(a.philoxKeys, frm, (int)sub, pix, 0);
-      float g = 0.f;
-      if constexpr (RN) g = normal_counter(st);
-      if constexpr (POIS) v = poisson_counter_tab(st, v, *s_tab);
-      if constexpr (RN)
-        v += rn * g + a.readBg;
-      else
-        v += a.readBg;
-      return v < thr ? 0.f : v - tsub;
-    };
-    auto store = [&](long long off, int g, float v) {
-      if (!pw1) v = a.pxlPower == 2.f ? v * v : powf(v, a.pxlPower);
-      a.bimg[off] = v;
-      if (out2) a.bimgOut[off] = v;
-      if (cents) img[g] = v;
+        x += a.readBg;
+      x = x < thr ? 0.f : x - tsub;
+      if (!pw1) x = a.pxlPower == 2.f ? x * x : powf(x, a.pxlPower);
+      return x;
     };
     int nq = 0;  // bright pixels queued (warp-uniform)
-    const int npx = nk * mm;
-    // this lane's pixel g = g0 + lane is pixel pix of item s
-    int s = 0, pix = lane;
-    while (pix >= mm) {
-      pix -= mm;
+    const int nqi = (mm + 3) >> 2, nqc = nk * nqi;  // quads per item, per chunk
+    // this lane's quad Q = Q0 + lane of the chunk is quad q of item s
+    int s = 0, q = lane;
+    while (q >= nqi) {
+      q -= nqi;
       s++;
     }
-    // one round of 32 pixels; TAIL: the last, partial round
-    auto round = [&](int g0, auto TAIL) {
-      const int g = g0 + lane;
-      const bool in = !decltype(TAIL)::value || g < npx;
-      const int4 it = items[in ? s : 0];
-      const long long ob = offs[in ? s : 0];
-      float v = img[in ? g : 0];
-      bool queued = false, bright = false;
+    // one round of 32 quads (the last may be partial)
+    auto round = [&](int Q0) {
+      const bool in = Q0 + lane < nqc;
+      const int si = in ? s : 0;
+      const int4 it = items[si];
+      (void)it;  // unused without noise
+      const int p0 = 4 * q, np = in ? min(4, mm - p0) : 0;
+      float* src = img + si * mm + p0;
+      float v[4];
+      if (vec4 && in) {
+        const float4 t = *reinterpret_cast<const float4*>(src);
+        v[0] = t.x, v[1] = t.y, v[2] = t.z, v[3] = t.w;
+      } else {
+#pragma unroll
+        for (int k = 0; k < 4; k++) v[k] = k < np ? src[k] : 0.f;
+      }
+      unsigned bmask = 0;  // pixels with lambda >= 64, queued
       if constexpr (POIS) {
-        bright = noise && in && it.z && v >= kModalMaxLam;
-        const unsigned bm = __ballot_sync(0xffffffffu, bright);
-        if (bm) {
-          if (bright) {
-            const int slot = nq + __popc(bm & ((1u << lane) - 1u));
-            if (slot < kWarpQ) {
-              q_idx[slot] = g;
-              q_val[slot] = v;
-              queued = true;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          const bool br = noise && k < np && it.z && v[k] >= kModalMaxLam;
+          const unsigned bm = __ballot_sync(0xffffffffu, br);
+          if (bm) {
+            if (br) {
+              bmask |= 1u << k;
+              const int slot = nq + __popc(bm & ((1u << lane) - 1u));
+              q_idx[slot] = (unsigned short)(si * mm + p0 + k);
+            }
+            nq += __popc(bm);
+          }
+        }
+      }
+      if (noise && in) {
+        float g[4] = {0.f, 0.f, 0.f, 0.f};
+        if constexpr (RN) quad_normals(a.philoxKeys, (uint32_t)it.y, (uint32_t)it.x, (uint32_t)q, g);
+        if constexpr (POIS) {
+          if (it.z) {
+            quad_poisson(a.philoxKeys, (uint32_t)it.y, (uint32_t)it.x, (uint32_t)q, *s_tab, v, bmask);
+          }
+        }
+        // a queued pixel keeps its mean (in img too) until the drain
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          const float x = finish(v[k], g[k]);
+          v[k] = ((bmask >> k) & 1u) ? v[k] : x;
+        }
+      } else if (!pw1) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) v[k] = a.pxlPower == 2.f ? v[k] * v[k] : powf(v[k], a.pxlPower);
+      }
+      if (in) {
+        const long long ob = offs[si] + p0;
+        // (queued pixels too: the drain overwrites them after a __syncwarp)
+        if (vec4) {
+          const float4 t = make_float4(v[0], v[1], v[2], v[3]);
+          *reinterpret_cast<float4*>(a.bimg + ob) = t;
+          if (out2) *reinterpret_cast<float4*>(a.bimgOut + ob) = t;
+          if (cents) *reinterpret_cast<float4*>(src) = t;
+        } else {
+#pragma unroll
+          for (int k = 0; k < 4; k++) {
+            if (k < np) {
+              a.bimg[ob + k] = v[k];
+              if (out2) a.bimgOut[ob + k] = v[k];
+              if (cents) src[k] = v[k];
             }
           }
-          nq += __popc(bm);
         }
       }
-      if (in && !queued) {
-        if (noise) {
-          if (POIS && bright)
-            v = draw_bright(v, (uint32_t)it.x, (uint32_t)it.y, pix);
-          else
-            v = draw_fast(v, (uint32_t)it.x, (uint32_t)it.y, pix, it.z);
-        }
-        store(ob + pix, g, v);
-      }
-      pix += 32;
-      while (pix >= mm) {
-        pix -= mm;
+      q += 32;
+      while (q >= nqi) {
+        q -= nqi;
         s++;
       }
     };
-    const int nfull = npx & ~31;
-    for (int g0 = 0; g0 < nfull; g0 += 32) round(g0, std::false_type{});
-    if (nfull < npx) round(nfull, std::true_type{});
-    if constexpr (POIS) {
-      if (noise && nq) {
-        __syncwarp();
-        for (int q = lane; q < min(nq, kWarpQ); q += 32) {
-          const int g = q_idx[q];
-          const int sq = div_small(g, mm, inv_mm), pq = g - sq * mm;
-          const int4 it = items[sq];
-          store(offs[sq] + pq, g, draw_bright(q_val[q], (uint32_t)it.x, (uint32_t)it.y, pq));
-        }
+    // the queued bright pixels, drawn by the whole warp: after a round that
+    // left more than 32 (a round queues at most 128) and after the last round
+    auto drain = [&]() {
+      __syncwarp();
+      for (int k = lane; k < nq; k += 32) {
+        const int g = q_idx[k];
+        const int sq = div_small(g, mm, inv_mm), pq = g - sq * mm;
+        const int4 it = items[sq];
+        float gn = 0.f;
+        if constexpr (RN) gn = pixel_normal(a.philoxKeys, (uint32_t)it.y, (uint32_t)it.x, (uint32_t)pq);
+        const float x = finish(ptrs_pixel(a.philoxKeys, (uint32_t)it.y, (uint32_t)it.x, (uint32_t)pq, img[g]), gn);
+        a.bimg[offs[sq] + pq] = x;
+        if (out2) a.bimgOut[offs[sq] + pq] = x;
+        if (cents) img[g] = x;
       }
+      nq = 0;
+      __syncwarp();
+    };
+    // one copy of each in the loop: the samplers' code is large, and a
+    // second copy of either (a separate last round, a drain after the loop)
+    // overflowed the instruction cache
+    for (int Q0 = 0; Q0 < nqc; Q0 += 32) {
+      round(Q0);
+      if constexpr (POIS)
+        if (nq > kWarpQ - 128 || (nq && Q0 + 32 >= nqc)) drain();
     }
     if (cents) {
       __syncwarp();

@@ -1,5 +1,6 @@
 // Unlit-subaperture kernel of the WFS step.
 #include <algorithm>
+#include <cstring>
 
 #include "wfs_plain.cuh"
 
@@ -71,16 +72,48 @@ cudaError_t launch_set_counter(unsigned long long* ctr, unsigned long long v, cu
   return cudaGetLastError();
 }
 
-// n draws of the counter-based noise (kind 0 Poisson of mean lam[i], kind 1
-// standard normal), element i from the stream of (seed, frame, i), as the
-// pipeline draws one pixel's noise
-__global__ void sample_noise_kernel(const float* __restrict__ lam, long long n, unsigned long long seed,
-                                    unsigned long long frame, int kind, float* __restrict__ out,
-                                    const PoisTab* __restrict__ tab) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    CounterStream st(seed, frame, (int)(i >> 16), (int)(i & 0xffff), 2);
-    out[i] = kind == 0 ? poisson_counter(st, lam[i])
-                       : (kind == 2 ? poisson_counter_tab(st, lam[i], *tab) : normal_counter(st));
+// n draws of the counter-based noise, element i as the pipeline draws pixel
+// i & 0xffff of subaperture i >> 16 in frame `frame` (one thread per quad of
+// four elements): kind 1 its read-noise normal (quad_normals), kind 2 its
+// Poisson(lam[i]) shot noise (quad_poisson below lambda 64, ptrs_pixel
+// above); kind 0 Poisson(lam[i]) by the table-free modal inversion / PTRS
+// from the element's own stream (seed, frame, i >> 16, i & 0xffff, purpose
+// 2), an independent sampler kept to cross-check kind 2
+__global__ void sample_noise_kernel(const float* __restrict__ lam, long long n, const PhiloxKeys keys,
+                                    unsigned long long seed, unsigned long long frame, int kind,
+                                    float* __restrict__ out, const PoisTab* __restrict__ tab) {
+  const long long nq = (n + 3) >> 2;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nq; t += (long long)gridDim.x * blockDim.x) {
+    const long long i0 = 4 * t;
+    const int np = (int)(n - i0 < 4 ? n - i0 : 4);
+    const uint32_t subap = (uint32_t)(i0 >> 16), pix0 = (uint32_t)(i0 & 0xffff), fr = (uint32_t)frame;
+    float v[4];
+    if (kind == 0) {
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        v[k] = 0.f;
+        if (k < np) {
+          CounterStream st(seed, frame, (int)subap, (int)(pix0 + k), 2);
+          v[k] = poisson_counter(st, lam[i0 + k]);
+        }
+      }
+    } else if (kind == 1) {
+      quad_normals(keys, fr, subap, pix0 >> 2, v);
+    } else {
+      unsigned bm = 0;
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        v[k] = k < np ? lam[i0 + k] : 0.f;
+        if (v[k] >= kModalMaxLam) bm |= 1u << k;
+      }
+      quad_poisson(keys, fr, subap, pix0 >> 2, *tab, v, bm);
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+        if ((bm >> k) & 1u) v[k] = ptrs_pixel(keys, fr, subap, pix0 + k, v[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      if (k < np) out[i0 + k] = v[k];
   }
 }
 
@@ -92,8 +125,13 @@ cudaError_t launch_sample_noise(const float* lam, long long n, unsigned long lon
     cudaError_t e = pois_table_device(&tab);
     if (e != cudaSuccess) return e;
   }
-  const long long blocks = (n + 255) / 256 < 152 * 16 ? (n + 255) / 256 : 152 * 16;
-  sample_noise_kernel<<<(int)blocks, 256, 0, stream>>>(lam, n, seed, frame, kind, out, tab);
+  WfsArgs tmp;
+  memset(&tmp, 0, sizeof(tmp));
+  tmp.seed = seed;
+  set_philox_keys(tmp);
+  const long long nq = (n + 3) / 4;
+  const long long blocks = (nq + 255) / 256 < 152 * 16 ? (nq + 255) / 256 : 152 * 16;
+  sample_noise_kernel<<<(int)blocks, 256, 0, stream>>>(lam, n, tmp.philoxKeys, seed, frame, kind, out, tab);
   return cudaGetLastError();
 }
 

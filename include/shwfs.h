@@ -333,13 +333,15 @@ shwfs_status shwfs_set_split_event(shwfs_handle* h, void* event);
 
 /* Draws of the engine's counter-based noise for testing its samplers (no
  * reference counterpart; the reference draws through rk_poisson/gsl,
- * cmod/src/centmodule.c:722-784).  kind 2: out[i] ~ Poisson(lam[i]) by the
- * tabulated sampler every compute form uses (tables below lambda 64, PTRS
- * above); kind 1: out[i] ~ N(0, 1) (lam
- * unused); kind 0: out[i] ~ Poisson(lam[i]) by the table-free modal
- * inversion (an independent exact sampler, kept to cross-check kind 2).  Element i uses the stream of
- * (seed, frame, i).  lam and out are device pointers; with stream NULL the
- * call waits for the result. */
+ * cmod/src/centmodule.c:722-784).  Element i is drawn as the pipeline draws
+ * pixel i & 0xffff of subaperture i >> 16 in frame `frame`: kind 2 out[i] ~
+ * Poisson(lam[i]) by the tabulated sampler every compute form uses (the
+ * pixel's quad stream below lambda 64, PTRS from its own stream above);
+ * kind 1 out[i] ~ N(0, 1), the pixel's read-noise normal (lam unused);
+ * kind 0 out[i] ~ Poisson(lam[i]) by the table-free modal inversion from a
+ * stream of its own (an independent exact sampler, kept to cross-check
+ * kind 2).  lam and out are device pointers; with stream NULL the call waits
+ * for the result. */
 shwfs_status shwfs_sample_noise(int kind, const float* lam, int64_t n, uint64_t seed, uint64_t frame, float* out,
                                 void* stream);
 

@@ -86,3 +86,23 @@ def test_streams_depend_on_seed_and_frame():
     d = _draw(0, 9.7, 4096, seed=2, frame=0)
     assert np.array_equal(a, b)
     assert not np.array_equal(a, c) and not np.array_equal(a, d)
+
+
+def test_quad_draws_independent_within_a_quad():
+    """The four pixels of a quad share three Philox blocks (two Box-Muller
+    pairs, four alias words, four inversion uniforms): the cosine and sine
+    normals of one pair, and the Poisson draws of neighbouring pixels, are
+    uncorrelated."""
+    n = 1 << 21
+    g = _draw(1, 0.0, n).reshape(-1, 4)
+    for j, k in [(0, 1), (2, 3), (0, 2), (1, 3)]:
+        r = np.corrcoef(g[:, j], g[:, k])[0, 1]
+        assert abs(r) < 6 / np.sqrt(g.shape[0]), (j, k, r)
+    # the pair's squared radius -2 ln u1 is shared: its branches are
+    # independent only if g0^2 + g1^2 is Exp(1/2), which it is for exact pairs
+    r2 = g[:, 0] ** 2 + g[:, 1] ** 2
+    assert stats.kstest(r2 / 2, "expon").pvalue > 1e-6
+    p = _draw(2, 9.7, n).reshape(-1, 4)
+    for j, k in [(0, 1), (1, 2), (2, 3)]:
+        r = np.corrcoef(p[:, j], p[:, k])[0, 1]
+        assert abs(r) < 6 / np.sqrt(p.shape[0]), (j, k, r)
