@@ -159,6 +159,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   __shared__ Bars bars;
   __shared__ uint32_t s_tmem;
   __shared__ float s_tilt[256];
+  __shared__ int s_poff[256];  // pixel -> (row, column) offset in the phase frame
   __shared__ int s_abort;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int p = a.p, pp = p * p, ppr = (pp + 7) & ~7, mm = a.m * a.m;
@@ -173,7 +174,11 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   const int nseq = g.noc * g.nkc;
   const int K1B = g.K1 * ESZ;
 
-  for (int k = tid; k < pp; k += blockDim.x) s_tilt[k] = a.tilt[k];
+  for (int k = tid; k < pp; k += blockDim.x) {
+    s_tilt[k] = a.tilt[k];
+    const int ii = k / p;
+    s_poff[k] = ii * a.W + (k - ii * p);
+  }
   if (tid == 0) s_abort = 0;
   if (warp == 0) {
     tc::tmem_alloc<kTmemCols>(&s_tmem);
@@ -432,8 +437,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         for (int e = 0; e < 8; e += 2) {
           const int pix = pix0 + e;
           if (pix < pp) {
-            const int ii = pix / p, jj = pix - ii * p;  // jj even: the pair stays in the row
-            const float2 v2 = *reinterpret_cast<const float2*>(ph + (long long)ii * a.W + jj);
+            // the column is even: the pair stays in the row
+            const float2 v2 = *reinterpret_cast<const float2*>(ph + s_poff[pix]);
             phv[e] = v2.x;
             phv[e + 1] = v2.y;
           } else {
@@ -444,8 +449,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
 #pragma unroll
         for (int e = 0; e < 8; e++) {
           const int pix = pix0 + e;
-          const int ii = pix / p, jj = pix - ii * p;
-          phv[e] = (R.live && pix < pp) ? ph[(long long)ii * a.W + jj] : 0.f;
+          phv[e] = (R.live && pix < pp) ? ph[s_poff[pix]] : 0.f;
         }
       }
     };
