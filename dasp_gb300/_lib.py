@@ -108,7 +108,9 @@ class ShwfsInfo(ctypes.Structure):
                 ("nimg", ctypes.c_int), ("phasesize", ctypes.c_int), ("tile_subaps", ctypes.c_int),
                 ("smem_bytes", ctypes.c_int), ("grid_ctas", ctypes.c_int), ("noise_mode", ctypes.c_int),
                 ("cur_integ", ctypes.c_int), ("frames_read", ctypes.c_uint64), ("form", ctypes.c_int),
-                ("form_active", ctypes.c_int), ("host_io_direct", ctypes.c_int)]
+                ("form_active", ctypes.c_int), ("host_io_direct", ctypes.c_int),
+                ("gemm_kcb", ctypes.c_int), ("gemm_nw", ctypes.c_int), ("gemm_nk", ctypes.c_int),
+                ("gemm_dbuf", ctypes.c_int)]
 
 
 _lib = None

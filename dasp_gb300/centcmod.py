@@ -402,9 +402,12 @@ class centcmod:
         check(_lib.lib().shwfs_set_split_event(self.centstruct, ev), "set_split_event")
 
     def autotune(self) -> int:
-        """Time the FP32 kernel over the candidate CTA tile sizes on this
-        handle's own phase input and keep the fastest; returns the tile size
-        (subapertures per CTA).  Results do not depend on the tile size."""
+        """Time this handle's kernels over their launch shapes on its own
+        phase input and keep the fastest: the FP32 kernel's CTA tile size, or
+        for a tensor-core form the GEMM kernel's shared-memory staging
+        (``info()["gemm_kcb"/"gemm_nw"/"gemm_nk"/"gemm_dbuf"]``).  Returns
+        the FP32 tile size (subapertures per CTA).  Results do not depend on
+        either choice."""
         best = ctypes.c_int(0)
         check(_lib.lib().shwfs_autotune(self.centstruct, ctypes.byref(best)), "autotune")
         return best.value

@@ -65,6 +65,10 @@ __host__ __device__ inline GemmSmem gemm_smem_layout(const GemmGeom& g) {
 
 // fills the geometry for one operand format; false if it does not fit the kernel
 bool gemm_geometry(const GemmSpec& sp, int fmt, int passes, GemmGeom* g);
+// every staging that fits the kernel for this spec and format (W2 chunk
+// width, field / GEMM2-operand double buffering, Kc stages; the W2 ring as
+// deep as shared memory allows), gemm_geometry's choice first; empty if none
+std::vector<GemmGeom> gemm_geometry_candidates(const GemmSpec& sp, int fmt, int passes);
 int gemm_smem_bytes(const GemmGeom& g);
 void gemm_build_w2(const GemmSpec& sp, const GemmGeom& g, std::vector<uint8_t>& out);
 // dense [m^2][c^2] map from the cropped power spectrum to the binned image

@@ -741,12 +741,8 @@ bool gemm_active(const shwfs_handle* h) {
          h->noiseMode == SHWFS_NOISE_COUNTER;
 }
 
-shwfs_status build_gemm(shwfs_handle* h) {
-  h->gemmBuilt = false;
-  if (h->form == SHWFS_FORM_FP32) return SHWFS_OK;
-  GemmSpec sp;
-  GemmGeom g{};
-  if (!gemm_static_ok(h, &g, &sp)) return SHWFS_OK;  // falls back to the FP32 form
+// the W2 and Kc constants of geometry g, in its tensor-core staging order
+shwfs_status upload_gemm_consts(shwfs_handle* h, const GemmSpec& sp, const GemmGeom& g) {
   std::vector<uint8_t> w2, kc2;
   std::vector<double> kc;
   gemm_build_w2(sp, g, w2);
@@ -754,6 +750,16 @@ shwfs_status build_gemm(shwfs_handle* h) {
   gemm_build_kc(sp, g, kc, kc2);
   CK(h->d_w2.upload(w2.data(), w2.size()));
   CK(h->d_kc2.upload(kc2.data(), kc2.size()));
+  return SHWFS_OK;
+}
+
+shwfs_status build_gemm(shwfs_handle* h) {
+  h->gemmBuilt = false;
+  if (h->form == SHWFS_FORM_FP32) return SHWFS_OK;
+  GemmSpec sp;
+  GemmGeom g{};
+  if (!gemm_static_ok(h, &g, &sp)) return SHWFS_OK;  // falls back to the FP32 form
+  if (shwfs_status s = upload_gemm_consts(h, sp, g)) return s;
   if (g.fmt == kFmtFP16) {
     const int pp = h->phasesize * h->phasesize;
     std::vector<float> isc((size_t)h->nsubaps, 1.f);
@@ -1874,6 +1880,10 @@ shwfs_status shwfs_get_info(const shwfs_handle* h, shwfs_info* info) {
   info->form = h->form;
   info->form_active = gemm_active(h) ? h->form : SHWFS_FORM_FP32;
   info->host_io_direct = (h->centsDirect ? 1 : 0) | (h->bimgDirect ? 2 : 0) | (h->inDirect ? 4 : 0);
+  info->gemm_kcb = h->gemmBuilt ? h->gemm.KCB : 0;
+  info->gemm_nw = h->gemmBuilt ? h->gemm.NW : 0;
+  info->gemm_nk = h->gemmBuilt ? h->gemm.NK : 0;
+  info->gemm_dbuf = h->gemmBuilt ? (h->gemm.dbE ? 1 : 0) | (h->gemm.dbA2 ? 2 : 0) : 0;
   return SHWFS_OK;
 }
 
@@ -2085,12 +2095,19 @@ shwfs_status shwfs_set_split_event(shwfs_handle* h, void* event) {
   return SHWFS_OK;
 }
 
+shwfs_status autotune_gemm(shwfs_handle* h);
+
 shwfs_status shwfs_autotune(shwfs_handle* h, int* best_tile) {
   if (!h) return fail(SHWFS_ERR_INVALID, "null handle");
   g_err.clear();
   CK(cudaSetDevice(h->device));
-  if (h->lit.empty() || is_none(h->phs) || h->noiseMode == SHWFS_NOISE_REFERENCE || gemm_active(h)) {
-    // nothing to choose: no FP32 phase-input launches on this handle
+  if (!h->lit.empty() && !is_none(h->phs) && gemm_active(h)) {
+    shwfs_status s = autotune_gemm(h);
+    if (best_tile) *best_tile = h->TS;
+    return s;
+  }
+  if (h->lit.empty() || is_none(h->phs) || h->noiseMode == SHWFS_NOISE_REFERENCE) {
+    // nothing to choose: no phase-input launches on this handle
     if (best_tile) *best_tile = h->TS;
     return SHWFS_OK;
   }
@@ -2145,6 +2162,65 @@ shwfs_status shwfs_autotune(shwfs_handle* h, int* best_tile) {
   if (sp) return sp;
   if (best_tile) *best_tile = h->TS;
   return SHWFS_OK;
+}
+
+// tensor-core forms: time every staging of the GEMM kernel that fits
+// (gemm_geometry_candidates) on this handle's own phase and keep the fastest
+// with its constants.  The MMAs see the same k-steps in the same order
+// whatever the staging, so the results do not change.
+shwfs_status autotune_gemm(shwfs_handle* h) {
+  GemmSpec sp;
+  GemmGeom g0{};
+  if (!gemm_static_ok(h, &g0, &sp)) return SHWFS_OK;
+  const std::vector<GemmGeom> cands = gemm_geometry_candidates(sp, g0.fmt, g0.passes);
+  if (cands.size() < 2) return SHWFS_OK;
+  if (shwfs_status s = prepare_readout(h)) return s;
+  const int nlit = (int)h->lit.size();
+  const size_t mm = (size_t)h->nimg * h->nimg;
+  const int nf = (int)std::max<long long>(1, std::min<long long>(64, (16LL * 128 * h->numSMs + nlit - 1) / nlit));
+  DevBuf<float> ph, ce, bi;
+  const float* phs = (const float*)h->phs.data;
+  if (!h->phs.on_device) {
+    CK(ph.upload(phs, (size_t)numel(h->phs)));
+    phs = ph.p;
+  }
+  CK(ce.alloc((size_t)nf * h->nsubaps * 2));
+  CK(bi.alloc((size_t)nf * h->nsubaps * mm));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  const GemmGeom saved = h->gemm;
+  float bestMs = 1e30f;
+  size_t best = 0;
+  shwfs_status s = SHWFS_OK;
+  for (size_t c = 0; c < cands.size() && !s; c++) {
+    if ((s = upload_gemm_consts(h, sp, cands[c]))) break;
+    h->gemm = cands[c];
+    float ms = 0.f;
+    for (int rep = 0; rep < 2 && !s; rep++) {  // rep 0 warms up
+      if (cudaEventRecord(e0, h->stream) != cudaSuccess) s = fail(SHWFS_ERR_CUDA, "event record failed");
+      for (int k = 0; k < 3 && !s; k++) s = enqueue_readout(h, phs, ce.p, bi.p, nf, 0, h->stream);
+      if (!s && cudaEventRecord(e1, h->stream) != cudaSuccess) s = fail(SHWFS_ERR_CUDA, "event record failed");
+      if (!s && cudaEventSynchronize(e1) != cudaSuccess) s = fail(SHWFS_ERR_CUDA, "autotune launch failed");
+      if (!s) cudaEventElapsedTime(&ms, e0, e1);
+    }
+    if (!s && ms < bestMs) {
+      bestMs = ms;
+      best = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  const std::string err = g_err;
+  const GemmGeom keep = s ? saved : cands[best];
+  const shwfs_status su = upload_gemm_consts(h, sp, keep);
+  h->gemm = keep;
+  h->version++;
+  if (s) {
+    g_err = err;
+    return s;
+  }
+  return su;
 }
 
 }  // extern "C"

@@ -782,6 +782,38 @@ bool gemm_geometry(const GemmSpec& sp, int fmt, int passes, GemmGeom* g) {
   return false;
 }
 
+std::vector<GemmGeom> gemm_geometry_candidates(const GemmSpec& sp, int fmt, int passes) {
+  std::vector<GemmGeom> out;
+  GemmGeom g{};
+  if (!gemm_geometry(sp, fmt, passes, &g)) return out;
+  out.push_back(g);  // the default first
+  const int esz = fmt == kFmtTF32 ? 4 : 2;
+  const uint32_t limit = 227 * 1024 - 4096;
+  // the ranges gemm_geometry draws from: four k-steps per W2 chunk and two
+  // field buffers only for one-pass (16-bit) formats
+  for (int kcb = passes == 1 ? 128 : 64; kcb >= 64; kcb -= 64)
+    for (int db = (passes == 1 && esz == 2) ? 1 : 0; db >= 0; db--)
+      for (int da = 1; da >= 0; da--)
+        for (int nk = 2; nk >= 1; nk--) {
+          GemmGeom t = g;
+          t.KCB = kcb;
+          t.nkc = (t.K1 * esz + kcb - 1) / kcb;
+          t.dbE = db;
+          t.dbA2 = da;
+          t.NK = nk;
+          t.NW = 0;
+          const GemmSmem base = gemm_smem_layout(t);
+          if (base.total > limit) continue;
+          int nw = (int)((limit - base.total) / base.wStage);
+          if (nw > kGemmMaxNW) nw = kGemmMaxNW;
+          if (nw < (nk == 2 ? 3 : 2)) continue;
+          t.NW = nw;
+          if (t.KCB == g.KCB && t.dbE == g.dbE && t.dbA2 == g.dbA2 && t.NK == g.NK && t.NW == g.NW) continue;
+          out.push_back(t);
+        }
+  return out;
+}
+
 int gemm_smem_bytes(const GemmGeom& g) { return (int)gemm_smem_layout(g).total; }
 
 void gemm_build_w2(const GemmSpec& sp, const GemmGeom& g, std::vector<uint8_t>& out) {

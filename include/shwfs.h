@@ -221,6 +221,11 @@ typedef struct shwfs_info {
                            2 images written into the host arrays by the kernels,
                            4 input (phase or detector image) read from the host
                            array by the kernels */
+  int gemm_kcb;         /* tensor-core forms' staging: bytes of K per W2 chunk row, */
+  int gemm_nw;          /* W2 ring stages, */
+  int gemm_nk;          /* Kc ring stages, */
+  int gemm_dbuf;        /* 1: two field buffers, 2: two |F|^2 buffers (OR); all 0
+                           when no tensor-core form is built */
 } shwfs_info;
 
 typedef struct shwfs_handle shwfs_handle;
@@ -319,9 +324,14 @@ shwfs_status shwfs_batch_create(shwfs_handle* const* handles, int n, shwfs_batch
 shwfs_status shwfs_batch_run(shwfs_batch* b, void* stream);
 shwfs_status shwfs_batch_free(shwfs_batch* b);
 
-/* Time the fused FP32 kernel over the candidate tile sizes on scratch
- * buffers and keep the fastest for this handle (results are unchanged: the
- * tile size only changes how subapertures are grouped per CTA). */
+/* Time the handle's phase-input kernels over their launch shapes on scratch
+ * buffers and keep the fastest: for the FP32 form the candidate tile sizes
+ * of the fused kernel (*best_tile receives the one kept); for a tensor-core
+ * form every shared-memory staging of the GEMM kernel that fits (W2 chunk
+ * width, double buffering of the field and |F|^2 operands, Kc stages, W2
+ * ring depth; shwfs_info.gemm_* report the one kept).  Results are
+ * unchanged: the tile size only groups subapertures per CTA, and the MMAs
+ * see the same k-steps in the same order whatever the staging. */
 shwfs_status shwfs_autotune(shwfs_handle* h, int* best_tile);
 
 /* Timing aid (no reference counterpart): with a non-NULL CUDA event, every

@@ -139,3 +139,25 @@ def test_autotune_keeps_results():
         base.run_alone()
         tuned.run_alone()
     _same([base.outputs()], [tuned.outputs()])
+
+
+@pytest.mark.parametrize("form", ["fp16", "bf16x3", "tf32"])
+def test_autotune_gemm_staging_keeps_results(form):
+    """The tensor-core forms' autotuner times every shared-memory staging of
+    the GEMM kernel and keeps one; the MMAs see the same k-steps in the same
+    order, so the outputs stay bit-identical to the default staging."""
+    kw = dict(nsubx=16, p=10, N=20, C=20, m=10, psf="gauss", **NOISY)
+    base = DevEngine(Case(**kw), form)
+    tuned = DevEngine(Case(**kw), form)
+    d = base.eng.info()
+    assert d["form_active"] != 0 and d["gemm_kcb"] in (64, 128)
+    tuned.eng.autotune()
+    t = tuned.eng.info()
+    assert t["gemm_kcb"] in (64, 128) and t["gemm_nw"] >= 2 and t["gemm_nk"] in (1, 2) and 0 <= t["gemm_dbuf"] <= 3
+    assert t["frames_read"] == 0
+    for k in range(2):
+        if k:
+            _new_phase([(base, tuned)], 40)
+        base.run_alone()
+        tuned.run_alone()
+        _same([base.outputs()], [tuned.outputs()])
