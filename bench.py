@@ -1035,13 +1035,12 @@ def main():
         eng.set_form(form)
         if eng.info()["form_active"] != FORM_CODES[form]:
             return None
-        staging = None
-        if form != "fp32":
-            # the engine's own autotuner picks the GEMM kernel's shared-memory
-            # staging on this handle's phase (results do not depend on it)
-            eng.autotune()
-            inf = eng.info()
-            staging = {k: inf["gemm_" + k] for k in ("kcb", "nw", "nk", "dbuf")}
+        # the engine's own autotuner picks the launch shape on this handle's
+        # phase (results do not depend on it): the FP32 kernel's tile size,
+        # the GEMM kernel's shared-memory staging
+        ts = eng.autotune()
+        inf = eng.info()
+        staging = {k: inf["gemm_" + k] for k in ("kcb", "nw", "nk", "dbuf")} if form != "fp32" else {"tile": ts}
         with torch.cuda.stream(stream):
             for k in range(args.warmup):
                 eng.run_batch(batches[k % 2], dc, db, stream=stream)
@@ -1079,8 +1078,7 @@ def main():
         if split:
             out["formation_ms"] = float(np.mean([a.elapsed_time(m_) for (a, _), m_ in zip(ev, mid)]))
             out["post_ms"] = float(np.mean([m_.elapsed_time(b) for (_, b), m_ in zip(ev, mid)]))
-        if staging:
-            out["gemm_staging"] = staging
+        out["tuned"] = staging
         return out
 
     with ClockSampler(local) as clk:
@@ -1190,8 +1188,7 @@ def main():
         if r:
             form_report[f] = {"value": r["value"], "ms_per_step": r["ms_per_step"],
                               "kernel_ms_per_launch": r["per_launch_ms"], **rooflines(f, r)}
-            if "gemm_staging" in r:
-                form_report[f]["gemm_staging"] = r["gemm_staging"]
+            form_report[f]["tuned"] = r["tuned"]
     if rank != 0:
         eng.free()
         return
