@@ -132,23 +132,28 @@ def test_argument_checks():
     eng2.free()
 
 
+@pytest.mark.parametrize("geom", [dict(nsubx=8, p=8, N=16), dict(nsubx=8, p=8, N=16, C=16, m=5),
+                                  dict(nsubx=6, p=8, N=24, C=24, m=6)])
 @pytest.mark.parametrize("sig", [2e3, 1e6])
 @pytest.mark.parametrize("extra", [dict(), dict(parabolicFit=1)])
-def test_counter_draws_identical_in_every_noise_kernel(sig, extra):
+def test_counter_draws_identical_in_every_noise_kernel(sig, extra, geom):
     """The fused FP32 kernel (noise drawn on its own images), the warp noise
     kernel (run_prenoise, window CoG) and the general noise kernel
     (run_prenoise with a parabolic fit) draw each quad of pixels from one
     stream: on equal pre-noise images their noisy images are equal bit for
     bit.  sig 1e6 puts most pixels above lambda 64, so the rejection
-    sampler's queue fills and drains inside a chunk."""
-    kw = dict(nsubx=8, p=8, N=16, sig=sig, addPoisson=1, readnoise=2.0, readbg=1.5, noiseFloor=-1e9,
-              threshType=1, seed=9)
+    sampler's queue fills and drains inside a chunk; nimg 5 (25 pixels)
+    ends every image on a partial quad, nimg 6 (36) on whole quads that
+    straddle image rows."""
+    kw = dict(sig=sig, addPoisson=1, readnoise=2.0, readbg=1.5, noiseFloor=-1e9, threshType=1, seed=9)
+    kw.update(geom)
     kw.update(extra)
     quiet = Case(**dict(kw, addPoisson=0, readnoise=0.0, readbg=0.0))
+    n, m = quiet.nsubaps, quiet.m
     qe = quiet.engine()
     qe.set_form("fp32")
     qe.run(0)
-    lam = quiet.bimg.reshape(64, 8, 8).copy()
+    lam = quiet.bimg.reshape(n, m, m).copy()
     qe.free()
     lit = quiet.lit()
     if sig > 1e5:
@@ -161,8 +166,8 @@ def test_counter_draws_identical_in_every_noise_kernel(sig, extra):
     for f in range(3):
         fe.run(0)
         pe.run_prenoise(lam)
-        a = fused.bimg.reshape(64, -1)[lit]
-        b = post.bimg.reshape(64, -1)[lit]
+        a = fused.bimg.reshape(n, -1)[lit]
+        b = post.bimg.reshape(n, -1)[lit]
         np.testing.assert_array_equal(a, b, err_msg="frame %d" % f)
         assert np.abs(fused.cents - post.cents).max() <= 1e-4
     fe.free()
