@@ -251,6 +251,14 @@ def test_unlit_image_only_gets_noise_and_no_cents():
 
 
 def test_reference_stream_noise_matches_oracle():
+    """Reference-stream noise on images the engine forms itself: its
+    pre-noise means differ from the oracle's float restatement in the last
+    bits, and a mean that moves across a step of the Poisson inversion (or
+    the PTRS acceptance test) changes that pixel's draw and, through the
+    shared PCG32 stream, the later draws of its worker thread.  So a small
+    share of pixels may differ here; the exact reproduction -- every pixel,
+    centroids within 1e-5 px -- is tested on the reference module's own
+    pre-noise images (test_prenoise_gpu.py)."""
     c = Case(nsubx=16, p=8, N=16, sig=3e3, addPoisson=1, readnoise=3.0, skybrightness=10.0, noiseFloor=6.0,
              nthreads=5, seed=17)
     eng = c.engine()
