@@ -1040,7 +1040,7 @@ def main():
         # the GEMM kernel's shared-memory staging
         ts = eng.autotune()
         inf = eng.info()
-        staging = {k: inf["gemm_" + k] for k in ("kcb", "nw", "nk", "dbuf")} if form != "fp32" else {"tile": ts}
+        staging = {k: inf["gemm_" + k] for k in ("cw", "kcb", "nw", "nk", "dbuf")} if form != "fp32" else {"tile": ts}
         with torch.cuda.stream(stream):
             for k in range(args.warmup):
                 eng.run_batch(batches[k % 2], dc, db, stream=stream)

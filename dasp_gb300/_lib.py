@@ -110,7 +110,8 @@ class ShwfsInfo(ctypes.Structure):
                 ("cur_integ", ctypes.c_int), ("frames_read", ctypes.c_uint64), ("form", ctypes.c_int),
                 ("form_active", ctypes.c_int), ("host_io_direct", ctypes.c_int),
                 ("gemm_kcb", ctypes.c_int), ("gemm_nw", ctypes.c_int), ("gemm_nk", ctypes.c_int),
-                ("gemm_dbuf", ctypes.c_int)]
+                ("gemm_dbuf", ctypes.c_int), ("gemm_cw", ctypes.c_int), ("gemm_staging", ctypes.c_int),
+                ("gemm_candidates", ctypes.c_int)]
 
 
 _lib = None

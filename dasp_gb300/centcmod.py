@@ -54,9 +54,10 @@ HOSTIO_OUTPUTS = 1  # kernels write cents / final images into the pinned host ar
 HOSTIO_PHASE = 2  # image-formation kernels read the pinned host phase directly
 INTEGMODE = 104  # extension: integration mode (INTEGMODES below)
 INTEGMODES = {"compat": 0, "physical": 1}
+GEMMSTAGING = 105  # extension: tensor-core forms' GEMM staging index (info()["gemm_candidates"] of them)
 
 _INT_CODES = {CALSOURCE, ADDPOISSON, NCEN, NTHREADS, OPTICALBINNING, CORRELATIONCENTROIDING, INTEGSTEPS,
-              NOISEMODE, TILESUBAPS, FORM, INTEGMODE}
+              NOISEMODE, TILESUBAPS, FORM, INTEGMODE, GEMMSTAGING}
 _INT_ARRAY_CODES = {USEBRIGHTEST}
 
 

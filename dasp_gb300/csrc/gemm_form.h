@@ -29,16 +29,26 @@ struct GemmGeom {
   int K1;      // GEMM1 K in elements: [Re E | Im E], each p^2 rounded up to 8, total rounded up to 16
   int KCB;     // GEMM1 K bytes per row of one streamed W2 chunk (multiple of 32)
   int nkc;     // W2 chunks per output chunk
-  int noc;     // output chunks of 64 complex outputs (GEMM1 N = 128 columns each)
+  int CW;      // complex outputs per GEMM1 output chunk (GEMM1 N = 2 CW columns; 64, or a wider
+               // multiple of 16 that needs fewer chunks for the c x c crop)
+  int noc;     // output chunks of CW complex outputs
   int N2;      // GEMM2 N: nimg^2 rounded up to 16
   int NW, NK;  // ring stages for W2 and Kc chunks
   int dbE;     // 1: two field (GEMM1 A operand) buffers, the next tile's built during this one
   int dbA2;    // 1: two |F|^2 (GEMM2 A operand) buffers, alternating between output chunks
-  int nd1;     // D1 (GEMM1 accumulator) buffers in TMEM: 3 when N2 <= 128, else 2
+  int nd1;     // D1 (GEMM1 accumulator) buffers in TMEM: 3 when N2 <= 128 and CW == 64, else 2
   const uint8_t* w2;   // [noc][nkc] x {hi[, lo]} x [128 x KCB bytes], tensor-core smem order
   const uint8_t* kc2;  // [noc] x {hi[, lo]} x [N2 x 64 elements], tensor-core smem order
   const float* pupT;   // pupil by pixel group: [ppr/8][nlit][8], lit order
 };
+
+// TMEM columns of D1 buffer b and of D2: three 128-column D1 buffers around
+// D2 at 256 when nd1 == 3 (CW 64, N2 <= 128), else D1 at 0 and 2 CW and D2
+// after them (4 CW + N2 <= 512)
+__host__ __device__ inline uint32_t gemm_d1_col(const GemmGeom& g, int b) {
+  return (g.nd1 == 3 && b == 2) ? 384u : (uint32_t)(b * 2 * g.CW);
+}
+__host__ __device__ inline uint32_t gemm_d2_col(const GemmGeom& g) { return g.nd1 == 3 ? 256u : (uint32_t)(4 * g.CW); }
 
 // dynamic shared-memory layout (byte offsets)
 struct GemmSmem {
@@ -50,10 +60,10 @@ __host__ __device__ inline GemmSmem gemm_smem_layout(const GemmGeom& g) {
   GemmSmem L;
   const uint32_t esz = g.fmt == kFmtTF32 ? 4u : 2u, hl = g.passes == 3 ? 2u : 1u;
   L.a1Half = 128u * (uint32_t)g.K1 * esz;
-  L.a2Half = 128u * 64u * esz;
-  L.wHalf = 128u * (uint32_t)g.KCB;
+  L.a2Half = 128u * (uint32_t)g.CW * esz;
+  L.wHalf = 2u * (uint32_t)g.CW * (uint32_t)g.KCB;
   L.wStage = L.wHalf * hl;
-  L.kHalf = (uint32_t)g.N2 * 64u * esz;
+  L.kHalf = (uint32_t)g.N2 * (uint32_t)g.CW * esz;
   L.kStage = L.kHalf * hl;
   L.a1 = 0;
   L.a2 = (L.a1 + L.a1Half * hl * (g.dbE ? 2u : 1u) + 1023u) & ~1023u;

@@ -172,6 +172,8 @@ struct shwfs_handle {
   int form = SHWFS_FORM_FP32;
   bool gemmBuilt = false;
   GemmGeom gemm{};
+  int gemmStaging = 0;     // SHWFS_GEMMSTAGING: index into gemm_geometry_candidates
+  int gemmCandidates = 0;  // their number for the built geometry
   DevBuf<uint8_t> d_w2, d_kc2;
   DevBuf<float> d_iscale;  // fp16 form: 1 / (sum of the subaperture's pupil)^2
   DevBuf<float> d_pupT;    // tensor-core forms: pupil by pixel group [ppr/8][nlit][8]
@@ -755,10 +757,18 @@ shwfs_status upload_gemm_consts(shwfs_handle* h, const GemmSpec& sp, const GemmG
 
 shwfs_status build_gemm(shwfs_handle* h) {
   h->gemmBuilt = false;
+  h->gemmCandidates = 0;
   if (h->form == SHWFS_FORM_FP32) return SHWFS_OK;
   GemmSpec sp;
   GemmGeom g{};
   if (!gemm_static_ok(h, &g, &sp)) return SHWFS_OK;  // falls back to the FP32 form
+  {
+    // the staging chosen by SHWFS_GEMMSTAGING (or the autotuner)
+    const std::vector<GemmGeom> cands = gemm_geometry_candidates(sp, g.fmt, g.passes);
+    h->gemmCandidates = (int)cands.size();
+    if (h->gemmStaging < 0 || h->gemmStaging >= (int)cands.size()) h->gemmStaging = 0;
+    if (!cands.empty()) g = cands[h->gemmStaging];
+  }
   if (shwfs_status s = upload_gemm_consts(h, sp, g)) return s;
   if (g.fmt == kFmtFP16) {
     const int pp = h->phasesize * h->phasesize;
@@ -1675,6 +1685,7 @@ shwfs_status shwfs_update(shwfs_handle* h, int code, const shwfs_value* v) {
       if ((s = set_spot_psf(h, v->kind == SHWFS_VAL_ARRAY ? v->arr[0] : none))) return s;
       if ((s = update_totsig(h))) return s;
       if ((s = plan(h))) return s;
+      h->gemmStaging = 0;
       return build_gemm(h);
     }
     case SHWFS_NTHREADS:
@@ -1792,6 +1803,14 @@ shwfs_status shwfs_update(shwfs_handle* h, int code, const shwfs_value* v) {
       if (v->ival < SHWFS_FORM_FP32 || v->ival > SHWFS_FORM_TF32)
         return fail(SHWFS_ERR_INVALID, "unknown compute form %lld", (long long)v->ival);
       h->form = (int)v->ival;
+      h->gemmStaging = 0;
+      return build_gemm(h);
+    case SHWFS_GEMMSTAGING:
+      if ((s = need(SHWFS_VAL_INT, "int"))) return s;
+      if (v->ival < 0 || (h->gemmCandidates > 0 && v->ival >= h->gemmCandidates))
+        return fail(SHWFS_ERR_INVALID, "staging index %lld outside [0, %d)", (long long)v->ival,
+                    h->gemmCandidates);
+      h->gemmStaging = (int)v->ival;
       return build_gemm(h);
     case SHWFS_TILESUBAPS:
       if ((s = need(SHWFS_VAL_INT, "int"))) return s;
@@ -1884,6 +1903,9 @@ shwfs_status shwfs_get_info(const shwfs_handle* h, shwfs_info* info) {
   info->gemm_nw = h->gemmBuilt ? h->gemm.NW : 0;
   info->gemm_nk = h->gemmBuilt ? h->gemm.NK : 0;
   info->gemm_dbuf = h->gemmBuilt ? (h->gemm.dbE ? 1 : 0) | (h->gemm.dbA2 ? 2 : 0) : 0;
+  info->gemm_cw = h->gemmBuilt ? h->gemm.CW : 0;
+  info->gemm_staging = h->gemmBuilt ? h->gemmStaging : 0;
+  info->gemm_candidates = h->gemmBuilt ? h->gemmCandidates : 0;
   return SHWFS_OK;
 }
 
@@ -2213,6 +2235,7 @@ shwfs_status autotune_gemm(shwfs_handle* h) {
   cudaEventDestroy(e1);
   const std::string err = g_err;
   const GemmGeom keep = s ? saved : cands[best];
+  if (!s) h->gemmStaging = (int)best;
   const shwfs_status su = upload_gemm_consts(h, sp, keep);
   h->gemm = keep;
   h->version++;

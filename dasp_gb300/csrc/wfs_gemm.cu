@@ -72,7 +72,6 @@ constexpr uint32_t kLBO = 128;  // bytes between core matrices along K
 
 // TMEM columns: D1 buffers 0 and 1 at 0 and 128, D2 at 256 (N2 <= 256
 // columns), a third D1 buffer at 384 when N2 <= 128
-__device__ __forceinline__ uint32_t d1_col(int b) { return b == 2 ? 384u : (uint32_t)b * 128u; }
 
 // ---- element encodings (device) ----
 template <int FMT>
@@ -170,7 +169,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   uint8_t* A2lo = A2hi + L.a2Half;
   const uint32_t sboE = (uint32_t)(g.K1 * ESZ / 16) * 128;
   const uint32_t sboW = (uint32_t)(g.KCB / 16) * 128;
-  const uint32_t sbo2 = (uint32_t)(64 * ESZ / 16) * 128;
+  const uint32_t sbo2 = (uint32_t)(g.CW * ESZ / 16) * 128;
+  const uint32_t d2c = gemm_d2_col(g);
   const int nseq = g.noc * g.nkc;
   const int K1B = g.K1 * ESZ;
 
@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     // output chunk gC goes to D1 buffer d1b in round d1r.
     if (myTiles > 0) {
       const bool leader = lane == 0;
-      constexpr uint32_t idesc1 = tc::idesc_f32acc(FMT, 128, 128);
+      const uint32_t idesc1 = tc::idesc_f32acc(FMT, 128, 2 * g.CW);
       const uint32_t wbase = tc::smem_addr(smem + L.w);
       // descriptors: the 14-bit start-address field (bits 0-13, in 16-byte
       // units) advances by 16 per k-step of 256 bytes; all addresses < 256 KB
@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         for (int oc = 0; oc < g.noc; oc++) {
           if (d1r > 0) wait(&bars.d1free[d1b], (d1r - 1) & 1);
           tc::fence_after_sync();
-          const uint32_t dcol = tmem + d1_col(d1b);
+          const uint32_t dcol = tmem + gemm_d1_col(g, d1b);
           int ks = 0;
           for (int kc = 0; kc < g.nkc; kc++) {
             wait(&bars.wfull[cs], cph);
@@ -343,7 +343,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       uint32_t gK = 0;
       const uint64_t dK0 = tc::smem_desc(kbase, kLBO, sbo2);
       const uint64_t dKstage = (uint64_t)(L.kStage >> 4), dKlo = (uint64_t)(L.kHalf >> 4);
-      const uint32_t dcol = tmem + 256;
+      const uint32_t dcol = tmem + d2c;
+      const int ks2 = g.CW * ESZ / 32;  // k-steps of one chunk
       int ksg = 0;
       uint32_t kph = 0;
       for (int lt = 0; lt < myTiles; lt++) {
@@ -356,7 +357,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
           tc::fence_after_sync();
           const uint64_t dKh = dK0 + (uint64_t)ksg * dKstage;
           if (leader) {
-            for (int ks = 0; ks < 2 * ESZ; ks++) {
+            for (int ks = 0; ks < ks2; ks++) {
               const uint64_t o = (uint64_t)ks * 16;
               const uint32_t acc0 = (oc > 0 || ks > 0) ? 1u : 0u;
               tc::mma<FMT>(dcol, dAh + o, dKh + o, idesc2, acc0);
@@ -558,7 +559,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         const float* skyA = a.skyArr ? a.skyArr + (long long)i * mm : nullptr;
         for (int cb = h * 32; cb < mm; cb += 64) {
           uint32_t v[32];
-          tc::tmem_ld32(tmem + 256 + lanebase + cb, v);
+          tc::tmem_ld32(tmem + d2c + lanebase + cb, v);
           tc::tmem_ld_wait();
           if (!P.live) continue;
           const int n = min(32, mm - cb);
@@ -585,49 +586,71 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         if (lane == 0) tc::mbar_arrive(&bars.d2free);
       };
 
-      // one output chunk of the current tile: |F|^2 of the 32 complex
-      // outputs in columns 64h .. 64h+63 of this row -> the GEMM2 operand
+      // one output chunk of the current tile: |F|^2 of the CW/2 complex
+      // outputs in columns h CW .. h CW + CW - 1 of this row -> the GEMM2
+      // operand (K h CW/2 .. h CW/2 + CW/2 - 1)
       auto chunk = [&](float isc) {
         wait(&bars.d1full[d1b], d1r & 1);
         tc::fence_after_sync();
-        float I[32];
-        {
-          // both halves in flight before one wait
-          uint32_t v0[32], v1[32];
-          const uint32_t col = tmem + d1_col(d1b) + lanebase + h * 64;
-          tc::tmem_ld32(col, v0);
-          tc::tmem_ld32(col + 32, v1);
-          tc::tmem_ld_wait();
-#pragma unroll
-          for (int e = 0; e < 16; e++) {
-            I[e] = (__uint_as_float(v0[2 * e]) * __uint_as_float(v0[2 * e]) +
-                    __uint_as_float(v0[2 * e + 1]) * __uint_as_float(v0[2 * e + 1])) * isc;
-            I[16 + e] = (__uint_as_float(v1[2 * e]) * __uint_as_float(v1[2 * e]) +
-                         __uint_as_float(v1[2 * e + 1]) * __uint_as_float(v1[2 * e + 1])) * isc;
+        const uint32_t col = tmem + gemm_d1_col(g, d1b) + lanebase + h * g.CW;
+        // A2 buffer of this chunk
+        const uint32_t ab = g.dbA2 ? (gA & 1) : 0;
+        uint8_t* Ahi = A2hi + (size_t)ab * L.a2Half * (SPLIT ? 2 : 1);
+        uint8_t* Alo = Ahi + L.a2Half;
+        auto a2_wait = [&]() {
+          // A2 is free once the previous chunk's GEMM2 has completed
+          if (g.dbA2) {
+            if (gA >= 2) wait(&bars.a2free[ab], ((gA >> 1) - 1) & 1);
+          } else if (gA >= 1) {
+            wait(&bars.a2free[0], (gA - 1) & 1);
           }
+        };
+        if (g.CW == 64) {
+          float I[32];
+          {
+            // both halves in flight before one wait
+            uint32_t v0[32], v1[32];
+            tc::tmem_ld32(col, v0);
+            tc::tmem_ld32(col + 32, v1);
+            tc::tmem_ld_wait();
+#pragma unroll
+            for (int e = 0; e < 16; e++) {
+              I[e] = (__uint_as_float(v0[2 * e]) * __uint_as_float(v0[2 * e]) +
+                      __uint_as_float(v0[2 * e + 1]) * __uint_as_float(v0[2 * e + 1])) * isc;
+              I[16 + e] = (__uint_as_float(v1[2 * e]) * __uint_as_float(v1[2 * e]) +
+                           __uint_as_float(v1[2 * e + 1]) * __uint_as_float(v1[2 * e + 1])) * isc;
+            }
+          }
+          tc::fence_before_sync();
+          __syncwarp();
+          if (lane == 0) tc::mbar_arrive(&bars.d1free[d1b]);
+          a2_wait();
+#pragma unroll
+          for (int k8 = 0; k8 < 4; k8++) {
+            float x8[8];
+#pragma unroll
+            for (int e = 0; e < 8; e++) x8[e] = I[k8 * 8 + e];
+            store8<FMT, SPLIT>(Ahi, Alo, kmaj(r, h * 32 + k8 * 8, ESZ, sbo2), x8);
+          }
+        } else {
+          // wider chunks: 16 columns (8 complex outputs) at a time, each
+          // stored as soon as it is computed
+          a2_wait();
+          for (int u = 0; u < g.CW; u += 16) {
+            float v16[16];
+            tc::tmem_ld16_sync(col + u, v16);
+            float x8[8];
+#pragma unroll
+            for (int e = 0; e < 8; e++) x8[e] = (v16[2 * e] * v16[2 * e] + v16[2 * e + 1] * v16[2 * e + 1]) * isc;
+            store8<FMT, SPLIT>(Ahi, Alo, kmaj(r, h * (g.CW / 2) + u / 2, ESZ, sbo2), x8);
+          }
+          tc::fence_before_sync();
+          __syncwarp();
+          if (lane == 0) tc::mbar_arrive(&bars.d1free[d1b]);
         }
-        tc::fence_before_sync();
-        __syncwarp();
-        if (lane == 0) tc::mbar_arrive(&bars.d1free[d1b]);
         if (++d1b == g.nd1) {
           d1b = 0;
           d1r++;
-        }
-        // A2 is free once the previous chunk's GEMM2 has completed
-        const uint32_t ab = g.dbA2 ? (gA & 1) : 0;
-        if (g.dbA2) {
-          if (gA >= 2) wait(&bars.a2free[ab], ((gA >> 1) - 1) & 1);
-        } else if (gA >= 1) {
-          wait(&bars.a2free[0], (gA - 1) & 1);
-        }
-        uint8_t* Ahi = A2hi + (size_t)ab * L.a2Half * (SPLIT ? 2 : 1);
-        uint8_t* Alo = Ahi + L.a2Half;
-#pragma unroll
-        for (int k8 = 0; k8 < 4; k8++) {
-          float x8[8];
-#pragma unroll
-          for (int e = 0; e < 8; e++) x8[e] = I[k8 * 8 + e];
-          store8<FMT, SPLIT>(Ahi, Alo, kmaj(r, h * 32 + k8 * 8, ESZ, sbo2), x8);
         }
         tc::fence_async_smem();
         __syncwarp();
@@ -746,6 +769,7 @@ bool gemm_geometry(const GemmSpec& sp, int fmt, int passes, GemmGeom* g) {
   g->passes = passes;
   g->K1 = K1;
   g->N2 = N2;
+  g->CW = 64;
   g->nd1 = N2 <= 128 ? 3 : 2;
   g->noc = (sp.c * sp.c + 63) / 64;
   // dynamic limit: 227 KB minus the kernel's static shared memory (< 2 KB)
@@ -784,33 +808,53 @@ bool gemm_geometry(const GemmSpec& sp, int fmt, int passes, GemmGeom* g) {
 
 std::vector<GemmGeom> gemm_geometry_candidates(const GemmSpec& sp, int fmt, int passes) {
   std::vector<GemmGeom> out;
-  GemmGeom g{};
-  if (!gemm_geometry(sp, fmt, passes, &g)) return out;
-  out.push_back(g);  // the default first
+  GemmGeom g0{};
+  if (!gemm_geometry(sp, fmt, passes, &g0)) return out;
+  out.push_back(g0);  // the default first
   const int esz = fmt == kFmtTF32 ? 4 : 2;
   const uint32_t limit = 227 * 1024 - 4096;
-  // the ranges gemm_geometry draws from: four k-steps per W2 chunk and two
-  // field buffers only for one-pass (16-bit) formats
-  for (int kcb = passes == 1 ? 128 : 64; kcb >= 64; kcb -= 64)
-    for (int db = (passes == 1 && esz == 2) ? 1 : 0; db >= 0; db--)
-      for (int da = 1; da >= 0; da--)
-        for (int nk = 2; nk >= 1; nk--) {
-          GemmGeom t = g;
-          t.KCB = kcb;
-          t.nkc = (t.K1 * esz + kcb - 1) / kcb;
-          t.dbE = db;
-          t.dbA2 = da;
-          t.NK = nk;
-          t.NW = 0;
-          const GemmSmem base = gemm_smem_layout(t);
-          if (base.total > limit) continue;
-          int nw = (int)((limit - base.total) / base.wStage);
-          if (nw > kGemmMaxNW) nw = kGemmMaxNW;
-          if (nw < (nk == 2 ? 3 : 2)) continue;
-          t.NW = nw;
-          if (t.KCB == g.KCB && t.dbE == g.dbE && t.dbA2 == g.dbA2 && t.NK == g.NK && t.NW == g.NW) continue;
-          out.push_back(t);
-        }
+  // chunk widths: 64 complex outputs, and for each smaller chunk count the
+  // narrowest multiple of 16 that covers the crop in that many chunks, when
+  // two D1 buffers and D2 fit the 512 TMEM columns (GEMM1 N = 2 CW <= 256)
+  const int cc = sp.c * sp.c;
+  std::vector<int> widths = {64};
+  for (int k = (cc + 127) / 128; k < (cc + 63) / 64; k++) {
+    const int cw = 16 * ((cc + 16 * k - 1) / (16 * k));
+    if (cw <= 64 || 2 * cw > 256 || 4 * cw + g0.N2 > 512) continue;
+    bool dup = false;
+    for (int w : widths) dup = dup || w == cw;
+    if (!dup) widths.push_back(cw);
+  }
+  for (int cw : widths) {
+    GemmGeom g = g0;
+    g.CW = cw;
+    g.noc = (cc + cw - 1) / cw;
+    g.nd1 = (cw == 64 && g.N2 <= 128) ? 3 : 2;
+    // the ranges gemm_geometry draws from: four k-steps per W2 chunk and two
+    // field buffers only for one-pass (16-bit) formats
+    for (int kcb = passes == 1 ? 128 : 64; kcb >= 64; kcb -= 64)
+      for (int db = (passes == 1 && esz == 2) ? 1 : 0; db >= 0; db--)
+        for (int da = 1; da >= 0; da--)
+          for (int nk = 2; nk >= 1; nk--) {
+            GemmGeom t = g;
+            t.KCB = kcb;
+            t.nkc = (t.K1 * esz + kcb - 1) / kcb;
+            t.dbE = db;
+            t.dbA2 = da;
+            t.NK = nk;
+            t.NW = 0;
+            const GemmSmem base = gemm_smem_layout(t);
+            if (base.total > limit) continue;
+            int nw = (int)((limit - base.total) / base.wStage);
+            if (nw > kGemmMaxNW) nw = kGemmMaxNW;
+            if (nw < (nk == 2 ? 3 : 2)) continue;
+            t.NW = nw;
+            if (t.CW == g0.CW && t.KCB == g0.KCB && t.dbE == g0.dbE && t.dbA2 == g0.dbA2 && t.NK == g0.NK &&
+                t.NW == g0.NW)
+              continue;
+            out.push_back(t);
+          }
+  }
   return out;
 }
 
@@ -825,8 +869,8 @@ void gemm_build_w2(const GemmSpec& sp, const GemmGeom& g, std::vector<uint8_t>& 
   const uint32_t sbo = (uint32_t)(g.KCB / 16) * 128;
   const int kce = g.KCB / esz;  // elements per chunk row
   for (int oc = 0; oc < g.noc; oc++)
-    for (int ol = 0; ol < 64; ol++) {
-      const int o = oc * 64 + ol;
+    for (int ol = 0; ol < g.CW; ol++) {
+      const int o = oc * g.CW + ol;
       if (o >= c * c) continue;
       const int ku = sp.ro + o / c, kv = sp.ro + o % c;
       for (int k = 0; k < 2 * ppr; k++) {
@@ -936,14 +980,14 @@ void gemm_build_kc(const GemmSpec& sp, const GemmGeom& g, const std::vector<doub
   const int esz = g.fmt == kFmtTF32 ? 4 : 2;
   const bool split = g.passes == 3;
   const GemmSmem L = gemm_smem_layout(g);
-  const uint32_t sbo = (uint32_t)(64 * esz / 16) * 128;
+  const uint32_t sbo = (uint32_t)(g.CW * esz / 16) * 128;
   out.assign((size_t)g.noc * L.kStage, 0);
   for (int oc = 0; oc < g.noc; oc++) {
     uint8_t* hi = out.data() + (size_t)oc * L.kStage;
     uint8_t* lo = hi + L.kHalf;
     for (int q = 0; q < mm; q++)
-      for (int ol = 0; ol < 64; ol++) {
-        const int o = oc * 64 + ol;
+      for (int ol = 0; ol < g.CW; ol++) {
+        const int o = oc * g.CW + ol;
         if (o >= cc) continue;
         put_val(g.fmt, split, hi, lo, kmaj(q, ol, esz, sbo), kc[(size_t)q * cc + o]);
       }

@@ -75,7 +75,13 @@ enum {
   SHWFS_HOSTIO = 103,
   /* extension: how sub-exposures (nintegrations > 1) form the image, ival =
    * SHWFS_INTEG_COMPAT (default) or SHWFS_INTEG_PHYSICAL */
-  SHWFS_INTEGMODE = 104
+  SHWFS_INTEGMODE = 104,
+  /* extension: the tensor-core forms' GEMM staging, ival = an index into the
+   * stagings that fit the handle's geometry (0 = the default choice;
+   * shwfs_info.gemm_candidates gives their number); shwfs_autotune sets it
+   * to the fastest.  Results do not depend on it.  Reset to 0 when the form
+   * or the spot PSF changes. */
+  SHWFS_GEMMSTAGING = 105
 };
 
 /* integration modes (SHWFS_INTEGMODE) */
@@ -224,8 +230,11 @@ typedef struct shwfs_info {
   int gemm_kcb;         /* tensor-core forms' staging: bytes of K per W2 chunk row, */
   int gemm_nw;          /* W2 ring stages, */
   int gemm_nk;          /* Kc ring stages, */
-  int gemm_dbuf;        /* 1: two field buffers, 2: two |F|^2 buffers (OR); all 0
-                           when no tensor-core form is built */
+  int gemm_dbuf;        /* 1: two field buffers, 2: two |F|^2 buffers (OR), */
+  int gemm_cw;          /* complex outputs per GEMM1 chunk; all 0 when no
+                           tensor-core form is built */
+  int gemm_staging;     /* index of the staging in use (SHWFS_GEMMSTAGING) */
+  int gemm_candidates;  /* stagings that fit (0 without a tensor-core form) */
 } shwfs_info;
 
 typedef struct shwfs_handle shwfs_handle;
@@ -327,9 +336,9 @@ shwfs_status shwfs_batch_free(shwfs_batch* b);
 /* Time the handle's phase-input kernels over their launch shapes on scratch
  * buffers and keep the fastest: for the FP32 form the candidate tile sizes
  * of the fused kernel (*best_tile receives the one kept); for a tensor-core
- * form every shared-memory staging of the GEMM kernel that fits (W2 chunk
- * width, double buffering of the field and |F|^2 operands, Kc stages, W2
- * ring depth; shwfs_info.gemm_* report the one kept).  Results are
+ * form every staging of the GEMM kernel that fits (GEMM1 output-chunk width,
+ * W2 chunk width, double buffering of the field and |F|^2 operands, Kc
+ * stages, W2 ring depth; shwfs_info.gemm_* report the one kept).  Results are
  * unchanged: the tile size only groups subapertures per CTA, and the MMAs
  * see the same k-steps in the same order whatever the staging. */
 shwfs_status shwfs_autotune(shwfs_handle* h, int* best_tile);

@@ -67,6 +67,7 @@ def test_extension_codes_match_header():
     assert code("SHWFS_HOSTIO_OUTPUTS") == cc.HOSTIO_OUTPUTS
     assert code("SHWFS_HOSTIO_PHASE") == cc.HOSTIO_PHASE
     assert code("SHWFS_INTEGMODE") == cc.INTEGMODE
+    assert code("SHWFS_GEMMSTAGING") == cc.GEMMSTAGING
     for name, v in cc.FORMS.items():
         assert code("SHWFS_FORM_%s" % name.upper()) == v
 

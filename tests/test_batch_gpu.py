@@ -143,9 +143,10 @@ def test_autotune_keeps_results():
 
 @pytest.mark.parametrize("form", ["fp16", "bf16x3", "tf32"])
 def test_autotune_gemm_staging_keeps_results(form):
-    """The tensor-core forms' autotuner times every shared-memory staging of
-    the GEMM kernel and keeps one; the MMAs see the same k-steps in the same
-    order, so the outputs stay bit-identical to the default staging."""
+    """The tensor-core forms' autotuner times every staging of the GEMM
+    kernel and keeps one; the MMAs see the same k-steps in the same order
+    (GEMM2's K padding beyond the crop only adds zeros), so the outputs stay
+    bit-identical to the default staging."""
     kw = dict(nsubx=16, p=10, N=20, C=20, m=10, psf="gauss", **NOISY)
     base = DevEngine(Case(**kw), form)
     tuned = DevEngine(Case(**kw), form)
@@ -154,6 +155,7 @@ def test_autotune_gemm_staging_keeps_results(form):
     tuned.eng.autotune()
     t = tuned.eng.info()
     assert t["gemm_kcb"] in (64, 128) and t["gemm_nw"] >= 2 and t["gemm_nk"] in (1, 2) and 0 <= t["gemm_dbuf"] <= 3
+    assert d["gemm_cw"] == 64 and t["gemm_cw"] in (64, 80)  # 20 x 20 crop: 7 chunks of 64 or 5 of 80
     assert t["frames_read"] == 0
     for k in range(2):
         if k:
@@ -161,3 +163,31 @@ def test_autotune_gemm_staging_keeps_results(form):
         base.run_alone()
         tuned.run_alone()
         _same([base.outputs()], [tuned.outputs()])
+
+
+@pytest.mark.parametrize("form", ["fp16", "bf16x3", "tf32"])
+def test_every_gemm_staging_gives_the_same_results(form):
+    """Every staging the tensor-core forms can run (SHWFS_GEMMSTAGING; output
+    chunks of 64 or 80 complex outputs for the 20 x 20 crop, W2 chunk width,
+    operand double buffering, ring depths) gives bit-identical images and
+    centroids."""
+    from dasp_gb300.centcmod import GEMMSTAGING
+    kw = dict(nsubx=16, p=10, N=20, C=20, m=10, psf="gauss", **NOISY)
+    base = DevEngine(Case(**kw), form)
+    n = base.eng.info()["gemm_candidates"]
+    assert n >= 2
+    base.run_alone()
+    ref = base.outputs()
+    cws = set()
+    for i in range(1, n):
+        e = DevEngine(Case(**kw), form)
+        e.eng.update(GEMMSTAGING, i)
+        inf = e.eng.info()
+        assert inf["gemm_staging"] == i
+        cws.add(inf["gemm_cw"])
+        e.run_alone()
+        _same([ref], [e.outputs()])
+        e.eng.free()
+    assert 80 in cws
+    with pytest.raises(Exception):
+        base.eng.update(GEMMSTAGING, n)
