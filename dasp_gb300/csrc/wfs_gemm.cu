@@ -7,7 +7,8 @@
 //          E = pup*exp(i(phs - tilt)) as [Re E | Im E] over the p x p pixels,
 //          W2 = real embedding of the 2-D DFT restricted to the c x c outputs
 //          that survive the central crop (addPowerSpecCentral,
-//          cmod/src/centmodule.c:430-471), 64 complex outputs per chunk
+//          cmod/src/centmodule.c:430-471), CW complex outputs per chunk
+//          (64, or wider when that needs fewer chunks)
 //   |F|^2  per thread (its own subaperture row)
 //   GEMM2  B[s, q] += I[s, o] . Kc[q, o]                                   -> f32 (TMEM)
 //          Kc = the whole linear chain 180-degree placement -> [prebin] ->
