@@ -634,10 +634,28 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
             store8<FMT, SPLIT>(Ahi, Alo, kmaj(r, h * 32 + k8 * 8, ESZ, sbo2), x8);
           }
         } else {
-          // wider chunks: 16 columns (8 complex outputs) at a time, each
-          // stored as soon as it is computed
+          // wider chunks: 64 columns (32 complex outputs) at a time with
+          // one wait, then 16 at a time, each stored as soon as it is computed
           a2_wait();
-          for (int u = 0; u < g.CW; u += 16) {
+          int u = 0;
+          for (; u + 64 <= g.CW; u += 64) {
+            uint32_t v0[32], v1[32];
+            tc::tmem_ld32(col + u, v0);
+            tc::tmem_ld32(col + u + 32, v1);
+            tc::tmem_ld_wait();
+#pragma unroll
+            for (int k8 = 0; k8 < 4; k8++) {
+              const uint32_t* vv = k8 < 2 ? v0 : v1;
+              const int o = (k8 & 1) * 16;
+              float x8[8];
+#pragma unroll
+              for (int e = 0; e < 8; e++)
+                x8[e] = (__uint_as_float(vv[o + 2 * e]) * __uint_as_float(vv[o + 2 * e]) +
+                         __uint_as_float(vv[o + 2 * e + 1]) * __uint_as_float(vv[o + 2 * e + 1])) * isc;
+              store8<FMT, SPLIT>(Ahi, Alo, kmaj(r, h * (g.CW / 2) + u / 2 + k8 * 8, ESZ, sbo2), x8);
+            }
+          }
+          for (; u < g.CW; u += 16) {
             float v16[16];
             tc::tmem_ld16_sync(col + u, v16);
             float x8[8];
