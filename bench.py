@@ -974,6 +974,9 @@ def main():
     ap.add_argument("--form", default=None, choices=["fp32", "fp16", "bf16x3", "tf32", "bf16"],
                     help="headline form (and the end-to-end run's) instead of the fastest within 1e-3 px; for "
                          "profiling runs, whose timings cannot choose")
+    ap.add_argument("--staging", type=int, default=None,
+                    help="with --form: that form's GEMM staging index instead of the autotuner's choice "
+                         "(profiling runs)")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--precision-frames", type=int, default=8)
     ap.add_argument("--serve-inflight", type=int, default=16)
@@ -1037,8 +1040,14 @@ def main():
             return None
         # the engine's own autotuner picks the launch shape on this handle's
         # phase (results do not depend on it): the FP32 kernel's tile size,
-        # the GEMM kernel's shared-memory staging
-        ts = eng.autotune()
+        # the GEMM kernel's staging (--staging fixes the headline form's for
+        # profiling runs, which then launch no tuning kernels)
+        if args.staging is not None and form == args.form and form != "fp32":
+            from dasp_gb300.centcmod import GEMMSTAGING
+            eng.update(GEMMSTAGING, args.staging)
+            ts = eng.info()["tile_subaps"]
+        else:
+            ts = eng.autotune()
         inf = eng.info()
         staging = {k: inf["gemm_" + k] for k in ("cw", "kcb", "nw", "nk", "dbuf")} if form != "fp32" else {"tile": ts}
         with torch.cuda.stream(stream):
