@@ -85,7 +85,7 @@ def make_engine(pup, phs, cents, bimg, noiseless=False):
 
 # DRAM bytes (read + write) per launch of the 64-frame step, from one ncu
 # capture of each kernel (commands and figures in profiles/)
-NCU_TRAFFIC = {"wfs_gemm_kernel": 162.2e6, "wfs_post_warp_kernel": 149.3e6}
+NCU_TRAFFIC = {"wfs_gemm_kernel": 161.5e6, "wfs_post_warp_kernel": 149.3e6}
 
 
 def tensor_flops_per_subap():
