@@ -775,35 +775,44 @@ cudaError_t launch_one(const WfsArgs& a, const GemmGeom& g, const float* iscale,
 
 }  // namespace
 
-bool gemm_geometry(const GemmSpec& sp, int fmt, int passes, GemmGeom* g) {
-  if (fmt != kFmtBF16 && fmt != kFmtFP16 && fmt != kFmtTF32) return false;
-  if (passes != 1 && !(passes == 3 && fmt == kFmtBF16)) return false;
-  const int esz = fmt == kFmtTF32 ? 4 : 2;
-  const int pp = sp.p * sp.p, ppr = (pp + 7) & ~7;
-  const int K1 = ((2 * ppr + 15) / 16) * 16;
-  const int mm = sp.m * sp.m;
-  const int N2 = ((mm + 15) / 16) * 16;
-  if (N2 > 256 || pp > 256) return false;
-  g->fmt = fmt;
-  g->passes = passes;
-  g->K1 = K1;
-  g->N2 = N2;
-  g->CW = 64;
-  g->nd1 = N2 <= 128 ? 3 : 2;
-  g->noc = (sp.c * sp.c + 63) / 64;
-  // dynamic limit: 227 KB minus the kernel's static shared memory (< 2 KB)
+namespace {
+
+// GEMM1 output-chunk widths for a c x c crop: for each chunk count below
+// that of 64-wide chunks, the narrowest multiple of 16 covering the crop in
+// that many chunks, when GEMM1 N = 2 CW <= 256 and two D1 buffers and D2 fit
+// the 512 TMEM columns; fewest chunks first, 64 last
+std::vector<int> chunk_widths(int cc, int N2) {
+  std::vector<int> widths;
+  for (int k = (cc + 127) / 128; k < (cc + 63) / 64; k++) {
+    const int cw = 16 * ((cc + 16 * k - 1) / (16 * k));
+    if (cw <= 64 || 2 * cw > 256 || 4 * cw + N2 > 512) continue;
+    bool dup = false;
+    for (int w : widths) dup = dup || w == cw;
+    if (!dup) widths.push_back(cw);
+  }
+  widths.push_back(64);
+  return widths;
+}
+
+// the stagings of chunk width cw that fit shared memory, in preference
+// order: four k-steps per W2 chunk, then two field buffers (one-pass 16-bit
+// formats), two |F|^2 buffers, two Kc stages, as long as the W2 ring keeps
+// enough stages (as deep as shared memory allows)
+std::vector<GemmGeom> stagings_of_width(GemmGeom g, int cw, int cc, int passes) {
+  std::vector<GemmGeom> out;
+  const int esz = g.fmt == kFmtTF32 ? 4 : 2;
+  // dynamic limit: 227 KB minus the kernel's static shared memory (< 4 KB)
   const uint32_t limit = 227 * 1024 - 4096;
-  // bytes of K per row in one streamed W2 chunk: four k-steps for one-pass
-  // formats, two for the split form (whose stages carry hi and lo), two
-  // when four do not fit; prefer two field buffers (one-pass 16-bit
-  // formats), then two Kc stages, as long as the W2 ring keeps enough stages
-  for (int kcb = passes == 1 ? 128 : 64; kcb >= 64; kcb -= 64) {
-    g->KCB = kcb;
-    g->nkc = (K1 * esz + kcb - 1) / kcb;
-    for (int db = (passes == 1 && esz == 2) ? 1 : 0; db >= 0; db--) {
-      for (int da = 1; da >= 0; da--) {
+  g.CW = cw;
+  g.noc = (cc + cw - 1) / cw;
+  g.nd1 = (cw == 64 && g.N2 <= 128) ? 3 : 2;
+  for (int kcb = passes == 1 ? 128 : 64; kcb >= 64; kcb -= 64)
+    for (int db = (passes == 1 && esz == 2) ? 1 : 0; db >= 0; db--)
+      for (int da = 1; da >= 0; da--)
         for (int nk = 2; nk >= 1; nk--) {
-          GemmGeom t = *g;
+          GemmGeom t = g;
+          t.KCB = kcb;
+          t.nkc = (t.K1 * esz + kcb - 1) / kcb;
           t.dbE = db;
           t.dbA2 = da;
           t.NK = nk;
@@ -813,13 +822,35 @@ bool gemm_geometry(const GemmSpec& sp, int fmt, int passes, GemmGeom* g) {
           int nw = (int)((limit - base.total) / base.wStage);
           if (nw > kGemmMaxNW) nw = kGemmMaxNW;
           if (nw < (nk == 2 ? 3 : 2)) continue;
-          g->dbE = db;
-          g->dbA2 = da;
-          g->NK = nk;
-          g->NW = nw;
-          return true;
+          t.NW = nw;
+          out.push_back(t);
         }
-      }
+  return out;
+}
+
+}  // namespace
+
+bool gemm_geometry(const GemmSpec& sp, int fmt, int passes, GemmGeom* g) {
+  if (fmt != kFmtBF16 && fmt != kFmtFP16 && fmt != kFmtTF32) return false;
+  if (passes != 1 && !(passes == 3 && fmt == kFmtBF16)) return false;
+  const int pp = sp.p * sp.p, ppr = (pp + 7) & ~7;
+  const int K1 = ((2 * ppr + 15) / 16) * 16;
+  const int mm = sp.m * sp.m;
+  const int N2 = ((mm + 15) / 16) * 16;
+  if (N2 > 256 || pp > 256) return false;
+  GemmGeom t = *g;
+  t.fmt = fmt;
+  t.passes = passes;
+  t.K1 = K1;
+  t.N2 = N2;
+  // the first staging that fits, with the fewest GEMM1 output chunks (each
+  // chunk costs the epilogue a TMEM read, a fence and barrier round trips)
+  const int cc = sp.c * sp.c;
+  for (int cw : chunk_widths(cc, N2)) {
+    const std::vector<GemmGeom> st = stagings_of_width(t, cw, cc, passes);
+    if (!st.empty()) {
+      *g = st[0];
+      return true;
     }
   }
   return false;
@@ -830,50 +861,14 @@ std::vector<GemmGeom> gemm_geometry_candidates(const GemmSpec& sp, int fmt, int 
   GemmGeom g0{};
   if (!gemm_geometry(sp, fmt, passes, &g0)) return out;
   out.push_back(g0);  // the default first
-  const int esz = fmt == kFmtTF32 ? 4 : 2;
-  const uint32_t limit = 227 * 1024 - 4096;
-  // chunk widths: 64 complex outputs, and for each smaller chunk count the
-  // narrowest multiple of 16 that covers the crop in that many chunks, when
-  // two D1 buffers and D2 fit the 512 TMEM columns (GEMM1 N = 2 CW <= 256)
   const int cc = sp.c * sp.c;
-  std::vector<int> widths = {64};
-  for (int k = (cc + 127) / 128; k < (cc + 63) / 64; k++) {
-    const int cw = 16 * ((cc + 16 * k - 1) / (16 * k));
-    if (cw <= 64 || 2 * cw > 256 || 4 * cw + g0.N2 > 512) continue;
-    bool dup = false;
-    for (int w : widths) dup = dup || w == cw;
-    if (!dup) widths.push_back(cw);
-  }
-  for (int cw : widths) {
-    GemmGeom g = g0;
-    g.CW = cw;
-    g.noc = (cc + cw - 1) / cw;
-    g.nd1 = (cw == 64 && g.N2 <= 128) ? 3 : 2;
-    // the ranges gemm_geometry draws from: four k-steps per W2 chunk and two
-    // field buffers only for one-pass (16-bit) formats
-    for (int kcb = passes == 1 ? 128 : 64; kcb >= 64; kcb -= 64)
-      for (int db = (passes == 1 && esz == 2) ? 1 : 0; db >= 0; db--)
-        for (int da = 1; da >= 0; da--)
-          for (int nk = 2; nk >= 1; nk--) {
-            GemmGeom t = g;
-            t.KCB = kcb;
-            t.nkc = (t.K1 * esz + kcb - 1) / kcb;
-            t.dbE = db;
-            t.dbA2 = da;
-            t.NK = nk;
-            t.NW = 0;
-            const GemmSmem base = gemm_smem_layout(t);
-            if (base.total > limit) continue;
-            int nw = (int)((limit - base.total) / base.wStage);
-            if (nw > kGemmMaxNW) nw = kGemmMaxNW;
-            if (nw < (nk == 2 ? 3 : 2)) continue;
-            t.NW = nw;
-            if (t.CW == g0.CW && t.KCB == g0.KCB && t.dbE == g0.dbE && t.dbA2 == g0.dbA2 && t.NK == g0.NK &&
-                t.NW == g0.NW)
-              continue;
-            out.push_back(t);
-          }
-  }
+  for (int cw : chunk_widths(cc, g0.N2))
+    for (const GemmGeom& t : stagings_of_width(g0, cw, cc, passes)) {
+      if (t.CW == g0.CW && t.KCB == g0.KCB && t.dbE == g0.dbE && t.dbA2 == g0.dbA2 && t.NK == g0.NK &&
+          t.NW == g0.NW)
+        continue;
+      out.push_back(t);
+    }
   return out;
 }
 

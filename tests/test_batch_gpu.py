@@ -155,7 +155,7 @@ def test_autotune_gemm_staging_keeps_results(form):
     tuned.eng.autotune()
     t = tuned.eng.info()
     assert t["gemm_kcb"] in (64, 128) and t["gemm_nw"] >= 2 and t["gemm_nk"] in (1, 2) and 0 <= t["gemm_dbuf"] <= 3
-    assert d["gemm_cw"] == 64 and t["gemm_cw"] in (64, 80)  # 20 x 20 crop: 7 chunks of 64 or 5 of 80
+    assert d["gemm_cw"] == 80 and t["gemm_cw"] in (64, 80)  # 20 x 20 crop: 5 chunks of 80 (default) or 7 of 64
     assert t["frames_read"] == 0
     for k in range(2):
         if k:
@@ -188,6 +188,6 @@ def test_every_gemm_staging_gives_the_same_results(form):
         e.run_alone()
         _same([ref], [e.outputs()])
         e.eng.free()
-    assert 80 in cws
+    assert 64 in cws
     with pytest.raises(Exception):
         base.eng.update(GEMMSTAGING, n)
