@@ -748,6 +748,10 @@ def run_lgs_batch(args):
     with ClockSampler(0) as clk:
         g_med, g_mean = timed(run_graph)
         s_med, s_mean = timed(run_seq)
+        # the same graph with the FP32-form LGS sensors as one multi-handle kernel
+        batch.set_multi(True)
+        multi = batch.multi_launches()
+        m_med, _ = timed(run_graph)
     batch.free()
     for e in engines:
         e.free()
@@ -757,7 +761,9 @@ def run_lgs_batch(args):
         "warmup": args.warmup, "ms_per_step": g_med, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "per WFS: " + ", ".join(forms),
         "data": "synthetic: seeded von Karman screens, elongated LGS and Gaussian NGS spots",
-        "config": {"workload": "lgs_batch_6x74_3ngs", "wfs": [{k: v for k, v in sp.items() if k != "obs"} for sp in specs],
+        "config": {"workload": "lgs_batch_6x74_3ngs",
+                   "multi_handle": {"launches": multi, "ms_per_step": m_med},
+                   "wfs": [{k: v for k, v in sp.items() if k != "obs"} for sp in specs],
                    "lit_subaps_per_step": lit, "l2": "flushed between timed steps (256 MB write, untimed)"},
         "sequential_ms_per_step": s_med, "graph_speedup_vs_sequential": s_med / g_med,
         "clocks": clk.summary(),

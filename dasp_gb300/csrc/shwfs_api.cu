@@ -92,6 +92,13 @@ std::vector<T> to_host(const shwfs_array& a) {
 
 }  // namespace
 
+// a fused-kernel launch of one handle held back for a multi-handle launch
+struct DeferredPlain {
+  struct shwfs_handle* h;
+  shwfs::WfsArgs a;
+  long long ntiles;
+};
+
 struct shwfs_handle {
   // parameters (names as in centstruct)
   int nthreads = 1, nsubaps = 0, nsubx = 0, ncen = 0, fftsize = 0, clipsize = 0, nimg = 0, phasesize = 0;
@@ -178,6 +185,10 @@ struct shwfs_handle {
   DevBuf<float> d_iscale;  // fp16 form: 1 / (sum of the subaperture's pupil)^2
   DevBuf<float> d_pupT;    // tensor-core forms: pupil by pixel group [ppr/8][nlit][8]
   cudaEvent_t splitEvent = nullptr;  // recorded between image formation and post stages
+  // while a multi-sensor batch captures: where the fused FP32 kernel's
+  // launch goes instead of the stream (the batch launches the kernels of
+  // several handles of one instantiation as one multi-handle kernel)
+  std::vector<struct DeferredPlain>* plainSink = nullptr;
   const PoisTab* poisTab = nullptr;  // Poisson CDF tables on this device
   // correlation centroiding: pattern (host copy), its size, the per-mode
   // device kernel, and the corrimg output (borrowed; device mirror)
@@ -921,7 +932,10 @@ shwfs_status enqueue_readout(shwfs_handle* h, const float* phs, float* cents, fl
       plainDirect = bimgHost != nullptr;
       if (plainDirect) bimg = bimgHost;
       WfsArgs a = make_args(h, phs, cents, bimg, nframes, phsStride, kForm | kNoiseCounter | kPost);
-      CK(h->entry->launch(a, grid, h->smem, st));
+      if (h->plainSink && !plainDirect)
+        h->plainSink->push_back(DeferredPlain{h, a, ntiles});
+      else
+        CK(h->entry->launch(a, grid, h->smem, st));
     }
     if (!h->unlit.empty() && !(postDone & kPostDidUnlit)) {
       WfsArgs a = make_args(h, phs, cents, bimg, nframes, phsStride, 0);
@@ -1923,6 +1937,11 @@ struct shwfs_batch {
   cudaStream_t cap = nullptr;  // capture origin and default launch stream
   std::vector<cudaStream_t> branch;
   std::vector<cudaEvent_t> ev;  // ev[0] fork, ev[1 + i] join of branch i
+  // the multi-handle fused-kernel launches' branch and its join
+  cudaStream_t multiBranch = nullptr;
+  cudaEvent_t multiJoin = nullptr;
+  int multiLaunches = 0;  // multi-handle launches in the captured graph
+  bool multiEnabled = false;  // shwfs_batch_set_multi
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   DevBuf<unsigned long long*> d_ctrs;
@@ -1939,6 +1958,8 @@ struct shwfs_batch {
     drop_graph();
     for (cudaStream_t s : branch) cudaStreamDestroy(s);
     for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    if (multiBranch) cudaStreamDestroy(multiBranch);
+    if (multiJoin) cudaEventDestroy(multiJoin);
     if (cap) cudaStreamDestroy(cap);
   }
 };
@@ -1952,6 +1973,27 @@ shwfs_status batch_capture(shwfs_batch* b) {
   b->drop_graph();
   for (shwfs_handle* h : b->hs)
     if (shwfs_status s = prepare_readout(h)) return s;
+  // handles whose readout is one fused FP32 kernel plus independent work
+  // (counter noise, no correlation, no phase interpolation) and that share
+  // an instantiation with another such handle: their fused kernels run as
+  // one multi-handle launch on a branch of their own
+  std::vector<DeferredPlain> deferred;
+  for (shwfs_handle* h : b->hs) {
+    h->plainSink = nullptr;
+    const bool ok = b->multiEnabled && h->entry && !gemm_active(h) && h->noiseMode == SHWFS_NOISE_COUNTER && !corr_active(h) &&
+                    !h->interp && !h->lit.empty();
+    if (!ok) continue;
+    // same instantiation and the same shared-memory footprint (so that the
+    // multi-handle launch keeps each handle's occupancy)
+    int same = 0;
+    for (shwfs_handle* o : b->hs)
+      same += (o->entry == h->entry && o->smem == h->smem && !gemm_active(o) && o->noiseMode == SHWFS_NOISE_COUNTER &&
+               !corr_active(o) && !o->interp && !o->lit.empty())
+                  ? 1
+                  : 0;
+    if (same >= 2) h->plainSink = &deferred;
+  }
+  b->multiLaunches = 0;
   CK(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeRelaxed));
   auto body = [&]() -> shwfs_status {
     CK(cudaEventRecord(b->ev[0], b->cap));
@@ -1966,10 +2008,48 @@ shwfs_status batch_capture(shwfs_batch* b) {
       CK(cudaEventRecord(b->ev[1 + i], b->branch[i]));
       CK(cudaStreamWaitEvent(b->cap, b->ev[1 + i], 0));
     }
+    if (!deferred.empty()) {
+      CK(cudaStreamWaitEvent(b->multiBranch, b->ev[0], 0));
+      // groups of one instantiation, at most kPlainMulti handles each
+      std::vector<bool> done(deferred.size(), false);
+      for (size_t i = 0; i < deferred.size(); i++) {
+        if (done[i]) continue;
+        std::vector<size_t> grp;
+        for (size_t j = i; j < deferred.size() && grp.size() < (size_t)kPlainMulti; j++)
+          if (!done[j] && deferred[j].h->entry == deferred[i].h->entry && deferred[j].h->smem == deferred[i].h->smem)
+            grp.push_back(j);
+        int smem = 0, numSMs = deferred[i].h->numSMs;
+        for (size_t j : grp) {
+          done[j] = true;
+          smem = std::max(smem, deferred[j].h->smem);
+        }
+        int ctas = 0;
+        CK(deferred[i].h->entry->occupancy_multi(&ctas, smem));
+        if (ctas < 1) return fail(SHWFS_ERR_UNSUPPORTED, "multi-handle kernel cannot be resident");
+        // each handle gets the CTAs a launch of its own would have (the
+        // block scheduler then balances the union as it balances
+        // concurrent launches)
+        const long long perHandle = (long long)numSMs * ctas;
+        PlainMulti m{};
+        m.n = (int)grp.size();
+        m.ctaStart[0] = 0;
+        for (size_t k = 0; k < grp.size(); k++) {
+          const long long t = deferred[grp[k]].ntiles;
+          const long long c = std::max<long long>(1, std::min<long long>(t, perHandle));
+          m.a[k] = deferred[grp[k]].a;
+          m.ctaStart[k + 1] = m.ctaStart[k] + (int)c;
+        }
+        CK(deferred[i].h->entry->launch_multi(m, smem, b->multiBranch));
+        b->multiLaunches++;
+      }
+      CK(cudaEventRecord(b->multiJoin, b->multiBranch));
+      CK(cudaStreamWaitEvent(b->cap, b->multiJoin, 0));
+    }
     CK(launch_bump_counters(b->d_ctrs.p, (int)b->hs.size(), b->cap));
     return SHWFS_OK;
   };
   const shwfs_status s = body();
+  for (shwfs_handle* h : b->hs) h->plainSink = nullptr;
   const std::string err = g_err;
   cudaGraph_t g = nullptr;
   const cudaError_t e = cudaStreamEndCapture(b->cap, &g);
@@ -2032,6 +2112,8 @@ shwfs_status shwfs_batch_create(shwfs_handle* const* handles, int n, shwfs_batch
       CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
       b->ev.push_back(e);
     }
+    CK(cudaStreamCreateWithFlags(&b->multiBranch, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&b->multiJoin, cudaEventDisableTiming));
     CK(b->d_ctrs.upload(ptrs.data(), ptrs.size()));
     return batch_capture(b);
   };
@@ -2042,6 +2124,21 @@ shwfs_status shwfs_batch_create(shwfs_handle* const* handles, int n, shwfs_batch
     return s;
   }
   *out = b;
+  return SHWFS_OK;
+}
+
+shwfs_status shwfs_batch_set_multi(shwfs_batch* b, int on) {
+  if (!b) return fail(SHWFS_ERR_INVALID, "null batch");
+  CK(cudaSetDevice(b->device));
+  if (b->multiEnabled == (on != 0)) return SHWFS_OK;
+  b->multiEnabled = on != 0;
+  CK(cudaStreamSynchronize(b->cap));
+  return batch_capture(b);
+}
+
+shwfs_status shwfs_batch_multi_launches(const shwfs_batch* b, int* n) {
+  if (!b || !n) return fail(SHWFS_ERR_INVALID, "null batch or output");
+  *n = b->multiLaunches;
   return SHWFS_OK;
 }
 

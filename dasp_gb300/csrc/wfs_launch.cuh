@@ -14,6 +14,9 @@ namespace shwfs {
 
 struct PlainEntry {
   cudaError_t (*launch)(const WfsArgs&, int grid, int smem, cudaStream_t);
+  // several handles of this instantiation in one launch (grid = m.ctaStart[m.n])
+  cudaError_t (*launch_multi)(const PlainMulti& m, int smem, cudaStream_t);
+  cudaError_t (*occupancy_multi)(int* ctas_per_sm, int smem);
   cudaError_t (*occupancy)(int* ctas_per_sm, int smem);
   cudaError_t (*psf_spectra)(const float* psf, int npsf, float2* out, cudaStream_t);
 };
@@ -62,6 +65,19 @@ cudaError_t plain_launch(const WfsArgs& a, int grid, int smem, cudaStream_t stre
 }
 
 template <int N, int P>
+cudaError_t plain_launch_multi(const PlainMulti& m, int smem, cudaStream_t stream) {
+  cudaError_t e = kernel_smem_setup((const void*)wfs_plain_multi_kernel<N, P>, smem, kThreads, nullptr);
+  if (e != cudaSuccess) return e;
+  wfs_plain_multi_kernel<N, P><<<m.ctaStart[m.n], kThreads, smem, stream>>>(m);
+  return cudaGetLastError();
+}
+
+template <int N, int P>
+cudaError_t plain_occupancy_multi(int* ctas, int smem) {
+  return kernel_smem_setup((const void*)wfs_plain_multi_kernel<N, P>, smem, kThreads, ctas);
+}
+
+template <int N, int P>
 cudaError_t plain_occupancy(int* ctas, int smem) {
   return kernel_smem_setup((const void*)wfs_plain_kernel<N, P>, smem, kThreads, ctas);
 }
@@ -79,7 +95,9 @@ cudaError_t psf_spectra_launch(const float* psf, int npsf, float2* out, cudaStre
 template <int N, int P>
 struct PlainRegistrar {
   PlainRegistrar() {
-    plain_registry()[{N, P}] = PlainEntry{&plain_launch<N, P>, &plain_occupancy<N, P>, &psf_spectra_launch<P>};
+    plain_registry()[{N, P}] =
+        PlainEntry{&plain_launch<N, P>, &plain_launch_multi<N, P>, &plain_occupancy_multi<N, P>,
+                   &plain_occupancy<N, P>, &psf_spectra_launch<P>};
   }
 };
 

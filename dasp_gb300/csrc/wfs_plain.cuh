@@ -387,8 +387,11 @@ __device__ __forceinline__ void post_tile(const WfsArgs& a, int ns, const int* s
     }
 }
 
+// The fused kernel's work for one handle, run by CTA `cta` of the `nctas`
+// CTAs that share its tiles (the whole grid for a single handle, a slice of
+// it in a multi-handle launch).
 template <int N, int P>
-__global__ void __launch_bounds__(kThreads) wfs_plain_kernel(const WfsArgs a) {
+__device__ __forceinline__ void plain_body(const WfsArgs& a, long long cta, long long nctas) {
   extern __shared__ float4 smem4[];
   float* smem = reinterpret_cast<float*>(smem4);
   const int tid = threadIdx.x;
@@ -445,7 +448,7 @@ __global__ void __launch_bounds__(kThreads) wfs_plain_kernel(const WfsArgs a) {
   const int cc = padded > N ? N : padded;
   const int nexp = a.opticalBinning == 1 ? 2 * a.ncen : mm;
 
-  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  for (long long tile = cta; tile < ntiles; tile += nctas) {
     const long long w0 = tile * TS;
     const int ns = (int)min((long long)TS, nwork - w0);
     __syncthreads();  // previous tile fully consumed
@@ -766,6 +769,28 @@ __global__ void __launch_bounds__(kThreads) wfs_plain_kernel(const WfsArgs a) {
 #undef AMPSUM
 #undef SCAL
   }
+}
+
+template <int N, int P>
+__global__ void __launch_bounds__(kThreads) wfs_plain_kernel(const __grid_constant__ WfsArgs a) {
+  plain_body<N, P>(a, blockIdx.x, gridDim.x);
+}
+
+// Several handles of one (fftsize, psfsize) instantiation in one launch (the
+// multi-sensor batches): handle h owns CTAs [ctaStart[h], ctaStart[h+1]) and
+// each of them loops over that handle's tiles, as in a launch of its own.
+constexpr int kPlainMulti = 8;
+struct PlainMulti {
+  WfsArgs a[kPlainMulti];
+  int ctaStart[kPlainMulti + 1];
+  int n;
+};
+
+template <int N, int P>
+__global__ void __launch_bounds__(kThreads) wfs_plain_multi_kernel(const __grid_constant__ PlainMulti m) {
+  int h = 0;
+  while (h + 1 < m.n && (int)blockIdx.x >= m.ctaStart[h + 1]) h++;
+  plain_body<N, P>(m.a[h], (long long)blockIdx.x - m.ctaStart[h], (long long)(m.ctaStart[h + 1] - m.ctaStart[h]));
 }
 
 // launcher of the unlit-subaperture kernel (wfs_unlit.cu)

@@ -325,13 +325,25 @@ const char* shwfs_version(void);
  * A batch captures one readout frame of every handle into a CUDA graph: each
  * handle's persistent kernel(s) on its own graph branch, branches running
  * concurrently, so WFSs of different subaperture counts, FFT sizes and spot
- * PSFs go to the GPU with one graph launch.  Every handle must have
- * device-resident phs/cents/bimg.  The graph is re-captured when a handle is
- * updated; noise frame counters advance on the device between replays. */
+ * PSFs go to the GPU with one graph launch.  With shwfs_batch_set_multi,
+ * handles on the fused FP32 kernel that share its (fftsize, psfsize)
+ * instantiation and shared-memory footprint (counter noise, no correlation
+ * centroiding, no phase interpolation) run as one persistent multi-handle
+ * kernel over their tiles (up to 8 handles per launch) on a branch of its
+ * own; results are identical either way.  Every handle must have
+ * device-resident phs/cents/bimg.
+ * The graph is re-captured when a handle is updated; noise frame counters
+ * advance on the device between replays. */
 typedef struct shwfs_batch shwfs_batch;
 shwfs_status shwfs_batch_create(shwfs_handle* const* handles, int n, shwfs_batch** out);
 shwfs_status shwfs_batch_run(shwfs_batch* b, void* stream);
 shwfs_status shwfs_batch_free(shwfs_batch* b);
+/* on != 0: group handles into multi-handle fused-kernel launches (off by
+ * default: on the measured workloads the concurrent per-handle launches were
+ * as fast or faster); re-captures the graph */
+shwfs_status shwfs_batch_set_multi(shwfs_batch* b, int on);
+/* multi-handle fused-kernel launches in the batch's captured graph */
+shwfs_status shwfs_batch_multi_launches(const shwfs_batch* b, int* n);
 
 /* Time the handle's phase-input kernels over their launch shapes on scratch
  * buffers and keep the fastest: for the FP32 form the candidate tile sizes

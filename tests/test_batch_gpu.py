@@ -191,3 +191,42 @@ def test_every_gemm_staging_gives_the_same_results(form):
     assert 64 in cws
     with pytest.raises(Exception):
         base.eng.update(GEMMSTAGING, n)
+
+
+def test_multi_handle_kernel_equals_individual_runs():
+    """FP32-form handles of one kernel instantiation (fftsize 16, no PSF;
+    8x8 to 20x20 subapertures, different signal, noise and seeds) run as one
+    persistent multi-handle kernel in the batch graph, beside a handle of
+    another instantiation and a tensor-core one; every handle's images and
+    centroids equal its run on its own, frame after frame."""
+    from dasp_gb300.batch import WfsBatch
+    same = [dict(nsubx=n, p=8, N=16, C=16, m=8, sig=s, skybrightness=sk, readnoise=rn, addPoisson=1, noiseFloor=1.0,
+                 seed=sd)
+            for n, s, sk, rn, sd in ((8, 2e3, 5.0, 2.0, 3), (12, 4e3, 1.0, 1.0, 4), (20, 1e3, 8.0, 3.0, 5),
+                                     (16, 3e3, 0.0, 0.5, 6))]
+    other = [dict(nsubx=12, p=10, N=20, C=20, m=10, psf="gauss", **NOISY)]
+    geoms = same + other + [dict(nsubx=12, p=10, N=20, C=20, m=10, psf="gauss", **NOISY)]
+    forms = ["fp32"] * (len(same) + 1) + ["fp16"]
+    a = [DevEngine(Case(**g), f) for g, f in zip(geoms, forms)]
+    b = [DevEngine(Case(**g), f) for g, f in zip(geoms, forms)]
+    batch = WfsBatch([x.eng for x in a])
+    assert batch.multi_launches() == 0  # off by default
+    batch.set_multi(True)
+    assert batch.multi_launches() == 1
+    for f in range(3):
+        _new_phase(list(zip(a, b)), 120 + 10 * f)
+        batch.run()
+        for y in b:
+            y.run_alone()
+        _same([x.outputs() for x in a], [y.outputs() for y in b])
+    batch.free()
+    # more handles of one instantiation than one launch takes: several launches
+    many = [DevEngine(Case(**dict(same[k % 4], seed=30 + k))) for k in range(10)]
+    solo = [DevEngine(Case(**dict(same[k % 4], seed=30 + k))) for k in range(10)]
+    batch = WfsBatch([x.eng for x in many], multi=True)
+    assert batch.multi_launches() == 2
+    batch.run()
+    for y in solo:
+        y.run_alone()
+    _same([x.outputs() for x in many], [y.outputs() for y in solo])
+    batch.free()
