@@ -2131,9 +2131,17 @@ shwfs_status shwfs_batch_set_multi(shwfs_batch* b, int on) {
   if (!b) return fail(SHWFS_ERR_INVALID, "null batch");
   CK(cudaSetDevice(b->device));
   if (b->multiEnabled == (on != 0)) return SHWFS_OK;
-  b->multiEnabled = on != 0;
   CK(cudaStreamSynchronize(b->cap));
-  return batch_capture(b);
+  b->multiEnabled = on != 0;
+  const shwfs_status s = batch_capture(b);
+  if (s) {
+    // keep a usable graph: back to the previous setting
+    const std::string err = g_err;
+    b->multiEnabled = !b->multiEnabled;
+    batch_capture(b);
+    g_err = err;
+  }
+  return s;
 }
 
 shwfs_status shwfs_batch_multi_launches(const shwfs_batch* b, int* n) {
