@@ -213,7 +213,8 @@ constexpr int kWarpMaxK = 16;      // subaperture-frames per chunk
 // drawn and the next one, copied in asynchronously), the chunk's item table
 // for both buffers (per item an int4 {subaperture, noise frame index,
 // Poisson flag, frame} and the 64-bit offset of its image in bimg), the
-// window-row partial sums of the centroids and the bright-pixel queue.
+// window-row partial sums of the centroids and the bright-pixel queue
+// (kWarpQ 16-bit indices into the chunk's buffer).
 __host__ __device__ inline int warp_smem_floats(int bufPx, int ncen) {
   return 2 * bufPx + 2 * 6 * kWarpMaxK + 2 * kWarpMaxK * ncen + kWarpQ / 2;
 }
