@@ -2154,7 +2154,8 @@ shwfs_status shwfs_batch_run(shwfs_batch* b, void* stream) {
   if (!b) return fail(SHWFS_ERR_INVALID, "null batch");
   CK(cudaSetDevice(b->device));
   cudaStream_t st = stream ? (cudaStream_t)stream : b->cap;
-  bool stale = false;
+  // no graph after a failed re-capture: capture again before launching
+  bool stale = b->exec == nullptr;
   for (size_t i = 0; i < b->hs.size(); i++) {
     if (shwfs_status s = batch_check(b->hs[i])) return s;
     stale |= b->versions[i] != b->hs[i]->version;
