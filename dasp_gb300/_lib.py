@@ -35,7 +35,7 @@ EXPORTS = ("shwfs_initialise", "shwfs_run", "shwfs_run_slope", "shwfs_update", "
            "shwfs_last_error", "shwfs_run_async", "shwfs_run_batch", "shwfs_set_io",
            "shwfs_get_info", "shwfs_version", "shwfs_image_centroids_noalloc",
            "shwfs_batch_create", "shwfs_batch_run", "shwfs_batch_free", "shwfs_batch_set_multi",
-           "shwfs_batch_multi_launches", "shwfs_autotune",
+           "shwfs_batch_multi_launches", "shwfs_autotune", "shwfs_gemm_stagings",
            "shwfs_sample_noise", "shwfs_set_split_event", "shwfs_server_create", "shwfs_server_add_system",
            "shwfs_server_remove_system", "shwfs_server_submit", "shwfs_server_poll", "shwfs_server_get_stats",
            "shwfs_server_clock", "shwfs_server_destroy", "shwfs_selftest_bounded_wait",
@@ -149,6 +149,8 @@ def lib() -> ctypes.CDLL:
         L.shwfs_batch_multi_launches.argtypes = [vp, P(ctypes.c_int)]
         L.shwfs_batch_set_multi.argtypes = [vp, ctypes.c_int]
         L.shwfs_autotune.argtypes = [vp, P(ctypes.c_int)]
+        L.shwfs_gemm_stagings.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          P(ctypes.c_int), ctypes.c_int, P(ctypes.c_int)]
         L.shwfs_set_split_event.argtypes = [vp, vp]
         L.shwfs_server_create.argtypes = [P(ShwfsServerConfig), P(vp)]
         L.shwfs_server_add_system.argtypes = [vp, P(ShwfsInit), ctypes.c_int, P(ctypes.c_int)]

@@ -80,6 +80,28 @@ def testcorrelation(img, corr):
           "testcorrelation")
 
 
+STAGING_FIELDS = ("cw", "noc", "kcb", "nkc", "dbuf", "dbuf_a2", "nk", "nw", "nd1", "k1", "n2", "smem", "tmem")
+
+
+def gemm_stagings(form, phasesize, crop, nimg):
+    """The GEMM kernel's stagings that fit a tensor-core ``form`` (a FORMS
+    name or code) for phasesize p, a ``crop`` x ``crop`` power spectrum (the
+    smaller of fftsize and the padded size) and nimg x nimg images, in the
+    order the GEMMSTAGING update code indexes them (the default first), as
+    dicts of STAGING_FIELDS.  Empty when the form cannot take the geometry
+    (the handle then keeps the FP32 form).  Host-only: needs no GPU."""
+    code = FORMS[form] if isinstance(form, str) else int(form)
+    L = _lib.lib()
+    n = ctypes.c_int(0)
+    check(L.shwfs_gemm_stagings(code, int(phasesize), int(crop), int(nimg), None, 0, ctypes.byref(n)),
+          "gemm_stagings")
+    k = len(STAGING_FIELDS)
+    rows = (ctypes.c_int * max(1, n.value * k))()
+    check(L.shwfs_gemm_stagings(code, int(phasesize), int(crop), int(nimg), rows, n.value, ctypes.byref(n)),
+          "gemm_stagings")
+    return [dict(zip(STAGING_FIELDS, rows[i * k:(i + 1) * k])) for i in range(n.value)]
+
+
 class centcmod:
     """Shack-Hartmann WFS engine handle with the ``util.centcmod`` interface."""
 

@@ -725,9 +725,16 @@ WfsArgs make_args(shwfs_handle* h, const float* phs, float* cents, float* bimg, 
   return a;
 }
 
+// operand format and split-product passes of a tensor-core form
+int form_fmt(int form) {
+  return form == SHWFS_FORM_FP16 ? kFmtFP16 : (form == SHWFS_FORM_TF32 ? kFmtTF32 : kFmtBF16);
+}
+int form_passes(int form) { return form == SHWFS_FORM_BF16X3 ? 3 : 1; }
+
 // GEMM-DFT form: eligibility and device constants.  Configurations outside the
 // GEMM kernel (per-subaperture PSFs, phase+amplitude, optical binning,
-// reference-stream noise, phasesize > 10, nimg > 16) run the FP32 form.
+// reference-stream noise, phasesize > 16, nimg > 16, no staging that fits
+// shared memory) run the FP32 form.
 bool gemm_static_ok(const shwfs_handle* h, GemmGeom* g, GemmSpec* sp) {
   if (h->psfDim == 4 || h->phaseAmp) return false;
   sp->p = h->phasesize;
@@ -745,8 +752,7 @@ bool gemm_static_ok(const shwfs_handle* h, GemmGeom* g, GemmSpec* sp) {
   sp->binT = h->binTHost;
   sp->binN = h->binNHost;
   sp->binIdx = h->binIdxHost;
-  const int fmt = h->form == SHWFS_FORM_FP16 ? kFmtFP16 : (h->form == SHWFS_FORM_TF32 ? kFmtTF32 : kFmtBF16);
-  return gemm_geometry(*sp, fmt, h->form == SHWFS_FORM_BF16X3 ? 3 : 1, g);
+  return gemm_geometry(*sp, form_fmt(h->form), form_passes(h->form), g);
 }
 
 bool gemm_active(const shwfs_handle* h) {
@@ -2289,6 +2295,40 @@ shwfs_status shwfs_autotune(shwfs_handle* h, int* best_tile) {
   }
   if (sp) return sp;
   if (best_tile) *best_tile = h->TS;
+  return SHWFS_OK;
+}
+
+shwfs_status shwfs_gemm_stagings(int form, int phasesize, int crop, int nimg, int* rows, int cap, int* n) {
+  if (!n || cap < 0 || (cap > 0 && !rows) || phasesize < 1 || crop < 1 || nimg < 1 || form < SHWFS_FORM_BF16 ||
+      form > SHWFS_FORM_TF32)
+    return fail(SHWFS_ERR_INVALID, "bad staging query arguments");
+  g_err.clear();
+  // the geometry depends on the phase, crop and image sizes only
+  GemmSpec sp{};
+  sp.p = phasesize;
+  sp.c = crop;
+  sp.m = nimg;
+  const std::vector<GemmGeom> cands = gemm_geometry_candidates(sp, form_fmt(form), form_passes(form));
+  *n = (int)cands.size();
+  for (int i = 0; i < cap && i < (int)cands.size(); i++) {
+    const GemmGeom& g = cands[i];
+    int* r = rows + (size_t)i * SHWFS_STAGING_FIELDS;
+    uint32_t tmem = gemm_d2_col(g) + (uint32_t)g.N2;
+    for (int b = 0; b < g.nd1; b++) tmem = std::max(tmem, gemm_d1_col(g, b) + 2u * (uint32_t)g.CW);
+    r[SHWFS_STG_CW] = g.CW;
+    r[SHWFS_STG_NOC] = g.noc;
+    r[SHWFS_STG_KCB] = g.KCB;
+    r[SHWFS_STG_NKC] = g.nkc;
+    r[SHWFS_STG_DBE] = g.dbE;
+    r[SHWFS_STG_DBA2] = g.dbA2;
+    r[SHWFS_STG_NK] = g.NK;
+    r[SHWFS_STG_NW] = g.NW;
+    r[SHWFS_STG_ND1] = g.nd1;
+    r[SHWFS_STG_K1] = g.K1;
+    r[SHWFS_STG_N2] = g.N2;
+    r[SHWFS_STG_SMEM] = gemm_smem_bytes(g);
+    r[SHWFS_STG_TMEM] = (int)tmem;
+  }
   return SHWFS_OK;
 }
 

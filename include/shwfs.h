@@ -355,6 +355,35 @@ shwfs_status shwfs_batch_multi_launches(const shwfs_batch* b, int* n);
  * see the same k-steps in the same order whatever the staging. */
 shwfs_status shwfs_autotune(shwfs_handle* h, int* best_tile);
 
+/* fields of one row of shwfs_gemm_stagings */
+enum {
+  SHWFS_STG_CW = 0,     /* complex outputs per GEMM1 output chunk (GEMM1 N = 2 CW) */
+  SHWFS_STG_NOC = 1,    /* GEMM1 output chunks covering the crop */
+  SHWFS_STG_KCB = 2,    /* GEMM1 K bytes per row of one streamed W2 chunk */
+  SHWFS_STG_NKC = 3,    /* W2 chunks per output chunk */
+  SHWFS_STG_DBE = 4,    /* 1: two field (GEMM1 A) buffers */
+  SHWFS_STG_DBA2 = 5,   /* 1: two |F|^2 (GEMM2 A) buffers */
+  SHWFS_STG_NK = 6,     /* Kc (GEMM2 B) ring stages */
+  SHWFS_STG_NW = 7,     /* W2 (GEMM1 B) ring stages */
+  SHWFS_STG_ND1 = 8,    /* GEMM1 accumulator buffers in tensor memory */
+  SHWFS_STG_K1 = 9,     /* GEMM1 K in elements */
+  SHWFS_STG_N2 = 10,    /* GEMM2 N (nimg^2 rounded up to 16) */
+  SHWFS_STG_SMEM = 11,  /* dynamic shared memory of a CTA, bytes */
+  SHWFS_STG_TMEM = 12,  /* tensor-memory columns used (end of the last accumulator) */
+  SHWFS_STAGING_FIELDS = 13
+};
+
+/* Host-only query (no GPU, no handle; no reference counterpart): the
+ * stagings of the GEMM kernel that fit for tensor-core form `form`
+ * (SHWFS_FORM_BF16 .. SHWFS_FORM_TF32), phasesize p, a crop x crop power
+ * spectrum (the smaller of fftsize and the padded size: clipsize, or the
+ * fftsize when pre-binning) and nimg x nimg
+ * images, the default first, in the order SHWFS_GEMMSTAGING indexes them.
+ * *n receives their number (0: the form cannot take this geometry and a
+ * handle keeps the FP32 form); the first min(*n, cap) are written to rows,
+ * SHWFS_STAGING_FIELDS ints each. */
+shwfs_status shwfs_gemm_stagings(int form, int phasesize, int crop, int nimg, int* rows, int cap, int* n);
+
 /* Timing aid (no reference counterpart): with a non-NULL CUDA event, every
  * readout of a tensor-core form records it on the launch stream between the
  * image-formation kernel and the noise/centroid kernel, so that a caller can
