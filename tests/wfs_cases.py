@@ -35,13 +35,13 @@ class Case:
             a = 1.0 + 0.2 * np.random.default_rng(phase_seed + 99).standard_normal((npup, npup))
             phs = np.ascontiguousarray(np.stack([phs, np.abs(a).astype(np.float32)]), dtype=np.float32)
         self.phs = np.ascontiguousarray(phs, dtype=np.float32)
-        if psf == "gauss":
+        if isinstance(psf, np.ndarray):
+            self.psf = psf
+        elif psf == "gauss":
             self.psf = gaussian_psf(self.P_default(), 1.5)
         elif psf == "gauss4d":
             frac = self.pup.getSubarea(nsubx) / (p * p)
             self.psf = lgs_psfs(nsubx, self.P_default(), 1.2, 6.0, subap_area=frac)
-        elif isinstance(psf, np.ndarray):
-            self.psf = psf
         else:
             self.psf = None
 
