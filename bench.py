@@ -821,6 +821,133 @@ def run_recon(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- AO loop on the device
+
+ATMOS = dict(layers=[  # Cn2 fraction, wind (pixels of 0.0527 m per frame: 10, 20, 30, 50 m/s at 1 kHz)
+    dict(frac=0.5, wind=0.19, seed=51), dict(frac=0.2, wind=0.38, seed=52),
+    dict(frac=0.2, wind=0.57, seed=53), dict(frac=0.1, wind=0.95, seed=54)], nacts=5316)
+
+
+def run_atmos(args):
+    """One AO-loop frame on the device, end to end, for the 74x74 sensor:
+    four frozen-flow layers advanced by their wind (infScrn's column
+    extrusion, science/infScrn.py:747-791, each layer's screen 741 x 742 px
+    in HBM), the sensor's 740x740 pupil phase from them (infAtmos'
+    createPupilPhs for a source at infinity, util/atmos.py:678-833: each
+    layer's window with linearshift's sub-pixel shift, piston removed,
+    scaled to 589 nm), the WFS frame in the FP16 form with Poisson and read
+    noise, and the reconstructor step (decay + MVM, 5,316 actuators over the
+    engine's 10,952-slope centroid vector, R 233 MB).  Every stage is queued
+    on one stream; nothing crosses the host link.  The loop rate is frames
+    over the events around the timed frames; the per-stage medians are
+    event intervals on the same stream (they include any wait for the
+    host's launches)."""
+    import torch
+    from dasp_gb300.infscreen import DeviceScreen, extrusion_matrices, phase_covariance, pupil_phase
+    from dasp_gb300.recon import Reconstructor
+    from dasp_gb300.screens import von_karman_screen
+    torch.cuda.set_device(0)
+    w = WORKLOAD
+    pup = make_pupil()
+    npup = w["nsubx"] * w["p"]
+    nsub = w["nsubx"] ** 2
+    ny, nx = npup + 1, npup + 2
+    scale = w["Dtel"] / npup
+    t0 = time.time()
+    ay, by = extrusion_matrices(ny, phase_covariance(ny, w["L0"], scale))
+    setup_s = time.time() - t0
+    layers = []
+    for ly in ATMOS["layers"]:
+        r0 = w["r0"] * ly["frac"] ** (-3. / 5)
+        init = von_karman_screen(nx, nx * scale, r0, w["L0"], ly["seed"], 500.0)[:ny, :nx]
+        layers.append(dict(ly, r0=r0, pos=0.0, screen=DeviceScreen(init, w["L0"], ay=ay, by=by, seed=ly["seed"])))
+    pupil_t = torch.from_numpy(pup.fn.astype(np.float32)).cuda()
+    area = float(pup.fn.sum())
+    dp = torch.zeros((npup, npup), device="cuda")
+    dc = torch.zeros(nsub * 2, device="cuda")
+    db = torch.zeros((nsub, w["m"], w["m"]), device="cuda")
+    hc = np.zeros(nsub * 2, np.float32)
+    hb = np.zeros((w["nsubx"], w["nsubx"], w["m"], w["m"]), np.float32)
+    eng = make_engine(pup, np.zeros((npup, npup), np.float32), hc, hb)
+    eng.set_form("fp16")
+    form = {0: "fp32", 1: "bf16", 2: "bf16x3", 3: "fp16", 4: "tf32"}[eng.info()["form_active"]]
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        pupil_phase([(ly["screen"], 0, 0, 0.0, 0.0) for ly in layers], pupil_t, dp, pupil_area=area,
+                    wavelength=w["wavelength"], stream=stream)
+    stream.synchronize()
+    eng.set_io(dp, dc, db)
+    eng.autotune()
+    rng = np.random.default_rng(2)
+    R = torch.from_numpy(rng.standard_normal((ATMOS["nacts"], nsub * 2), dtype=np.float32) * 1e-3).cuda()
+    rec = Reconstructor(R, 0.5, 0.99)
+    ncols = 0
+
+    def frame(ev=None):
+        nonlocal ncols
+        if ev:
+            ev[0].record(stream)
+        wins = []
+        for ly in layers:
+            ly["pos"] += ly["wind"]
+            k = int(ly["pos"])
+            if k:
+                ly["screen"].add_columns(k, ly["r0"], stream=stream)
+                ly["pos"] -= k
+                ncols += k
+            wins.append((ly["screen"], 0, 0, 0.0, float(ly["pos"])))
+        if ev:
+            ev[1].record(stream)
+        pupil_phase(wins, pupil_t, dp, pupil_area=area, wavelength=w["wavelength"], stream=stream)
+        if ev:
+            ev[2].record(stream)
+        eng.run_batch(dp.unsqueeze(0), dc.unsqueeze(0), db.unsqueeze(0), stream=stream)
+        if ev:
+            ev[3].record(stream)
+        rec.step(dc, stream=stream)
+        if ev:
+            ev[4].record(stream)
+
+    nframes = max(args.steps * 50, 500)
+    for _ in range(max(args.warmup, 3) * 10):
+        frame()
+    stream.synchronize()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(5)] for _ in range(nframes)]
+    ncols = 0
+    with ClockSampler(0) as clk:
+        with torch.cuda.stream(stream):
+            t0 = time.perf_counter()
+            for k in range(nframes):
+                frame(evs[k])
+            stream.synchronize()
+            wall = time.perf_counter() - t0
+    span_ms = evs[0][0].elapsed_time(evs[-1][4])
+    stage = lambda a, b: float(np.median([e[a].elapsed_time(e[b]) for e in evs]))  # noqa: E731
+    stages = {"screens_ms": stage(0, 1), "pupil_phase_ms": stage(1, 2), "wfs_ms": stage(2, 3),
+              "reconstructor_ms": stage(3, 4), "frame_ms": stage(0, 4)}
+    # a sanity check of the loop's output: finite slopes and commands
+    ok = bool(torch.isfinite(dc).all().item() and torch.isfinite(rec.act).all().item())
+    nlit = eng.info()["nlit"]
+    for ly in layers:
+        ly["screen"].free()
+    eng.free()
+    line = {
+        "metric": "AO-loop frames/s on the device (4 layers -> 74x74 pupil phase -> WFS -> reconstructor)",
+        "value": nframes / (span_ms / 1e3), "unit": "frames/s", "n_gpus": 1, "steps": nframes,
+        "warmup": max(args.warmup, 3) * 10, "ms_per_step": span_ms / nframes, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "screens f64 extrusion, f32 phase; WFS " + form,
+        "data": "synthetic: seeded von Karman layers (r0 0.157 m total, L0 25 m), seeded normal reconstructor",
+        "config": {"workload": "atmos_loop_74x74", "layers": [{k: ly[k] for k in ("frac", "wind", "r0")}
+                                                            for ly in layers],
+                   "screen_px": [ny, nx], "npup": npup, "lit_subaps": nlit, "nacts": ATMOS["nacts"],
+                   "columns_extruded": ncols, "matrix_setup_s": setup_s,
+                   "l2": "screens' extrusion matrices (53 MB) L2-resident; R (233 MB) larger than L2"},
+        "stages_median": stages, "wall_frames_per_s": nframes / wall, "finite": ok,
+        "clocks": clk.summary(), "gpu_launches": None,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_corr(args):
     """Correlation centroiding on the 74x74 sensor (noisy, Gaussian spot
     PSF): mode 1 (FFT correlation with a 20x20 pattern made by
@@ -971,12 +1098,13 @@ def main():
     ap.add_argument("--e2e-frames", type=int, default=1000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="ngs74",
-                    choices=["ngs74", "serving", "precision", "lgs_batch", "recon", "corr", "slope"],
+                    choices=["ngs74", "serving", "precision", "lgs_batch", "recon", "corr", "slope", "atmos"],
                     help="ngs74: the headline 74x74 NGS sensor; serving: 64 AO systems through the serving loop; "
                          "precision: per-form centroid error sweep vs the float64 oracle; "
                          "lgs_batch: 6 LGS + 3 NGS sensors in one CUDA graph; recon: the reconstructor step; "
                          "corr: correlation centroiding (modes 1 and 5) on the 74x74 sensor; "
-                         "slope: image input (runSlope) from a 740x740 detector frame")
+                         "slope: image input (runSlope) from a 740x740 detector frame; "
+                         "atmos: the AO loop on the device (layers, pupil phase, WFS, reconstructor)")
     ap.add_argument("--form", default=None, choices=["fp32", "fp16", "bf16x3", "tf32", "bf16"],
                     help="headline form (and the end-to-end run's) instead of the fastest within 1e-3 px; for "
                          "profiling runs, whose timings cannot choose")
@@ -988,12 +1116,12 @@ def main():
     ap.add_argument("--serve-inflight", type=int, default=16)
     args = ap.parse_args()
     ws, rank, local = dist_env()
-    if args.workload in ("serving", "precision", "lgs_batch", "recon", "corr", "slope") and args.impl == "ours":
+    if args.workload in ("serving", "precision", "lgs_batch", "recon", "corr", "slope", "atmos") and args.impl == "ours":
         if rank == 0:
             from dasp_gb300 import build
             build.build()
             {"serving": run_serving, "precision": run_precision, "lgs_batch": run_lgs_batch,
-             "recon": run_recon, "corr": run_corr, "slope": run_slope}[args.workload](args)
+             "recon": run_recon, "corr": run_corr, "slope": run_slope, "atmos": run_atmos}[args.workload](args)
         return
 
     if args.impl == "reference":

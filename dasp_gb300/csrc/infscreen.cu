@@ -108,6 +108,8 @@ struct LayerWin {
   float s1, s2, s3, s4;  // bilinear weights (1-x)(1-y), (1-x)y, x(1-y), xy
 };
 constexpr int kMaxLayers = 16;
+// threads per block of both pupil-phase kernels (their reductions assume it)
+constexpr int kPupilThreads = 256;
 struct LayerSet {
   LayerWin l[kMaxLayers];
   int n;
@@ -120,7 +122,7 @@ struct LayerSet {
 // and the result multiplied by the pupil and scaled (:818-833)
 __global__ void pupil_layers_kernel(const LayerSet L, int npup, float* __restrict__ out,
                                     const float* __restrict__ pfn, double* __restrict__ partial) {
-  __shared__ double red[256];
+  __shared__ double red[kPupilThreads];
   double acc = 0.0;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < (long long)npup * npup;
        k += (long long)gridDim.x * blockDim.x) {
@@ -152,12 +154,19 @@ __global__ void pupil_layers_kernel(const LayerSet L, int npup, float* __restric
 __global__ void pupil_finish_kernel(float* __restrict__ out, const float* __restrict__ pfn, long long n,
                                     const double* __restrict__ partial, int nparts, double area, int removePiston,
                                     float scale) {
+  // every block reduces the partial sums in the same order (a strided sum
+  // per thread, then a tree), so all blocks subtract the same piston
+  __shared__ double red[kPupilThreads];
   __shared__ float pist;
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int b = 0; b < nparts; b++) s += partial[b];
-    pist = removePiston ? (float)(s / area) : 0.f;
+  double s = 0.0;
+  for (int b = threadIdx.x; b < nparts; b += kPupilThreads) s += partial[b];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int st = kPupilThreads / 2; st; st >>= 1) {
+    if ((int)threadIdx.x < st) red[threadIdx.x] += red[threadIdx.x + st];
+    __syncthreads();
   }
+  if (threadIdx.x == 0) pist = removePiston ? (float)(red[0] / area) : 0.f;
   __syncthreads();
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
     out[k] = __fmul_rn(__fmul_rn(__fsub_rn(out[k], pist), pfn[k]), scale);
@@ -312,13 +321,14 @@ shwfs_status shwfs_screens_pupil_phase(shwfs_screen* const* screens, int nlayers
   }
   cudaStream_t st = stream ? (cudaStream_t)stream : screens[0]->stream;
   const long long n = (long long)npup * npup;
-  const int blocks = (int)std::min<long long>((n + 255) / 256, 1024);
+  const int blocks = (int)std::min<long long>((n + shwfs::kPupilThreads - 1) / shwfs::kPupilThreads, 1024);
   double* partial = nullptr;
   SCK(cudaMallocAsync((void**)&partial, (size_t)blocks * sizeof(double), st), "screens_pupil_phase");
-  shwfs::pupil_layers_kernel<<<blocks, 256, 0, st>>>(L, npup, out, pupil, partial);
+  shwfs::pupil_layers_kernel<<<blocks, shwfs::kPupilThreads, 0, st>>>(L, npup, out, pupil, partial);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) {
-    shwfs::pupil_finish_kernel<<<blocks, 256, 0, st>>>(out, pupil, n, partial, blocks, pupil_area, remove_piston, scale);
+    shwfs::pupil_finish_kernel<<<blocks, shwfs::kPupilThreads, 0, st>>>(out, pupil, n, partial, blocks, pupil_area,
+                                                                      remove_piston, scale);
     e = cudaGetLastError();
   }
   cudaFreeAsync(partial, st);

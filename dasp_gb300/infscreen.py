@@ -124,32 +124,41 @@ class DeviceScreen:
             mats["ax"], mats["bx"] = extrusion_matrices(nx, phase_covariance(nx, L0, pix_scale))
         return cls(big[:ny, :nx], L0, seed=seed, **mats)
 
-    def _add(self, axis, n, r0, step, noise):
+    def _add(self, axis, n, r0, step, noise, stream):
         coeff = (self.L0 / r0) ** (5. / 6)
         if noise is not None:
             noise = np.ascontiguousarray(noise, np.float64)
             if noise.size != n * self._check_noise_axis(axis):
                 raise ValueError("noise must hold n * (screen height or width) values")
+            if stream is not None:
+                # the host-to-device copies of the normals read the array
+                # after this call returns
+                raise ValueError("injected noise needs stream=None (the call waits for its copies)")
+        s = getattr(stream, "cuda_stream", stream)
         self._lib.check(self._lib.lib().shwfs_screen_add(self._s, axis, int(n), coeff, float(step),
-                                                         None if noise is None else noise.ctypes.data, None),
+                                                         None if noise is None else noise.ctypes.data, s),
                         "screen_add")
 
-    def add_columns(self, n, r0, step=0.0, noise=None):
-        self._add(0, n, r0, step, noise)
+    # With ``stream`` (torch stream or raw handle) the extrusions are queued
+    # there and not waited for; without, the call waits on the screen's own
+    # stream.
 
-    def add_rows(self, n, r0, step=0.0, noise=None):
-        self._add(1, n, r0, step, noise)
+    def add_columns(self, n, r0, step=0.0, noise=None, stream=None):
+        self._add(0, n, r0, step, noise, stream)
 
-    def add_columns_start(self, n, r0, step=0.0, noise=None):
+    def add_rows(self, n, r0, step=0.0, noise=None, stream=None):
+        self._add(1, n, r0, step, noise, stream)
+
+    def add_columns_start(self, n, r0, step=0.0, noise=None, stream=None):
         """n new columns at the start (the wind blowing the other way;
         addNewColumnOnStart, science/infScrn.py:793-823): the last column is
         dropped for each."""
-        self._add(2, n, r0, step, noise)
+        self._add(2, n, r0, step, noise, stream)
 
-    def add_rows_start(self, n, r0, step=0.0, noise=None):
+    def add_rows_start(self, n, r0, step=0.0, noise=None, stream=None):
         """n new rows at the start (addNewRowOnStart, science/infScrn.py:
         857-887)."""
-        self._add(3, n, r0, step, noise)
+        self._add(3, n, r0, step, noise, stream)
 
     def window(self, y0, x0, out, stream=None):
         """The out.shape[-2:] window at (y0, x0) into the CUDA tensor out."""
