@@ -914,13 +914,20 @@ def run_atmos(args):
     stream.synchronize()
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(5)] for _ in range(nframes)]
     ncols = 0
+    tq = []
     with ClockSampler(0) as clk:
         with torch.cuda.stream(stream):
             t0 = time.perf_counter()
             for k in range(nframes):
                 frame(evs[k])
+                if k < 33:
+                    tq.append(time.perf_counter())
             stream.synchronize()
             wall = time.perf_counter() - t0
+    # the host's time to queue one frame, over the first frames (before the
+    # launch queue fills and the host waits for the device): below the
+    # frame's event interval the device sets the rate, at it the host does
+    host_ms = float(np.median(np.diff(tq))) * 1e3
     span_ms = evs[0][0].elapsed_time(evs[-1][4])
     stage = lambda a, b: float(np.median([e[a].elapsed_time(e[b]) for e in evs]))  # noqa: E731
     stages = {"screens_ms": stage(0, 1), "pupil_phase_ms": stage(1, 2), "wfs_ms": stage(2, 3),
@@ -942,7 +949,8 @@ def run_atmos(args):
                    "screen_px": [ny, nx], "npup": npup, "lit_subaps": nlit, "nacts": ATMOS["nacts"],
                    "columns_extruded": ncols, "matrix_setup_s": setup_s,
                    "l2": "screens' extrusion matrices (53 MB) L2-resident; R (233 MB) larger than L2"},
-        "stages_median": stages, "wall_frames_per_s": nframes / wall, "finite": ok,
+        "stages_median": stages, "host_enqueue_ms_per_frame": host_ms, "wall_frames_per_s": nframes / wall,
+        "finite": ok,
         "clocks": clk.summary(), "gpu_launches": None,
     }
     print(json.dumps(line), flush=True)
