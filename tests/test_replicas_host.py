@@ -51,3 +51,13 @@ def test_reference_arm_runs_on_rank_zero_only():
     from oracle import ref_cent
     want = "reference" if ref_cent.available() else "port"
     assert d["impl"] == "reference" and d["value"] > 0 and d["cpu_baseline"]["kind"] == want
+    # the line keeps our arm's metric, unit and workload, and the contract's keys
+    import bench
+    assert d["metric"] == bench.METRIC and d["unit"] == bench.UNIT and d["higher_is_better"] is True
+    assert d["config"]["workload"] == bench.WORKLOAD["name"] and d["steps"] == 1 and d["warmup"] == 0
+    assert d["n_gpus"] == 2 and d["scaling"] == "weak" and d["vs_baseline"] is None
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["unit"] == bench.UNIT and cb["cores"] >= 1 and cb["sample"]
+    e2e = d["e2e"]
+    assert e2e == {"value": d["value"], "unit": bench.UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert d["ms_per_step"] > 0
