@@ -7,8 +7,10 @@
 array and the ``cents``/``bimg`` output arrays, then calls ``run`` every
 frame.  The arrays are borrowed exactly as the reference borrows them: the
 engine re-reads ``phs`` and overwrites ``cents``/``bimg`` in place on every
-readout frame.  They may be numpy arrays (host; copied to and from the GPU
-inside ``run``) or CUDA torch tensors (used in place).
+readout frame.  They may be numpy arrays (host: pinned in place so that the
+kernels read and write them through their device aliases during ``run``,
+or copied to and from the GPU where they cannot be pinned) or CUDA torch
+tensors (used in place).
 
 The work itself runs in hand-written sm_103a CUDA behind the C ABI of
 ``include/shwfs.h``; there is no CPU fallback.
@@ -21,7 +23,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import (NOISE_COUNTER, NOISE_REFERENCE, NOISEMODE, VAL_ARRAY, VAL_FLOAT, VAL_INT, VAL_NONE,
-                   VAL_TUPLE3, ShwfsArray, ShwfsInfo, ShwfsInit, ShwfsValue, as_array, check)
+                   VAL_TUPLE3, ShwfsInfo, ShwfsInit, ShwfsValue, as_array, check)
 
 CALSOURCE = 1
 SIG = 2

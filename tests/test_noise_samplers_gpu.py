@@ -5,8 +5,6 @@ exact Poisson pmf on both sides of every sampler boundary (modal inversion
 below lambda 64, PTRS transformed rejection above); normal draws by their
 moments and a binned chi-square test.  Each test fails with probability
 about 1e-6 for a correct sampler."""
-import ctypes
-
 import numpy as np
 import pytest
 

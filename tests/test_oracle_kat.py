@@ -4,7 +4,7 @@ streams, and known-answer properties of the reference's image formation
 import numpy as np
 import pytest
 
-from oracle.shwfs_oracle import (MT19937, PCG32, CentOracle, bin_image, bin_weights, flip_array, noise_lib,
+from oracle.shwfs_oracle import (MT19937, PCG32, bin_image, bin_weights, flip_array, noise_lib,
                                  philox4x32_10, tilt_fn)
 from tests.wfs_cases import Case
 
