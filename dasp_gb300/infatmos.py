@@ -32,9 +32,10 @@ frame; the device screens follow that counter.  (infScrn's own screen follows
 ``next``, which adds a line one frame earlier whenever the position is an
 integer; infAtmos receives it a frame later.)
 
-Sources at infinity only: the cone compression of LGS sources (a cubic-
-spline resampling of each layer, util/atmos.py:771-805) and uplink tip/tilt
-are not built, and neither are screens generated along one axis and rotated
+For an LGS each layer below it is seen through the cone's width and
+expanded to the pupil by the natural cubic spline DASP uses
+(gslCubSplineInterp, util/atmos.py:788-799); uplink tip/tilt is not built,
+and neither are screens generated along one axis and rotated
 (``rotateDirections``).  The reference's elliptical-pupil stretching for
 zenith angles is disabled in the reference itself (``zenithOld`` is always
 0), so windows are npup wide at every zenith angle.
@@ -271,28 +272,86 @@ class AtmosFrames:
         return plan
 
     def windows(self, idstr):
-        """Per layer, lowest first: (y0, x0, yshift, xshift) of the
-        (npup+1)-square window a source at infinity sees this frame -- its
-        static position (util/atmos.py:590-640) moved by the layer's
-        sub-pixel position (:696-720)."""
+        """The :class:`Window` of every layer the source sees this frame,
+        lowest first (util/atmos.py:590-640 for the static position, :696-720
+        for the sub-pixel motion).  A star at infinity sees every layer
+        through an npup-wide window; an LGS at height H sees only the layers
+        below it, each through the cone's width npup (1 - h/H) (rounded),
+        centred on its line of sight."""
         src = self.geom.sources[idstr]
-        if src.alt >= 0:
-            raise ValueError("only sources at infinity: the LGS cone projection is not built")
         npup = self.geom.npup
         xpos = np.tan(src.theta * _ARCSEC) * np.cos(src.phi * _DEG)
         ypos = np.tan(src.theta * _ARCSEC) * np.sin(src.phi * _DEG)
         out = []
-        for lf in self.layers:
+        for i, lf in enumerate(self.layers):
+            if not (src.alt < 0 or src.alt >= lf.height):
+                continue  # a layer above the LGS
             x = xpos * lf.height / self.scrn_scale - npup / 2 + self.xoff[lf.key]
             y = ypos * lf.height / self.scrn_scale - npup / 2 + self.yoff[lf.key]
             ny, nx = lf.shape
             if x < 0 or y < 0 or x + npup + 1 > nx or y + npup + 1 > ny:
                 raise ValueError("layer %r's screen does not contain source %r" % (lf.key, idstr))
+            width = npup
+            if src.alt > 0:
+                cone = npup * (1. - lf.height / src.alt)
+                x = x + (npup - cone) / 2
+                y = y + (npup - cone) / 2
+                width = int(cone + 0.5)
             col = (x - np.floor(x)) + _frame_shift(lf.col_add, lf.pos_col)
             row = (y - np.floor(y)) + _frame_shift(lf.row_add, lf.pos_row)
             dc, dr = int(np.floor(col)), int(np.floor(row))
-            out.append((int(y) + dr, int(x) + dc, float(row - dr), float(col - dc)))
+            out.append(Window(i, int(y) + dr, int(x) + dc, float(row - dr), float(col - dc), width))
         return out
+
+
+@dataclass(frozen=True)
+class Window:
+    """What one layer contributes to a source's pupil phase: the
+    (width+1)-square window of the layer's screen at row y0, column x0,
+    shifted by (yshift, xshift) in [0, 1) (linearshift) to width x width,
+    then, for an LGS (width < npup), expanded to npup x npup by a natural
+    cubic spline."""
+    layer: int     # index into AtmosFrames.layers (lowest first)
+    y0: int
+    x0: int
+    yshift: float
+    xshift: float
+    width: int
+
+
+def spline_matrix(width, npup):
+    """S (npup x width, float64) with S @ v the natural cubic spline through
+    (i, v[i]), i = 0 .. width-1, evaluated at i (width-1)/(npup-1),
+    i = 0 .. npup-1: the axes the reference hands to gslCubSplineInterp for
+    an LGS's cone (util/atmos.py:619-623, :788-799), whose spline is GSL's
+    ``gsl_interp_cspline`` (natural end conditions), applied along both axes
+    (cmod/src/interpmodule.c ``gslCubSplineIntrp``).  With unit knot spacing
+    the second derivatives m solve m[i-1] + 4 m[i] + m[i+1] = 6 (v[i+1] -
+    2 v[i] + v[i-1]) with m[0] = m[width-1] = 0, and on [i, i+1] at offset
+    t the spline is v[i] + b t + m[i]/2 t^2 + (m[i+1] - m[i])/6 t^3 with
+    b = v[i+1] - v[i] - (2 m[i] + m[i+1])/6 -- all linear in v."""
+    if width < 3:
+        raise ValueError("a cubic spline needs at least 3 points (cone width %d)" % width)
+    n = width
+    # m = M @ v: the tridiagonal solve applied to the second differences
+    d2 = np.zeros((n - 2, n))
+    for i in range(n - 2):
+        d2[i, i:i + 3] = (6., -12., 6.)
+    tri = np.diag(np.full(n - 2, 4.)) + np.diag(np.ones(n - 3), 1) + np.diag(np.ones(n - 3), -1)
+    mm = np.zeros((n, n))
+    mm[1:-1] = np.linalg.solve(tri, d2)
+    xs = np.arange(npup, dtype=np.float64) * ((width - 1) / float(npup - 1))
+    S = np.zeros((npup, n))
+    for r, x in enumerate(xs):
+        i = min(int(np.floor(x)), n - 2)  # the last point closes the last interval
+        t = x - i
+        e = np.zeros(n)
+        e[i], e[i + 1] = 1. - t, t          # v[i] + (v[i+1] - v[i]) t
+        # + m terms: -(2 m[i] + m[i+1])/6 t + m[i]/2 t^2 + (m[i+1] - m[i])/6 t^3
+        ci = -t / 3. + t * t / 2. - t ** 3 / 6.
+        cj = -t / 6. + t ** 3 / 6.
+        S[r] = e + ci * mm[i] + cj * mm[i + 1]
+    return S
 
 
 class DeviceAtmosphere:
@@ -344,18 +403,69 @@ class DeviceAtmosphere:
                 (scr.add_rows if row_end else scr.add_rows_start)(nrow, lf.r0, stream=stream)
 
     def windows(self, idstr):
-        """Per layer, lowest first: (screen, y0, x0, yshift, xshift), the
-        layer tuples of :func:`dasp_gb300.infscreen.pupil_phase`."""
-        return [(scr,) + w for scr, w in zip(self.screens, self.frames.windows(idstr))]
+        """Per layer the source sees, lowest first: (screen, y0, x0, yshift,
+        xshift), the layer tuples of :func:`dasp_gb300.infscreen.pupil_phase`."""
+        return [(self.screens[w.layer], w.y0, w.x0, w.yshift, w.xshift) for w in self.frames.windows(idstr)]
 
     def pupil_phase(self, idstr, pupil, out, pupil_area=None, remove_piston=True, stream=None):
-        """The source's pupil phase this frame into ``out`` (npup x npup CUDA
-        tensor): the layers' shifted windows summed lowest first, piston
-        removed over ``pupil``, times ``pupil`` and 500 / the source's
-        wavelength (util/atmos.py:678-833 for a source at infinity)."""
-        return self._pupil_phase(self.windows(idstr), pupil, out, pupil_area=pupil_area,
-                                 wavelength=self.geom.sources[idstr].lam, remove_piston=remove_piston,
-                                 stream=stream)
+        """The source's pupil phase this frame into ``out`` (npup x npup
+        float32 tensor on the device): the layers' shifted windows (for an LGS
+        each expanded from the cone's width to npup by the natural cubic
+        spline) summed lowest first, piston removed over ``pupil``, times
+        ``pupil`` and 500 / the source's wavelength (util/atmos.py:678-833).
+        A star's layers are summed in one pupil-phase kernel; an LGS's layers
+        go one at a time through that kernel (the shift) and two float32
+        library GEMMs (S W S^T, S from :func:`spline_matrix`; TF32 off, as
+        torch leaves it by default), the sum, piston and scaling in torch
+        on the same stream."""
+        src = self.geom.sources[idstr]
+        if src.alt < 0:
+            return self._pupil_phase(self.windows(idstr), pupil, out, pupil_area=pupil_area, wavelength=src.lam,
+                                     remove_piston=remove_piston, stream=stream)
+        return self._lgs_pupil_phase(idstr, pupil, out, pupil_area, remove_piston, stream)
+
+    def _lgs_pupil_phase(self, idstr, pupil, out, pupil_area, remove_piston, stream):
+        import contextlib
+
+        import torch
+        npup = self.geom.npup
+        dev = out.device
+        ctx = contextlib.nullcontext()
+        if stream is not None and dev.type == "cuda":
+            ts = stream if isinstance(stream, torch.cuda.Stream) else torch.cuda.ExternalStream(stream)
+            ctx = torch.cuda.stream(ts)
+        with ctx:
+            total = torch.zeros((npup, npup), dtype=torch.float32, device=dev)
+            for w in self.frames.windows(idstr):
+                tmp, ones, S = self._lgs_buffers(w.width, dev)
+                self._pupil_phase([(self.screens[w.layer], w.y0, w.x0, w.yshift, w.xshift)], ones, tmp,
+                                  pupil_area=1.0, wavelength=500.0, remove_piston=False, stream=stream)
+                # the ground layer spans the whole pupil: the spline through
+                # its own knots is the identity
+                total += tmp if S is None else torch.matmul(torch.matmul(S, tmp), S.t())
+            p = pupil.to(torch.float32)
+            scale = np.float32(500.0 / self.geom.sources[idstr].lam)
+            if remove_piston:
+                area = p.double().sum() if pupil_area is None else float(pupil_area)
+                pist = ((total.double() * p.double()).sum() / area).to(torch.float32)
+                out.copy_((total - pist) * p * scale)
+            else:
+                out.copy_(total * p * scale)
+        return out
+
+    def _lgs_buffers(self, width, dev):
+        """(shifted window, unit pupil, spline matrix or None) for a cone
+        width, kept per width and device."""
+        import torch
+        cache = self.__dict__.setdefault("_lgs_cache", {})
+        key = (width, str(dev))
+        if key not in cache:
+            S = None
+            if width != self.geom.npup:
+                S = torch.from_numpy(spline_matrix(width, self.geom.npup).astype(np.float32)).to(dev)
+            cache[key] = (torch.empty((width, width), dtype=torch.float32, device=dev),
+                          torch.ones((width, width), dtype=torch.float32, device=dev), S)
+        return cache[key]
 
     def free(self):
         for scr in self.screens:

@@ -3,8 +3,10 @@
 The fixture pins dasp_gb300/infatmos.py to DASP's atmosphere bookkeeping:
 for a few atmospheres it holds the layer geometry (screen sizes, layer
 offsets, zenith-scaled layers and r0), the layers' wind steps, and for 30
-frames the lines each layer's screen gains and each source's window (start
-row / column and sub-pixel shifts) per layer.  They are computed by running
+frames the lines each layer's screen gains and each source's window per
+layer (start row / column, sub-pixel shifts, and the window's size: the
+pupil for a star, the cone's width at the layer for an LGS; none for a
+layer above the LGS).  They are computed by running
 the reference's code itself, read from the reference tree:
 
 * util/getNewCols.py: the ``getNewCols`` class (the file up to its
@@ -45,6 +47,10 @@ CASES = [
          layers={"a": (500., 30., 40., 1., 4), "b": (8000., 300., 8., 2., 5)},
          sources=[("sci", 20., 120., -1, 5.), ("gs", 45., 10., -1, 0.)],
          ntel=80, npup=80, tel_diam=8.0, r0=0.12, l0=30., zenith=30., zenith_az=10., tstep=0.005),
+    dict(name="lgs_cone_and_layer_above",
+         layers={"low": (0., 20., 12., 0.5, 8), "mid": (7000., 160., 18., 0.3, 9), "top": (95000., 70., 30., 0.2, 10)},
+         sources=[("lgs", 15., 60., 90000., 0.), ("lgs2", 0., 0., 90000., 0.), ("ngs", 25., 300., -1, 0.)],
+         ntel=64, npup=64, tel_diam=8.0, r0=0.14, l0=25., zenith=0., zenith_az=0., tstep=0.004),
     dict(name="integer_steps_ntel_differs",
          layers={"x": (0., 180., 50., 0.5, 6), "y": (6000., 270., 20., 0.5, 7)},
          sources=[("on", 0., 0., -1, 0.), ("off", 40., 300., -1, 0.)],
@@ -145,10 +151,14 @@ def run_case(ns, case):
             wins = []
             for k in keys:
                 pd = posd[s.idstr][k]
+                if len(pd) == 0:  # a layer above the source is not used
+                    wins.append(None)
+                    continue
                 sx, sy, pc, pr = ns["window"](wa, k, pd, ipc, ipr)
                 # rows start at pd[1] + phsShiftX, columns at pd[0] + phsShiftY;
-                # linearshift(phs, interpPosCol, interpPosRow): column then row shift
-                wins.append([int(pd[1] + sx), int(pd[0] + sy), float(pr), float(pc)])
+                # linearshift(phs, interpPosCol, interpPosRow): column then row
+                # shift; the window is pd[3] + 1 rows by pd[2] + 1 columns
+                wins.append([int(pd[1] + sx), int(pd[0] + sy), float(pr), float(pc), int(pd[3]), int(pd[2])])
             frame["windows"][s.idstr] = wins
         out["frames"].append(frame)
     # the counters themselves for a spread of steps, both methods

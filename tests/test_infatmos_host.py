@@ -6,9 +6,12 @@ tests/golden/make_atmos_golden.py from util/getNewCols.py, util/atmos.py and
 science/infAtmos.py): the getNewCols counters, the atmosphere geometry, the
 wind steps, and 30 frames of lines added and source windows.  Integers must
 match exactly and positions to 1e-12.  Beyond the fixture: the window a
-source sees moves with the wind by exactly the step per frame, and
-DeviceAtmosphere applies the frame plan to its screens (fake screens here;
-the screen and pupil-phase kernels have their own GPU tests).
+source sees moves with the wind by exactly the step per frame; the LGS
+spline matrix is the natural cubic spline (scipy); DeviceAtmosphere
+applies the frame plan to its screens; and its LGS pupil phase (cone
+windows, spline expansion, piston) agrees with a float64 restatement to
+2e-5 of the peak (host stand-ins for the screens and the shift kernel,
+which have their own GPU tests).
 """
 import json
 import os
@@ -16,7 +19,8 @@ import os
 import numpy as np
 import pytest
 
-from dasp_gb300.infatmos import AtmosFrames, AtmosGeom, DeviceAtmosphere, Layer, NewCols, Source, wind_steps
+from dasp_gb300.infatmos import (AtmosFrames, AtmosGeom, DeviceAtmosphere, Layer, NewCols, Source, spline_matrix,
+                                 wind_steps)
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "atmos_frames.json")
 with open(GOLDEN) as _fh:
@@ -63,8 +67,11 @@ def test_frames_match_reference(case):
         assert [[p[0], p[2]] for p in plan] == [frame["lines"][k] for k in keys]
         for sid, want in frame["windows"].items():
             got = fr.windows(sid)
-            assert [list(w[:2]) for w in got] == [w[:2] for w in want], sid
-            assert np.allclose([w[2:] for w in got], [w[2:] for w in want], rtol=0, atol=1e-12), sid
+            used = [i for i, w in enumerate(want) if w is not None]  # layers above an LGS are skipped
+            want = [want[i] for i in used]
+            assert [w.layer for w in got] == used, sid
+            assert [[w.y0, w.x0, w.width, w.width] for w in got] == [[w[0], w[1], w[4], w[5]] for w in want], sid
+            assert np.allclose([[w.yshift, w.xshift] for w in got], [w[2:4] for w in want], rtol=0, atol=1e-12), sid
 
 
 def test_window_moves_with_the_wind():
@@ -79,7 +86,7 @@ def test_window_moves_with_the_wind():
         moved = {lf.key: [0, 0] for lf in fr.layers}  # net lines added at the end, per axis
 
         def content(sid):
-            return [(w[1] + w[3] + moved[lf.key][0], w[0] + w[2] + moved[lf.key][1])
+            return [(w.x0 + w.xshift + moved[lf.key][0], w.y0 + w.yshift + moved[lf.key][1])
                     for lf, w in zip(fr.layers, fr.windows(sid))]
 
         start = {sid: content(sid) for sid in ("s", "o")}
@@ -93,13 +100,28 @@ def test_window_moves_with_the_wind():
                     assert v - v0 == pytest.approx(-n * lf.row_add, abs=1e-9), (trial, lf.key, n)
 
 
-def test_only_sources_at_infinity_and_distinct_heights():
-    g = AtmosGeom({"a": Layer(0., 0., 5., 1.)}, [Source("lgs", 10., 0., alt=90000.)], 32, 32, 2.0, 0.15, 20.)
-    with pytest.raises(ValueError, match="LGS"):
-        AtmosFrames(g, 0.002).windows("lgs")
+def test_lgs_cone_widths_and_distinct_heights():
+    g = AtmosGeom({"a": Layer(0., 0., 5., .5), "b": Layer(30000., 0., 5., .3), "c": Layer(95000., 0., 5., .2)},
+                  [Source("lgs", 10., 0., alt=90000.)], 32, 32, 2.0, 0.15, 20.)
+    wins = AtmosFrames(g, 0.002).windows("lgs")
+    assert [w.layer for w in wins] == [0, 1]  # the layer above the LGS is not seen
+    assert [w.width for w in wins] == [32, int(32 * (1 - 30000. / 90000.) + 0.5)]
+    with pytest.raises(ValueError, match="at least 3 points"):
+        spline_matrix(2, 32)
     g = AtmosGeom({"a": Layer(0., 0., 5., .5), "b": Layer(0., 90., 5., .5)}, [Source("s")], 32, 32, 2.0, 0.15, 20.)
     with pytest.raises(ValueError, match="distinct heights"):
         AtmosFrames(g, 0.002)
+
+
+def test_spline_matrix_is_the_natural_cubic_spline():
+    from scipy.interpolate import CubicSpline
+    rng = np.random.default_rng(0)
+    for width, npup in ((3, 10), (5, 8), (59, 64), (100, 740), (683, 740)):
+        S = spline_matrix(width, npup)
+        v = rng.standard_normal(width)
+        xs = np.arange(npup) * ((width - 1) / float(npup - 1))
+        want = CubicSpline(np.arange(width, dtype=float), v, bc_type="natural")(xs)
+        assert np.abs(S @ v - want).max() <= 1e-13 * max(1.0, np.abs(want).max())
 
 
 class _FakeScreen:
@@ -142,7 +164,79 @@ def test_device_atmosphere_applies_the_frame_plan():
         atm.pupil_phase("off", None, None)
         assert got["lam"] == 640.
         assert [w[0] for w in got["wins"]] == atm.screens
-        assert [w[1:] for w in got["wins"]] == ref.windows("off")
+        assert [w[1:] for w in got["wins"]] == [(w.y0, w.x0, w.yshift, w.xshift) for w in ref.windows("off")]
+
+
+class _MovingScreen:
+    """A host screen that moves as the device screen does: lines added at
+    one end push the others along (new lines are seeded normals)."""
+
+    def __init__(self, init, l0, ay, by, ax, bx, seed):
+        self.screen = np.array(init, np.float32)
+        self.rng = np.random.default_rng(seed)
+
+    def _line(self, n):
+        return self.rng.standard_normal(n).astype(np.float32)
+
+    def add_columns(self, n, r0, stream=None):
+        for _ in range(n):
+            self.screen = np.concatenate([self.screen[:, 1:], self._line(self.screen.shape[0])[:, None]], 1)
+
+    def add_columns_start(self, n, r0, stream=None):
+        for _ in range(n):
+            self.screen = np.concatenate([self._line(self.screen.shape[0])[:, None], self.screen[:, :-1]], 1)
+
+    def add_rows(self, n, r0, stream=None):
+        for _ in range(n):
+            self.screen = np.concatenate([self.screen[1:], self._line(self.screen.shape[1])[None]], 0)
+
+    def add_rows_start(self, n, r0, stream=None):
+        for _ in range(n):
+            self.screen = np.concatenate([self._line(self.screen.shape[1])[None], self.screen[:-1]], 0)
+
+
+def test_lgs_pupil_phase_composition_matches_a_host_restatement():
+    # the LGS path (shift of each layer's cone window, natural-spline
+    # expansion, sum, piston, pupil, scale) with host stand-ins for the
+    # screens and the shift kernel, torch on the CPU for the rest, against
+    # the same chain in float64 with scipy's natural cubic spline
+    import torch
+    from scipy.interpolate import CubicSpline
+
+    from dasp_gb300.tel import Pupil
+    from oracle import atmos_oracle
+
+    def host_pupil_phase(wins, pupil, out, pupil_area=None, wavelength=500., remove_piston=True, stream=None):
+        scr = [w[0].screen for w in wins]
+        lay = [(q,) + tuple(w[1:]) for q, w in enumerate(wins)]
+        res = atmos_oracle.pupil_phase(scr, lay, pupil.numpy(), pupil_area=pupil_area, wavelength=wavelength,
+                                       remove_piston=remove_piston)
+        out.copy_(torch.from_numpy(res))
+        return out
+
+    npup = 32
+    layers = {"a": Layer(0., 30., 14., .5, 1), "b": Layer(6000., 200., 22., .3, 2), "c": Layer(12000., 110., 9., .2, 3),
+              "d": Layer(95000., 0., 5., .1, 4)}
+    g = AtmosGeom(layers, [Source("lgs", 20., 45., alt=90000., lam=589.)], npup, npup, 2.0, 0.15, 20.)
+    atm = DeviceAtmosphere(g, 0.003, screen_factory=_MovingScreen, pupil_phase_fn=host_pupil_phase)
+    pup = Pupil(npup, npup / 2., npup / 2. * 0.2).fn.astype(np.float32)
+    out = torch.zeros((npup, npup))
+    for frame in range(6):
+        atm.advance()
+        atm.pupil_phase("lgs", torch.from_numpy(pup), out)
+        total = np.zeros((npup, npup))
+        for w in atm.frames.windows("lgs"):
+            win = atm.screens[w.layer].screen[w.y0:w.y0 + w.width + 1, w.x0:w.x0 + w.width + 1]
+            shifted = atmos_oracle.linearshift(win, w.xshift, w.yshift, w.width, w.width).astype(np.float64)
+            if w.width < npup:
+                knots, xs = np.arange(w.width, dtype=float), np.arange(npup) * ((w.width - 1) / float(npup - 1))
+                shifted = CubicSpline(knots, shifted, axis=0, bc_type="natural")(xs)
+                shifted = CubicSpline(knots, shifted, axis=1, bc_type="natural")(xs)
+            total += shifted
+        want = (total - (total * pup).sum() / pup.sum()) * pup * (500. / 589.)
+        got = out.numpy()
+        assert np.abs(got - want).max() <= 2e-5 * np.abs(want).max(), frame
+        assert len(atm.frames.windows("lgs")) == 3
 
 
 def test_fixture_regenerates_from_the_reference():
