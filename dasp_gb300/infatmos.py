@@ -239,7 +239,7 @@ class AtmosFrames:
     """The frame-by-frame bookkeeping of infAtmos for the layers of an
     :class:`AtmosGeom` (host only): per frame, how many columns and rows each
     layer's screen gains and at which end, and where each layer's window
-    lies for a source at infinity.  ``tstep`` is the frame time (s)."""
+    lies for a source.  ``tstep`` is the frame time (s)."""
 
     def __init__(self, geom, tstep):
         self.geom = geom
@@ -356,7 +356,8 @@ def spline_matrix(width, npup):
 
 class DeviceAtmosphere:
     """The layers of an :class:`AtmosGeom` as device screens driven by
-    :class:`AtmosFrames`, with the pupil phase of any source at infinity.
+    :class:`AtmosFrames`, with the pupil phase of any source (stars, and
+    LGSs with the cone effect).
 
     Each layer gets a (scrnYPxls+1) x (scrnXPxls+1) screen at the pupil pixel
     scale (tel_diam / npup), its initial phase from the FFT method (seeded
@@ -416,8 +417,10 @@ class DeviceAtmosphere:
         A star's layers are summed in one pupil-phase kernel; an LGS's layers
         go one at a time through that kernel (the shift) and two float32
         library GEMMs (S W S^T, S from :func:`spline_matrix`; TF32 off, as
-        torch leaves it by default), the sum, piston and scaling in torch
-        on the same stream."""
+        torch leaves it by default), the sum, piston and scaling in torch,
+        all on one stream.  With ``stream`` the work is queued there and not
+        waited for (extrude the screens on the same stream); without, it runs
+        on torch's current stream and the call waits, as a star's does."""
         src = self.geom.sources[idstr]
         if src.alt < 0:
             return self._pupil_phase(self.windows(idstr), pupil, out, pupil_area=pupil_area, wavelength=src.lam,
@@ -430,16 +433,22 @@ class DeviceAtmosphere:
         import torch
         npup = self.geom.npup
         dev = out.device
-        ctx = contextlib.nullcontext()
-        if stream is not None and dev.type == "cuda":
-            ts = stream if isinstance(stream, torch.cuda.Stream) else torch.cuda.ExternalStream(stream)
-            ctx = torch.cuda.stream(ts)
+        ctx, ks = contextlib.nullcontext(), stream
+        if dev.type == "cuda":
+            # the shift kernels, the GEMMs and the element-wise steps share one
+            # stream (the given one, else torch's current stream), so that a
+            # kernel never overwrites a window buffer a pending GEMM still reads
+            if stream is None:
+                ks = torch.cuda.current_stream(dev)
+            elif not isinstance(stream, torch.cuda.Stream):
+                ks = torch.cuda.ExternalStream(stream)
+            ctx = torch.cuda.stream(ks)
         with ctx:
             total = torch.zeros((npup, npup), dtype=torch.float32, device=dev)
             for w in self.frames.windows(idstr):
                 tmp, ones, S = self._lgs_buffers(w.width, dev)
                 self._pupil_phase([(self.screens[w.layer], w.y0, w.x0, w.yshift, w.xshift)], ones, tmp,
-                                  pupil_area=1.0, wavelength=500.0, remove_piston=False, stream=stream)
+                                  pupil_area=1.0, wavelength=500.0, remove_piston=False, stream=ks)
                 # the ground layer spans the whole pupil: the spline through
                 # its own knots is the identity
                 total += tmp if S is None else torch.matmul(torch.matmul(S, tmp), S.t())
@@ -451,6 +460,10 @@ class DeviceAtmosphere:
                 out.copy_((total - pist) * p * scale)
             else:
                 out.copy_(total * p * scale)
+        if stream is None and dev.type == "cuda":
+            # as every screen call without a stream: the result is ready on
+            # return, and the screens may be extruded again at once
+            ks.synchronize()
         return out
 
     def _lgs_buffers(self, width, dev):
