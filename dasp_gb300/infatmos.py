@@ -157,6 +157,28 @@ class AtmosGeom:
             self.sources.setdefault(s.idstr, s)
         self.ntel, self.npup, self.tel_diam = int(ntel), int(npup), float(tel_diam)
 
+    @classmethod
+    def from_reference(cls, g, default_lam=500.):
+        """The geometry of a reference ``util.atmos.geom`` object (duck-typed:
+        ``layerDict``, ``sourceOrder``/``sourceDict``, ``ntel``, ``npup``,
+        ``telDiam``, ``r0``, ``l0``, ``zenith``, ``zenithAz``), as a parameter
+        file builds it.  That object has already scaled its layers, LGS
+        heights and r0 for its zenith angle and normalised the strengths,
+        so they are taken as they are.  A source's wavelength is its
+        ``sourcelam`` (science/infAtmos.py:245), else ``default_lam``."""
+        obj = cls({}, [], g.ntel, g.npup, g.telDiam, 1.0, g.l0)
+        obj.zenith, obj.zenith_az = float(g.zenith), float(getattr(g, "zenithAz", 0.))
+        obj.r0 = g.r0
+        obj.layers = {k: Layer(float(ly.height), float(ly.direction), float(ly.speed), float(ly.strength),
+                               int(getattr(ly, "seed", 0) or 0)) for k, ly in g.layerDict.items()}
+        order = getattr(g, "sourceOrder", None) or list(g.sourceDict)
+        for k in order:
+            s = g.sourceDict[k]
+            lam = getattr(s, "sourcelam", None)
+            obj.sources[s.idstr] = Source(s.idstr, float(s.theta), float(s.phi), float(s.alt),
+                                          float(getattr(s, "fov", 0.) or 0.), float(lam if lam else default_lam))
+        return obj
+
     def layer_r0(self, key):
         """r0 of one layer: r0 * strength^(-3/5) (science/infScrn.py:272, :411-420)."""
         return self.r0 * self.layers[key].strength ** (-3. / 5)

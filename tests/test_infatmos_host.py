@@ -244,3 +244,51 @@ def test_fixture_regenerates_from_the_reference():
     if not os.path.exists(os.path.join(mk.REF, "util", "getNewCols.py")):
         pytest.skip("reference sources not available")
     assert json.loads(json.dumps(mk.build(), sort_keys=True)) == DATA
+
+
+def _reference_geom(case):
+    """The reference's own util.atmos.geom object for a fixture case (its
+    classes run as the fixture generator runs them)."""
+    from tests.golden import make_atmos_golden as mk
+    if not os.path.exists(os.path.join(mk.REF, "util", "atmos.py")):
+        pytest.skip("reference sources not available")
+    ns = mk.reference_code()
+    layers = {k: ns["layer"](*v) for k, v in case["layers"].items()}
+    sources = [ns["source"](s[0], s[1], s[2], s[3], sourcelam=500. + 50 * i, fov=s[4])
+               for i, s in enumerate(case["sources"])]
+    return ns["geom"](layers, sources, case["ntel"], case["npup"], case["tel_diam"], case["r0"], case["l0"],
+                      zenith=case["zenith"], zenithAz=case["zenith_az"])
+
+
+@pytest.mark.parametrize("name", ["zenith_fast_wind_fov", "lgs_cone_and_layer_above"])
+def test_geometry_from_a_reference_geom_object(name):
+    case = next(c for c in CASES if c["name"] == name)
+    ref = _reference_geom(case)
+    g = AtmosGeom.from_reference(ref)
+    mine = _geom(case)
+    assert g.r0 == mine.r0 and (g.zenith, g.zenith_az) == (mine.zenith, mine.zenith_az)
+    assert g.layer_offsets() == mine.layer_offsets()
+    for k in case["layers"]:
+        assert g.screen_size(k) == mine.screen_size(k)
+        for f in ("height", "speed", "direction", "strength", "seed"):
+            assert getattr(g.layers[k], f) == pytest.approx(getattr(mine.layers[k], f), rel=1e-12)
+    assert list(g.sources) == [s[0] for s in case["sources"]]
+    assert [g.sources[s[0]].lam for s in case["sources"]] == [500. + 50 * i for i in range(len(case["sources"]))]
+    for sid in g.sources:
+        assert g.sources[sid].alt == mine.sources[sid].alt
+    # the same frames follow from either
+    a, b = AtmosFrames(g, case["tstep"]), AtmosFrames(mine, case["tstep"])
+    for _ in range(5):
+        assert a.advance() == b.advance()
+        for sid in g.sources:
+            assert a.windows(sid) == b.windows(sid)
+
+
+def test_geometry_from_a_duck_typed_geom():
+    import types
+    ly = types.SimpleNamespace(height=1000., direction=90., speed=12., strength=1., seed=4)
+    src = types.SimpleNamespace(idstr="s", theta=10., phi=20., alt=-1, fov=0., sourcelam=None)
+    ref = types.SimpleNamespace(layerDict={"l": ly}, sourceDict={"s": src}, ntel=32, npup=32, telDiam=2.,
+                                r0=0.12, l0=20., zenith=0.)
+    g = AtmosGeom.from_reference(ref, default_lam=640.)
+    assert g.sources["s"].lam == 640. and g.layers["l"].seed == 4 and g.r0 == 0.12 and g.zenith_az == 0.
