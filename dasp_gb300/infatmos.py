@@ -430,7 +430,7 @@ class DeviceAtmosphere:
         xshift), the layer tuples of :func:`dasp_gb300.infscreen.pupil_phase`."""
         return [(self.screens[w.layer], w.y0, w.x0, w.yshift, w.xshift) for w in self.frames.windows(idstr)]
 
-    def pupil_phase(self, idstr, pupil, out, pupil_area=None, remove_piston=True, stream=None):
+    def pupil_phase(self, idstr, pupil, out, pupil_area=None, remove_piston=True, stream=None, intrinsic=None):
         """The source's pupil phase this frame into ``out`` (npup x npup
         float32 tensor on the device): the layers' shifted windows (for an LGS
         each expanded from the cone's width to npup by the natural cubic
@@ -442,14 +442,18 @@ class DeviceAtmosphere:
         torch leaves it by default), the sum, piston and scaling in torch,
         all on one stream.  With ``stream`` the work is queued there and not
         waited for (extrude the screens on the same stream); without, it runs
-        on torch's current stream and the call waits, as a star's does."""
+        on torch's current stream and the call waits, as a star's does.
+        ``intrinsic`` (npup x npup tensor on the device, radians at 500 nm) is
+        a static phase the sum starts from, before the piston removal and the
+        scaling (infAtmos' intrinsicPhase, util/atmos.py:685-688); with it a
+        star's layers also go one at a time."""
         src = self.geom.sources[idstr]
-        if src.alt < 0:
+        if src.alt < 0 and intrinsic is None:
             return self._pupil_phase(self.windows(idstr), pupil, out, pupil_area=pupil_area, wavelength=src.lam,
                                      remove_piston=remove_piston, stream=stream)
-        return self._lgs_pupil_phase(idstr, pupil, out, pupil_area, remove_piston, stream)
+        return self._composed_pupil_phase(idstr, pupil, out, pupil_area, remove_piston, stream, intrinsic)
 
-    def _lgs_pupil_phase(self, idstr, pupil, out, pupil_area, remove_piston, stream):
+    def _composed_pupil_phase(self, idstr, pupil, out, pupil_area, remove_piston, stream, intrinsic):
         import contextlib
 
         import torch
@@ -466,7 +470,10 @@ class DeviceAtmosphere:
                 ks = torch.cuda.ExternalStream(stream)
             ctx = torch.cuda.stream(ks)
         with ctx:
-            total = torch.zeros((npup, npup), dtype=torch.float32, device=dev)
+            if intrinsic is None:
+                total = torch.zeros((npup, npup), dtype=torch.float32, device=dev)
+            else:
+                total = intrinsic.to(device=dev, dtype=torch.float32).clone()
             for w in self.frames.windows(idstr):
                 tmp, ones, S = self._lgs_buffers(w.width, dev)
                 self._pupil_phase([(self.screens[w.layer], w.y0, w.x0, w.yshift, w.xshift)], ones, tmp,

@@ -237,6 +237,18 @@ def test_lgs_pupil_phase_composition_matches_a_host_restatement():
         got = out.numpy()
         assert np.abs(got - want).max() <= 2e-5 * np.abs(want).max(), frame
         assert len(atm.frames.windows("lgs")) == 3
+    # an intrinsic phase is summed first, then piston-removed and scaled
+    # with the layers (a star's layers then go one at a time too)
+    intr = np.outer(np.linspace(-1, 1, npup), np.ones(npup)).astype(np.float32) * 3.0
+    g2 = AtmosGeom({"a": Layer(0., 30., 14., .6, 1), "b": Layer(6000., 200., 22., .4, 2)},
+                   [Source("ngs", 10., 20.)], npup, npup, 2.0, 0.15, 20.)
+    atm2 = DeviceAtmosphere(g2, 0.003, screen_factory=_MovingScreen, pupil_phase_fn=host_pupil_phase)
+    atm2.advance()
+    plain = atm2.pupil_phase("ngs", torch.from_numpy(pup), torch.zeros((npup, npup))).numpy().copy()
+    with_i = atm2.pupil_phase("ngs", torch.from_numpy(pup), torch.zeros((npup, npup)),
+                              intrinsic=torch.from_numpy(intr)).numpy()
+    extra = (intr - (intr * pup).sum() / pup.sum()) * pup
+    assert np.abs(with_i - plain - extra).max() <= 2e-5 * np.abs(plain).max()
 
 
 def test_fixture_regenerates_from_the_reference():
