@@ -394,6 +394,7 @@ class DeviceAtmosphere:
         self.frames = AtmosFrames(geom, tstep)
         self.geom = geom
         self._pupil_phase = pupil_phase_fn or infscreen.pupil_phase
+        self._lgs_cache = {}  # (cone width, device) -> (window, unit pupil, spline matrix)
         factory = screen_factory or (lambda init, l0, ay, by, ax, bx, seed: infscreen.DeviceScreen(
             init, l0, ay=ay, by=by, ax=ax, bx=bx, seed=seed))
         pix = self.frames.pix_scale
@@ -499,7 +500,7 @@ class DeviceAtmosphere:
         """(shifted window, unit pupil, spline matrix or None) for a cone
         width, kept per width and device."""
         import torch
-        cache = self.__dict__.setdefault("_lgs_cache", {})
+        cache = self._lgs_cache
         key = (width, str(dev))
         if key not in cache:
             S = None
